@@ -1,0 +1,181 @@
+// ibl_context.cu -- the bake context of include/althea_ibl.h: the GB300
+// counterpart of ImageBasedLighting::createResources / precomputeResources
+// (Src/ImageBasedLighting.cpp:137-412,415-605).  The env map stays resident
+// on the device with its full mip chain; a bake writes irradiance, every
+// prefiltered mip and (optionally) the BRDF LUT into caller-owned buffers,
+// stream ordered, with no host synchronisation (the reference blocks on
+// vkQueueWaitIdle, Src/SingleTimeCommandBuffer.cpp:28-54).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+
+#include "althea_ibl.h"
+#include "ibl_internal.h"
+
+using namespace ibl;
+
+struct althea_ibl_context {
+  althea_ibl_config cfg;
+  int device;
+  int irr_w, irr_h;
+  int mip_w[ALTHEA_IBL_MAX_MIPS], mip_h[ALTHEA_IBL_MAX_MIPS];
+  float mip_r[ALTHEA_IBL_MAX_MIPS];
+  float* chain;
+  size_t chain_texels;
+  void* irr_ws;
+  size_t irr_ws_bytes;
+  bool env_ready;
+};
+
+extern "C" void althea_ibl_config_reference(althea_ibl_config* c, int w, int h) {
+  if (!c) return;
+  memset(c, 0, sizeof(*c));
+  c->env_width = w;
+  c->env_height = h;
+  c->irradiance_width = w;   // Src/ImageBasedLighting.cpp:208-210
+  c->irradiance_height = h;
+  c->mip_count = 5;          // :184,192
+  c->first_mip_width = w >> 1;
+  c->first_mip_height = h >> 1;
+  c->samples = 10000;        // PreFilterEnvMap.comp:5
+  c->generator = ALTHEA_IBL_GEN_REF_HASH;
+  c->lut_size = 0;           // the reference loads brdf_lut.png instead
+  c->lut_samples = 1024;
+  c->lut_orientation = ALTHEA_IBL_LUT_ASSET;
+}
+
+extern "C" int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_context** out) {
+  if (!cfg || !out) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  int st = check_env(cfg->env_width, cfg->env_height);
+  if (st) return st;
+  althea_ibl_context* c = new (std::nothrow) althea_ibl_context();
+  if (!c) return set_error(ALTHEA_IBL_ERR_OUT_OF_MEMORY, "host allocation");
+  c->cfg = *cfg;
+  const int w = cfg->env_width, h = cfg->env_height;
+  c->irr_w = cfg->irradiance_width > 0 ? cfg->irradiance_width : w;
+  c->irr_h = cfg->irradiance_height > 0 ? cfg->irradiance_height : h;
+  if (cfg->mip_count < 1 || cfg->mip_count > ALTHEA_IBL_MAX_MIPS) {
+    delete c;
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "mip_count %d outside 1..%d",
+                     cfg->mip_count, ALTHEA_IBL_MAX_MIPS);
+  }
+  int fw = cfg->first_mip_width > 0 ? cfg->first_mip_width : (w >> 1);
+  int fh = cfg->first_mip_height > 0 ? cfg->first_mip_height : (h >> 1);
+  if (fw < 1) fw = 1;
+  if (fh < 1) fh = 1;
+  for (int m = 0; m < cfg->mip_count; ++m) {
+    c->mip_w[m] = (fw >> m) < 1 ? 1 : (fw >> m);
+    c->mip_h[m] = (fh >> m) < 1 ? 1 : (fh >> m);
+    // static_cast<float>(i) / 4.0f for 5 mips (Src/ImageBasedLighting.cpp:383)
+    c->mip_r[m] = cfg->mip_count > 1 ? (float)m / (float)(cfg->mip_count - 1) : 0.0f;
+  }
+  if (cfg->samples < 1 || cfg->samples > (1 << 24) ||
+      (cfg->generator != ALTHEA_IBL_GEN_REF_HASH && cfg->generator != ALTHEA_IBL_GEN_HAMMERSLEY)) {
+    delete c;
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "samples/generator");
+  }
+  if (cfg->lut_size < 0 || cfg->lut_size > 16384 ||
+      (cfg->lut_size > 0 && (cfg->lut_samples < 1 || cfg->lut_samples > (1 << 24)))) {
+    delete c;
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "lut_size/lut_samples");
+  }
+  st = check_irradiance_args(w, h, c->irr_w, c->irr_h);
+  if (st) {
+    delete c;
+    return st;
+  }
+  cudaGetDevice(&c->device);
+  c->chain_texels = althea_ibl_chain_texels(w, h);
+  c->irr_ws_bytes = irr_plan(w, h, c->irr_w, c->irr_h).workspace;
+  cudaError_t e = cudaMalloc(&c->chain, c->chain_texels * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&c->irr_ws, c->irr_ws_bytes);
+  if (e != cudaSuccess) {
+    if (c->chain) cudaFree(c->chain);
+    delete c;
+    return cuda_status(e, "context allocation");
+  }
+  *out = c;
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_destroy(althea_ibl_context* c) {
+  if (!c) return ALTHEA_IBL_OK;
+  cudaFree(c->chain);
+  cudaFree(c->irr_ws);
+  delete c;
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_mip_info(const althea_ibl_context* c, int m, int* w, int* h, float* r) {
+  if (!c || m < 0 || m >= c->cfg.mip_count)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "mip index");
+  if (w) *w = c->mip_w[m];
+  if (h) *h = c->mip_h[m];
+  if (r) *r = c->mip_r[m];
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_irradiance_size(const althea_ibl_context* c, int* w, int* h) {
+  if (!c) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null context");
+  if (w) *w = c->irr_w;
+  if (h) *h = c->irr_h;
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" const float* althea_ibl_env_chain(const althea_ibl_context* c) {
+  return c ? c->chain : nullptr;
+}
+
+extern "C" int althea_ibl_upload_env(althea_ibl_context* c, const float* rgba, int src_is_device,
+                                     void* stream) {
+  if (!c || !rgba) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  size_t bytes = (size_t)c->cfg.env_width * c->cfg.env_height * 16;
+  cudaError_t e = cudaMemcpyAsync(c->chain, rgba, bytes,
+                                  src_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  st);
+  if (e != cudaSuccess) return cuda_status(e, "env upload");
+  int r = launch_build_chain(c->chain, c->cfg.env_width, c->cfg.env_height, c->chain, st);
+  if (r == ALTHEA_IBL_OK) c->env_ready = true;
+  return r;
+}
+
+extern "C" int althea_ibl_bake(althea_ibl_context* c, const althea_ibl_outputs* o, void* stream) {
+  if (!c || !o) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
+  if (!c->env_ready)
+    return set_error(ALTHEA_IBL_ERR_NOT_READY, "no environment map uploaded to this context");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int w = c->cfg.env_width, h = c->cfg.env_height;
+  int r = check_image(o->irradiance_dev, c->irr_w, c->irr_h, o->irradiance_pitch_bytes, 16,
+                      "irradiance");
+  if (r) return r;
+  althea_ibl_mip_target mips[ALTHEA_IBL_MAX_MIPS];
+  for (int m = 0; m < c->cfg.mip_count; ++m) {
+    mips[m].out_dev = o->mip_dev[m];
+    mips[m].pitch_bytes = o->mip_pitch_bytes[m];
+    mips[m].width = c->mip_w[m];
+    mips[m].height = c->mip_h[m];
+    mips[m].roughness = c->mip_r[m];
+    r = check_image(mips[m].out_dev, mips[m].width, mips[m].height, mips[m].pitch_bytes, 16,
+                    "prefiltered mip");
+    if (r) return r;
+  }
+  if (c->cfg.lut_size > 0) {
+    r = check_image(o->lut_dev, c->cfg.lut_size, c->cfg.lut_size, o->lut_pitch_bytes, 8, "lut");
+    if (r) return r;
+  }
+  // Src/ImageBasedLighting.cpp:315-343: irradiance dispatch; :353-395: one
+  // prefilter dispatch per mip (here one launch for the whole chain).
+  r = launch_prefilter(c->chain, w, h, mips, c->cfg.mip_count, c->cfg.samples,
+                       c->cfg.generator, st);
+  if (r) return r;
+  r = launch_irradiance(c->chain, w, h, o->irradiance_dev, c->irr_w, c->irr_h,
+                        o->irradiance_pitch_bytes, c->irr_ws, st);
+  if (r) return r;
+  if (c->cfg.lut_size > 0)
+    r = launch_brdf_lut(o->lut_dev, c->cfg.lut_size, o->lut_pitch_bytes, c->cfg.lut_samples,
+                        c->cfg.lut_orientation, st);
+  return r;
+}

@@ -1,0 +1,38 @@
+// ibl_internal.h -- declarations shared between the translation units of
+// libalthea_ibl.so (not part of the public C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+#include "althea_ibl.h"
+
+namespace ibl {
+
+struct IrrPlan {
+  int phi;       // int(300 * H / W)
+  int tiles_x;   // 8-texel-wide tiles per row
+  int tiles;     // 8x4 tiles in the output
+  int gb;        // 256-thread blocks per tile
+  size_t workspace;
+};
+
+int set_error(int status, const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* what);
+const char* last_error();
+
+int check_env(int w, int h);
+int check_image(const void* p, int w, int h, size_t pitch, size_t texel_bytes, const char* what);
+int check_irradiance_args(int w, int h, int ow, int oh);
+IrrPlan irr_plan(int w, int h, int ow, int oh);
+
+int launch_build_chain(const float* level0, int w, int h, float* chain, cudaStream_t st);
+int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
+                     int mip_count, int samples, int generator, cudaStream_t st);
+int launch_irradiance(const float* chain, int w, int h, float* out, int ow, int oh,
+                      size_t pitch_bytes, void* ws, cudaStream_t st);
+int launch_brdf_lut(float* out, int n, size_t pitch_bytes, int samples, int orientation,
+                    cudaStream_t st);
+
+}  // namespace ibl

@@ -1,0 +1,604 @@
+// ibl_plain.cu -- plain (reference-estimator) IBL kernels for sm_103a and the
+// stateless C-ABI entry points of include/althea_ibl.h.
+//
+// Compiled with -fmad=false (see ibl_device.cuh): outputs equal the CPU
+// restatement of the reference shaders bit for bit, except the irradiance sum,
+// which is split across threads (tree order instead of serial order; ~1e-7).
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "althea_ibl.h"
+#include "ibl_device.cuh"
+#include "ibl_internal.h"
+
+namespace ibl {
+
+// ---------------------------------------------------------------------------
+// Error reporting shared by every entry point.
+// ---------------------------------------------------------------------------
+static thread_local char g_last_error[512] = "";
+
+int set_error(int status, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+int cuda_status(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return ALTHEA_IBL_OK;
+  int st = e == cudaErrorMemoryAllocation ? ALTHEA_IBL_ERR_OUT_OF_MEMORY : ALTHEA_IBL_ERR_CUDA;
+  return set_error(st, "%s: %s", what, cudaGetErrorString(e));
+}
+
+const char* last_error() { return g_last_error; }
+
+// ---------------------------------------------------------------------------
+// Mip chain: vkCmdBlitImage(VK_FILTER_LINEAR) per level (Src/Image.cpp:184-213).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) blit_level_kernel(const float4* __restrict__ src, int sw,
+                                                         int sh, float4* __restrict__ dst, int dw,
+                                                         int dh) {
+  int x = blockIdx.x * 32 + (threadIdx.x & 31);
+  int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (x >= dw || y >= dh) return;
+  float kx = (float)sw / (float)dw, ky = (float)sh / (float)dh;
+  float u = ((float)x + 0.5f) * kx - 0.5f;
+  float v = ((float)y + 0.5f) * ky - 0.5f;
+  float fx = floorf(u), fy = floorf(v);
+  float a = u - fx, b = v - fy;
+  int i0 = min(max((int)fx, 0), sw - 1), i1 = min(max((int)fx + 1, 0), sw - 1);
+  int j0 = min(max((int)fy, 0), sh - 1), j1 = min(max((int)fy + 1, 0), sh - 1);
+  const float4* r0 = src + (long long)j0 * sw;
+  const float4* r1 = src + (long long)j1 * sw;
+  float4 t00 = __ldg(r0 + i0), t10 = __ldg(r0 + i1), t01 = __ldg(r1 + i0), t11 = __ldg(r1 + i1);
+  float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b);
+  float w01 = (1.0f - a) * b, w11 = a * b;
+  float4 o;
+  o.x = ((w00 * t00.x + w10 * t10.x) + w01 * t01.x) + w11 * t11.x;
+  o.y = ((w00 * t00.y + w10 * t10.y) + w01 * t01.y) + w11 * t11.y;
+  o.z = ((w00 * t00.z + w10 * t10.z) + w01 * t01.z) + w11 * t11.z;
+  o.w = ((w00 * t00.w + w10 * t10.w) + w01 * t01.w) + w11 * t11.w;
+  dst[(long long)y * dw + x] = o;
+}
+
+int launch_build_chain(const float* level0, int w, int h, float* chain, cudaStream_t st) {
+  ChainTable t;
+  make_table(w, h, &t);
+  float4* c = reinterpret_cast<float4*>(chain);
+  if (level0 != chain) {
+    cudaError_t e = cudaMemcpyAsync(c, level0, (size_t)w * h * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e, "level-0 copy");
+  }
+  for (int l = 1; l < t.levels; ++l) {
+    dim3 grid((t.lw[l] + 31) / 32, (t.lh[l] + 7) / 8);
+    blit_level_kernel<<<grid, 256, 0, st>>>(c + t.off[l - 1], t.lw[l - 1], t.lh[l - 1],
+                                            c + t.off[l], t.lw[l], t.lh[l]);
+  }
+  return cuda_status(cudaGetLastError(), "blit_level_kernel launch");
+}
+
+// ---------------------------------------------------------------------------
+// GGX prefilter (PreFilterEnvMap.comp:126-177).  One thread = one output
+// texel, samples accumulated serially in the shader's order; every mip of
+// the chain in one launch (block ranges per mip).
+// ---------------------------------------------------------------------------
+constexpr int kPfTileX = 16, kPfTileY = 8;
+
+struct PrefilterJob {
+  float4* out;
+  long long pitch;  // in texels
+  int ow, oh;
+  float roughness;
+  int tiles_x;
+  int block_begin;
+};
+
+struct PrefilterParams {
+  const float4* chain;
+  int w, h;
+  int samples;
+  int generator;
+  int njobs;
+  PrefilterJob jobs[ALTHEA_IBL_MAX_MIPS];
+};
+
+__device__ __forceinline__ void prefilter_texel_degenerate(const float4* __restrict__ chain,
+                                                           const ChainTable& tab, Float3 n,
+                                                           Float3 t, Float3 b, uint32_t sx,
+                                                           uint32_t sy, int samples, int gen,
+                                                           float* acc, float& total) {
+  // roughness == 0: a2 = 0 makes sampleGGX return (cos(phi)*0, sin(phi)*0, 1),
+  // so every sample with xi.y < 1 yields the same H = n, the same L and the
+  // same texel value; xi.y == 1 gives 0/0 and the sample fails NdotL > 0
+  // (:163).  Evaluate the first kept sample once, then repeat the serial
+  // float accumulation for every kept sample, which is what the loop of
+  // :147-167 computes.
+  float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, ndotl = 0.0f;
+  bool have = false;
+  for (int i = 0; i < samples; ++i) {
+    float xi_x, xi_y;
+    if (gen == ALTHEA_IBL_GEN_HAMMERSLEY) {
+      hammersley(i, samples, xi_x, xi_y);
+    } else {
+      xi_x = hash_float(hash_bits(sx + 2u * (uint32_t)i + 1u, sy + 2u * (uint32_t)i + 1u));
+      xi_y = hash_float(hash_bits(sx + 2u * (uint32_t)i + 2u, sy + 2u * (uint32_t)i + 2u));
+    }
+    if (xi_y == 1.0f) continue;  // NaN sample, dropped by NdotL > 0
+    if (!have) {
+      Float3 hv = to_world(t, b, n, sample_ggx(xi_x, xi_y, 0.0f));
+      float vdh = (n.x * hv.x + n.y * hv.y) + n.z * hv.z;
+      float k = 2.0f * vdh;
+      Float3 l = f3(k * hv.x - n.x, k * hv.y - n.y, k * hv.z - n.z);
+      float len = sqrtf((l.x * l.x + l.y * l.y) + l.z * l.z);
+      l = f3(l.x / len, l.y / len, l.z / len);
+      ndotl = glsl_max((n.x * l.x + n.y * l.y) + n.z * l.z, 0.0f);
+      if (ndotl > 0.0f) {
+        Float3 c = sample_env(chain, tab, l, 0.0f);
+        c0 = c.x * ndotl;
+        c1 = c.y * ndotl;
+        c2 = c.z * ndotl;
+      }
+      have = true;
+    }
+    if (ndotl > 0.0f) {
+      acc[0] += c0;
+      acc[1] += c1;
+      acc[2] += c2;
+      total += ndotl;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kPfTileX* kPfTileY) prefilter_kernel(const PrefilterParams p) {
+  __shared__ ChainTable tab;
+  __shared__ PrefilterJob job;
+  if (threadIdx.x == 0) {
+    make_table(p.w, p.h, &tab);
+    int sel = 0;
+#pragma unroll
+    for (int k = 1; k < ALTHEA_IBL_MAX_MIPS; ++k)
+      if (k < p.njobs && (int)blockIdx.x >= p.jobs[k].block_begin) sel = k;
+#pragma unroll
+    for (int k = 0; k < ALTHEA_IBL_MAX_MIPS; ++k)
+      if (k == sel) job = p.jobs[k];
+  }
+  __syncthreads();
+  int local = (int)blockIdx.x - job.block_begin;
+  int x = (local % job.tiles_x) * kPfTileX + (int)(threadIdx.x % kPfTileX);
+  int y = (local / job.tiles_x) * kPfTileY + (int)(threadIdx.x / kPfTileX);
+  if (x >= job.ow || y >= job.oh) return;
+
+  const float4* __restrict__ chain = p.chain;
+  const int samples = p.samples;
+  Float3 n = texel_dir(x, y, job.ow, job.oh);
+  Float3 t, b;
+  local_frame(n, t, b);
+  const float roughness = job.roughness;
+  const float a2 = roughness * roughness;
+  float acc[3] = {0.0f, 0.0f, 0.0f};
+  float total = 0.0f;
+
+  if (roughness == 0.0f) {
+    prefilter_texel_degenerate(chain, tab, n, t, b, (uint32_t)x, (uint32_t)y, samples,
+                               p.generator, acc, total);
+  } else {
+    const float sa_texel = 4.0f * kPi / (6.0f * (float)p.w * (float)p.h);
+    const float fsamples = (float)samples;
+    uint32_t sx = (uint32_t)x, sy = (uint32_t)y;
+#pragma unroll 1
+    for (int i = 0; i < samples; ++i) {
+      float xi_x, xi_y;
+      if (p.generator == ALTHEA_IBL_GEN_HAMMERSLEY) {
+        hammersley(i, samples, xi_x, xi_y);
+      } else {
+        sx += 1u;
+        sy += 1u;
+        xi_x = hash_float(hash_bits(sx, sy));
+        sx += 1u;
+        sy += 1u;
+        xi_y = hash_float(hash_bits(sx, sy));
+      }
+      Float3 hv = to_world(t, b, n, sample_ggx(xi_x, xi_y, a2));
+      // V = R = N (:136-137): V.H, N.H and H.V are one and the same sum.
+      float vdh = (n.x * hv.x + n.y * hv.y) + n.z * hv.z;
+      float k = 2.0f * vdh;
+      Float3 l = f3(k * hv.x - n.x, k * hv.y - n.y, k * hv.z - n.z);
+      float len = sqrtf((l.x * l.x + l.y * l.y) + l.z * l.z);
+      l = f3(l.x / len, l.y / len, l.z / len);
+      float ndotl = glsl_max((n.x * l.x + n.y * l.y) + n.z * l.z, 0.0f);
+      if (ndotl > 0.0f) {
+        float ndoth = glsl_max(vdh, 0.0f);
+        float d = distribution_ggx(ndoth, a2);
+        float pdf = d * ndoth / (4.0f * ndoth + 0.00001f);
+        float sa_sample = 1.0f / (fsamples * pdf + 0.0001f);
+        float mip = 0.5f * agb_log2(sa_sample / sa_texel);
+        Float3 c = sample_env(chain, tab, l, mip);
+        acc[0] += c.x * ndotl;
+        acc[1] += c.y * ndotl;
+        acc[2] += c.z * ndotl;
+        total += ndotl;
+      }
+    }
+  }
+  float4 o;
+  o.x = acc[0] / total;
+  o.y = acc[1] / total;
+  o.z = acc[2] / total;
+  o.w = 1.0f;
+  job.out[(long long)y * job.pitch + x] = o;
+}
+
+int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
+                     int mip_count, int samples, int generator, cudaStream_t st) {
+  PrefilterParams p;
+  memset(&p, 0, sizeof(p));
+  p.chain = reinterpret_cast<const float4*>(chain);
+  p.w = w;
+  p.h = h;
+  p.samples = samples;
+  p.generator = generator;
+  p.njobs = mip_count;
+  int blocks = 0;
+  for (int m = 0; m < mip_count; ++m) {
+    PrefilterJob& j = p.jobs[m];
+    j.out = reinterpret_cast<float4*>(mips[m].out_dev);
+    j.pitch = (long long)(mips[m].pitch_bytes / sizeof(float4));
+    j.ow = mips[m].width;
+    j.oh = mips[m].height;
+    j.roughness = mips[m].roughness;
+    j.tiles_x = (j.ow + kPfTileX - 1) / kPfTileX;
+    j.block_begin = blocks;
+    blocks += j.tiles_x * ((j.oh + kPfTileY - 1) / kPfTileY);
+  }
+  if (blocks == 0) return ALTHEA_IBL_OK;
+  prefilter_kernel<<<blocks, kPfTileX * kPfTileY, 0, st>>>(p);
+  return cuda_status(cudaGetLastError(), "prefilter_kernel launch");
+}
+
+// ---------------------------------------------------------------------------
+// Irradiance (GenIrradianceMap.comp:106-155).  The 300 x Nphi grid of one
+// texel is split over G = 8*GB thread groups: a block = one tile of 8x4
+// output texels (the 32 lanes of a warp, so a warp's gathers stay close) x
+// 8 warps (groups); each thread sums a contiguous chunk of the grid in grid
+// order, the block adds its 8 warps in order into a partial, and a second
+// kernel adds the GB partials in order.  Deterministic.
+// ---------------------------------------------------------------------------
+constexpr int kIrrTileX = 8, kIrrTileY = 4, kIrrWarps = 8;
+constexpr int kThetaSamples = 300;  // GenIrradianceMap.comp:119
+constexpr int kMaxPhiSamples = 4096;
+
+__host__ __device__ inline int irr_phi_samples(int w, int h) {
+  // int(pushConstants.height * thetaSamples / pushConstants.width) (:120-121)
+  return (int)((float)h * (float)kThetaSamples / (float)w);
+}
+
+IrrPlan irr_plan(int w, int h, int ow, int oh) {
+  IrrPlan pl;
+  pl.phi = irr_phi_samples(w, h);
+  pl.tiles_x = (ow + kIrrTileX - 1) / kIrrTileX;
+  pl.tiles = pl.tiles_x * ((oh + kIrrTileY - 1) / kIrrTileY);
+  long long pairs = (long long)kThetaSamples * (pl.phi > 0 ? pl.phi : 1);
+  int target_blocks = 152 * 8;
+  int gb = (target_blocks + pl.tiles - 1) / pl.tiles;
+  int gb_max = (int)(pairs / (32 * kIrrWarps));  // >= 32 samples per thread
+  if (gb > gb_max) gb = gb_max;
+  if (gb < 1) gb = 1;
+  pl.gb = gb;
+  pl.workspace = (size_t)pl.tiles * gb * 32 * sizeof(float4);
+  return pl;
+}
+
+__global__ void __launch_bounds__(32 * kIrrWarps) irradiance_partial_kernel(
+    const float4* __restrict__ chain, int w, int h, int ow, int oh, int tiles_x, int gb_count,
+    int phi_samples, float4* __restrict__ partial) {
+  __shared__ ChainTable tab;
+  __shared__ float cos_t[kThetaSamples], sin_t[kThetaSamples];
+  __shared__ float cos_p[kMaxPhiSamples], sin_p[kMaxPhiSamples];
+  __shared__ float part[kIrrWarps][32][3];
+  if (threadIdx.x == 0) make_table(w, h, &tab);
+  for (int i = threadIdx.x; i < kThetaSamples; i += blockDim.x) {
+    // theta = i * 2 * PI / thetaSamples (:127): int i*2, then float.
+    float theta = (float)(i * 2) * kPi / (float)kThetaSamples;
+    cos_t[i] = agb_cos(theta);
+    sin_t[i] = agb_sin(theta);
+  }
+  for (int j = threadIdx.x; j < phi_samples; j += blockDim.x) {
+    float phi = (float)j * 0.5f * kPi / (float)phi_samples;  // :132
+    cos_p[j] = agb_cos(phi);
+    sin_p[j] = agb_sin(phi);
+  }
+  __syncthreads();
+
+  const int tile = blockIdx.x / gb_count;
+  const int gb = blockIdx.x % gb_count;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int x = (tile % tiles_x) * kIrrTileX + (lane % kIrrTileX);
+  const int y = (tile / tiles_x) * kIrrTileY + (lane / kIrrTileX);
+  const bool active = x < ow && y < oh;
+  float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+  if (active) {
+    Float3 n = texel_dir(x, y, ow, oh);
+    Float3 t, b;
+    local_frame(n, t, b);
+    const float mip = agb_log2((float)w / (float)kThetaSamples);  // :124
+    const long long pairs = (long long)kThetaSamples * phi_samples;
+    const long long groups = (long long)gb_count * kIrrWarps;
+    const long long chunk = (pairs + groups - 1) / groups;
+    long long f0 = ((long long)gb * kIrrWarps + warp) * chunk;
+    long long f1 = f0 + chunk < pairs ? f0 + chunk : pairs;
+    if (f0 < f1) {
+      int i = (int)(f0 / phi_samples), j = (int)(f0 % phi_samples);
+      float ct = cos_t[i], st = sin_t[i];
+#pragma unroll 1
+      for (long long f = f0; f < f1; ++f) {
+        float cp = cos_p[j], sp = sin_p[j];
+        Float3 d = to_world(t, b, n, f3(ct * sp, st * sp, cp));
+        Float3 c = sample_env(chain, tab, d, mip);
+        a0 += c.x * cp * sp;
+        a1 += c.y * cp * sp;
+        a2 += c.z * cp * sp;
+        if (++j == phi_samples) {
+          j = 0;
+          ++i;
+          if (i < kThetaSamples) {
+            ct = cos_t[i];
+            st = sin_t[i];
+          }
+        }
+      }
+    }
+  }
+  part[warp][lane][0] = a0;
+  part[warp][lane][1] = a1;
+  part[warp][lane][2] = a2;
+  __syncthreads();
+  if (warp == 0) {
+    float s0 = part[0][lane][0], s1 = part[0][lane][1], s2 = part[0][lane][2];
+#pragma unroll
+    for (int k = 1; k < kIrrWarps; ++k) {
+      s0 += part[k][lane][0];
+      s1 += part[k][lane][1];
+      s2 += part[k][lane][2];
+    }
+    partial[((long long)tile * gb_count + gb) * 32 + lane] = make_float4(s0, s1, s2, 0.0f);
+  }
+}
+
+__global__ void __launch_bounds__(256) irradiance_finish_kernel(const float4* __restrict__ partial,
+                                                                int ow, int oh, int tiles_x,
+                                                                int tiles, int gb_count,
+                                                                int phi_samples,
+                                                                float4* __restrict__ out,
+                                                                long long pitch) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= tiles * 32) return;
+  int tile = g / 32, lane = g % 32;
+  int x = (tile % tiles_x) * kIrrTileX + (lane % kIrrTileX);
+  int y = (tile / tiles_x) * kIrrTileY + (lane / kIrrTileX);
+  if (x >= ow || y >= oh) return;
+  const float4* p = partial + (long long)tile * gb_count * 32 + lane;
+  float4 s = p[0];
+  for (int k = 1; k < gb_count; ++k) {
+    float4 q = p[(long long)k * 32];
+    s.x += q.x;
+    s.y += q.y;
+    s.z += q.z;
+  }
+  // vec4(PI * irradiance / float(thetaSamples) / float(phiSamples), 1.0) (:145)
+  float4 o;
+  o.x = kPi * s.x / (float)kThetaSamples / (float)phi_samples;
+  o.y = kPi * s.y / (float)kThetaSamples / (float)phi_samples;
+  o.z = kPi * s.z / (float)kThetaSamples / (float)phi_samples;
+  o.w = 1.0f;
+  out[(long long)y * pitch + x] = o;
+}
+
+int launch_irradiance(const float* chain, int w, int h, float* out, int ow, int oh,
+                      size_t pitch_bytes, void* ws, cudaStream_t st) {
+  IrrPlan pl = irr_plan(w, h, ow, oh);
+  float4* partial = reinterpret_cast<float4*>(ws);
+  irradiance_partial_kernel<<<pl.tiles * pl.gb, 32 * kIrrWarps, 0, st>>>(
+      reinterpret_cast<const float4*>(chain), w, h, ow, oh, pl.tiles_x, pl.gb, pl.phi, partial);
+  int n = pl.tiles * 32;
+  irradiance_finish_kernel<<<(n + 255) / 256, 256, 0, st>>>(
+      partial, ow, oh, pl.tiles_x, pl.tiles, pl.gb, pl.phi, reinterpret_cast<float4*>(out),
+      (long long)(pitch_bytes / sizeof(float4)));
+  return cuda_status(cudaGetLastError(), "irradiance kernels launch");
+}
+
+// ---------------------------------------------------------------------------
+// Split-sum BRDF LUT (Karis 2013, IntegrateBRDF).  One thread per texel, N
+// Hammersley samples in order; FP32 (it is not a contraction).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) brdf_lut_kernel(float2* __restrict__ out, int n,
+                                                       long long pitch, int samples,
+                                                       int orientation) {
+  int i = blockIdx.x * 32 + (threadIdx.x & 31);
+  int j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= n || j >= n) return;
+  float nov = ((float)i + 0.5f) / (float)n;
+  float tj = ((float)j + 0.5f) / (float)n;
+  float rough = orientation == ALTHEA_IBL_LUT_ASSET ? 1.0f - tj : tj;
+  float vx = sqrtf(1.0f - nov * nov), vz = nov;
+  float alpha = rough * rough;
+  float a2 = alpha * alpha;
+  float k = alpha / 2.0f;
+  float sum_a = 0.0f, sum_b = 0.0f;
+#pragma unroll 1
+  for (int s = 0; s < samples; ++s) {
+    float xi_x, xi_y;
+    hammersley(s, samples, xi_x, xi_y);
+    float phi = 2.0f * kPi * xi_x;
+    float cos_t = sqrtf((1.0f - xi_y) / (1.0f + (a2 - 1.0f) * xi_y));
+    float sin_t = sqrtf(1.0f - cos_t * cos_t);
+    float hx = sin_t * agb_cos(phi), hz = cos_t;
+    float vdh = vx * hx + vz * hz;
+    float lz = 2.0f * vdh * hz - vz;
+    float nol = lz > 0.0f ? (lz < 1.0f ? lz : 1.0f) : 0.0f;
+    float noh = hz > 0.0f ? (hz < 1.0f ? hz : 1.0f) : 0.0f;
+    float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
+    if (nol > 0.0f) {
+      float g1l = nol / (nol * (1.0f - k) + k);
+      float g1v = nov / (nov * (1.0f - k) + k);
+      float g_vis = g1l * g1v * voh / (noh * nov);
+      float tt = 1.0f - voh;
+      float t2 = tt * tt;
+      float fc = t2 * t2 * tt;
+      sum_a += (1.0f - fc) * g_vis;
+      sum_b += fc * g_vis;
+    }
+  }
+  out[(long long)j * pitch + i] = make_float2(sum_a / (float)samples, sum_b / (float)samples);
+}
+
+int launch_brdf_lut(float* out, int n, size_t pitch_bytes, int samples, int orientation,
+                    cudaStream_t st) {
+  dim3 grid((n + 31) / 32, (n + 7) / 8);
+  brdf_lut_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<float2*>(out), n,
+                                        (long long)(pitch_bytes / sizeof(float2)), samples,
+                                        orientation);
+  return cuda_status(cudaGetLastError(), "brdf_lut_kernel launch");
+}
+
+// ---------------------------------------------------------------------------
+// Argument checks shared with the context API.
+// ---------------------------------------------------------------------------
+int check_env(int w, int h) {
+  if (w < 1 || h < 1 || w > 32768 || h > 32768)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
+                     "env size %dx%d outside 1..32768 per side", w, h);
+  return ALTHEA_IBL_OK;
+}
+
+int check_image(const void* p, int w, int h, size_t pitch, size_t texel_bytes, const char* what) {
+  if (!p) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "%s: null pointer", what);
+  if (w < 1 || h < 1 || w > 65536 || h > 65536)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "%s: bad size %dx%d", what, w, h);
+  if (pitch < (size_t)w * texel_bytes || pitch % texel_bytes != 0)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
+                     "%s: pitch %zu bytes must be a multiple of %zu and >= %zu", what, pitch,
+                     texel_bytes, (size_t)w * texel_bytes);
+  if (((uintptr_t)p) % texel_bytes != 0)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "%s: pointer not %zu-byte aligned", what,
+                     texel_bytes);
+  return ALTHEA_IBL_OK;
+}
+
+int check_irradiance_args(int w, int h, int ow, int oh) {
+  int phi = irr_phi_samples(w, h);
+  if (phi < 1 || phi > kMaxPhiSamples)
+    return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
+                     "irradiance grid int(300*H/W) = %d for %dx%d; supported 1..%d", phi, w, h,
+                     kMaxPhiSamples);
+  if (ow < 1 || oh < 1) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "irradiance size");
+  return ALTHEA_IBL_OK;
+}
+
+}  // namespace ibl
+
+// ===========================================================================
+// Stateless C ABI.
+// ===========================================================================
+using namespace ibl;
+
+extern "C" int althea_ibl_abi_version(void) { return ALTHEA_IBL_ABI_VERSION; }
+
+extern "C" const char* althea_ibl_last_error(void) { return ibl::last_error(); }
+
+extern "C" int althea_ibl_chain_levels(int w, int h) {
+  if (check_env(w, h) != ALTHEA_IBL_OK) return 0;
+  return chain_levels(w, h);
+}
+
+extern "C" size_t althea_ibl_chain_texels(int w, int h) {
+  if (check_env(w, h) != ALTHEA_IBL_OK) return 0;
+  ChainTable t;
+  make_table(w, h, &t);
+  return (size_t)(t.off[t.levels - 1] + (long long)t.lw[t.levels - 1] * t.lh[t.levels - 1]);
+}
+
+extern "C" size_t althea_ibl_chain_level_offset(int w, int h, int level) {
+  if (check_env(w, h) != ALTHEA_IBL_OK) return 0;
+  ChainTable t;
+  make_table(w, h, &t);
+  if (level < 0 || level >= t.levels) return 0;
+  return (size_t)t.off[level];
+}
+
+extern "C" int althea_ibl_build_env_chain(const float* level0, int w, int h, float* chain,
+                                          void* stream) {
+  int st = check_env(w, h);
+  if (st) return st;
+  if (!level0 || !chain) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null pointer");
+  if (((uintptr_t)level0 | (uintptr_t)chain) % 16)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "chain pointers must be 16-byte aligned");
+  return launch_build_chain(level0, w, h, chain, (cudaStream_t)stream);
+}
+
+extern "C" int althea_ibl_prefilter(const float* chain, int w, int h,
+                                    const althea_ibl_mip_target* mips, int mip_count,
+                                    int samples, int generator, void* stream) {
+  int st = check_env(w, h);
+  if (st) return st;
+  if (!chain || ((uintptr_t)chain) % 16)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "chain: null or not 16-byte aligned");
+  if (mip_count < 0 || mip_count > ALTHEA_IBL_MAX_MIPS || (mip_count > 0 && !mips))
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "mip_count %d outside 0..%d", mip_count,
+                     ALTHEA_IBL_MAX_MIPS);
+  if (samples < 1 || samples > (1 << 24))
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "samples %d outside 1..2^24", samples);
+  if (generator != ALTHEA_IBL_GEN_REF_HASH && generator != ALTHEA_IBL_GEN_HAMMERSLEY)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "unknown generator %d", generator);
+  for (int m = 0; m < mip_count; ++m) {
+    st = check_image(mips[m].out_dev, mips[m].width, mips[m].height, mips[m].pitch_bytes, 16,
+                     "prefilter mip");
+    if (st) return st;
+    float r = mips[m].roughness;
+    if (!(r >= 0.0f && r <= 1.0f))
+      return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "mip %d roughness %g outside [0,1]", m,
+                       (double)r);
+  }
+  return launch_prefilter(chain, w, h, mips, mip_count, samples, generator,
+                          (cudaStream_t)stream);
+}
+
+extern "C" size_t althea_ibl_irradiance_workspace_size(int w, int h, int ow, int oh) {
+  if (check_env(w, h) || check_irradiance_args(w, h, ow, oh)) return 0;
+  return irr_plan(w, h, ow, oh).workspace;
+}
+
+extern "C" int althea_ibl_irradiance(const float* chain, int w, int h, float* out, int ow, int oh,
+                                     size_t pitch, void* ws, size_t ws_bytes, void* stream) {
+  int st = check_env(w, h);
+  if (st) return st;
+  st = check_irradiance_args(w, h, ow, oh);
+  if (st) return st;
+  if (!chain || ((uintptr_t)chain) % 16)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "chain: null or not 16-byte aligned");
+  st = check_image(out, ow, oh, pitch, 16, "irradiance");
+  if (st) return st;
+  IrrPlan pl = irr_plan(w, h, ow, oh);
+  if (!ws || ws_bytes < pl.workspace || ((uintptr_t)ws) % 16)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
+                     "irradiance workspace needs %zu bytes (16-byte aligned), got %zu",
+                     pl.workspace, ws_bytes);
+  return launch_irradiance(chain, w, h, out, ow, oh, pitch, ws, (cudaStream_t)stream);
+}
+
+extern "C" int althea_ibl_brdf_lut(float* out, int n, size_t pitch, int samples, int orientation,
+                                   void* stream) {
+  if (n < 1 || n > 16384) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "LUT size %d", n);
+  int st = check_image(out, n, n, pitch, 8, "brdf lut");
+  if (st) return st;
+  if (samples < 1 || samples > (1 << 24))
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "LUT samples %d", samples);
+  if (orientation != ALTHEA_IBL_LUT_ASSET && orientation != ALTHEA_IBL_LUT_CORRECTED)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "LUT orientation %d", orientation);
+  return launch_brdf_lut(out, n, pitch, samples, orientation, (cudaStream_t)stream);
+}

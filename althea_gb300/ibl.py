@@ -1,0 +1,396 @@
+"""Host-side API over ``libalthea_ibl.so`` (the C ABI in include/althea_ibl.h).
+
+Mirrors the reference's interface for this path:
+
+* ``ImageBasedLighting.createResources``  -- Include/Althea/ImageBasedLighting.h:46-49,
+  Src/ImageBasedLighting.cpp:415-605 (bake, then hand out the four images);
+* ``IBLResources.bind / registerToHeap / getHandles`` -- :20-52 and
+  Include/Althea/ImageBasedLighting.h:24-43 (env, prefiltered, irradiance,
+  BRDF LUT, in that order);
+* ``IBLHandles`` -- Include/Althea/ImageBasedLighting.h:17-22.
+
+Device memory comes from PyTorch tensors (plumbing only); every computation
+runs in the CUDA library.  There is no CPU fallback: importing works without
+a GPU (so host logic can be tested), but any call that computes raises if the
+library or a CUDA device is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import List, NamedTuple, Optional
+
+from . import build as _build
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_CUDA = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_UNSUPPORTED = 4
+ERR_BUDGET = 5
+ERR_NOT_READY = 6
+
+GEN_REF_HASH = 0
+GEN_HAMMERSLEY = 1
+LUT_ASSET = 0
+LUT_CORRECTED = 1
+MAX_MIPS = 16
+
+
+class IBLError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"althea_ibl status {status}: {message}")
+        self.status = status
+
+
+class MipTarget(ctypes.Structure):
+    _fields_ = [("out_dev", ctypes.c_void_p), ("pitch_bytes", ctypes.c_size_t),
+                ("width", ctypes.c_int), ("height", ctypes.c_int), ("roughness", ctypes.c_float)]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "env_width", "env_height", "irradiance_width", "irradiance_height", "mip_count",
+        "first_mip_width", "first_mip_height", "samples", "generator", "lut_size", "lut_samples",
+        "lut_orientation")]
+
+
+class Outputs(ctypes.Structure):
+    _fields_ = [("irradiance_dev", ctypes.c_void_p), ("irradiance_pitch_bytes", ctypes.c_size_t),
+                ("mip_dev", ctypes.c_void_p * MAX_MIPS),
+                ("mip_pitch_bytes", ctypes.c_size_t * MAX_MIPS),
+                ("lut_dev", ctypes.c_void_p), ("lut_pitch_bytes", ctypes.c_size_t)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Loads libalthea_ibl.so (building it with nvcc when absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path) or (build_if_missing and not _build.up_to_date()):
+        if not build_if_missing:
+            raise OSError(f"{path} missing; run althea_gb300.build.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    vp, sz, i = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+    sig = {
+        "althea_ibl_abi_version": (i, []),
+        "althea_ibl_last_error": (ctypes.c_char_p, []),
+        "althea_ibl_chain_levels": (i, [i, i]),
+        "althea_ibl_chain_texels": (sz, [i, i]),
+        "althea_ibl_chain_level_offset": (sz, [i, i, i]),
+        "althea_ibl_build_env_chain": (i, [vp, i, i, vp, vp]),
+        "althea_ibl_prefilter": (i, [vp, i, i, ctypes.POINTER(MipTarget), i, i, i, vp]),
+        "althea_ibl_irradiance_workspace_size": (sz, [i, i, i, i]),
+        "althea_ibl_irradiance": (i, [vp, i, i, vp, i, i, sz, vp, sz, vp]),
+        "althea_ibl_brdf_lut": (i, [vp, i, sz, i, i, vp]),
+        "althea_ibl_config_reference": (None, [ctypes.POINTER(Config), i, i]),
+        "althea_ibl_create": (i, [ctypes.POINTER(Config), ctypes.POINTER(vp)]),
+        "althea_ibl_destroy": (i, [vp]),
+        "althea_ibl_mip_info": (i, [vp, i, ctypes.POINTER(i), ctypes.POINTER(i),
+                                    ctypes.POINTER(ctypes.c_float)]),
+        "althea_ibl_irradiance_size": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "althea_ibl_upload_env": (i, [vp, vp, i, vp]),
+        "althea_ibl_env_chain": (vp, [vp]),
+        "althea_ibl_bake": (i, [vp, ctypes.POINTER(Outputs), vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != OK:
+        msg = load().althea_ibl_last_error()
+        raise IBLError(status, msg.decode() if msg else "")
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_ptr(stream) -> Optional[int]:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _require_cuda(t, name, ncomp):
+    torch = _torch()
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise IBLError(ERR_INVALID_ARGUMENT, f"{name} must be a CUDA tensor")
+    if t.dtype != torch.float32:
+        raise IBLError(ERR_INVALID_ARGUMENT, f"{name} must be float32")
+    if t.dim() != 3 or t.shape[2] != ncomp or t.stride(2) != 1 or t.stride(1) != ncomp:
+        raise IBLError(ERR_INVALID_ARGUMENT, f"{name} must be (H, W, {ncomp}) with packed texels")
+
+
+def _pitch(t, ncomp) -> int:
+    return t.stride(0) * 4
+
+
+# ---- stateless kernels -------------------------------------------------------
+
+def chain_levels(w: int, h: int) -> int:
+    return load().althea_ibl_chain_levels(w, h)
+
+
+def chain_texels(w: int, h: int) -> int:
+    return load().althea_ibl_chain_texels(w, h)
+
+
+def chain_level_offset(w: int, h: int, level: int) -> int:
+    return load().althea_ibl_chain_level_offset(w, h, level)
+
+
+def build_env_chain(env, stream=None):
+    """env: CUDA (H, W, 4) float32 -> chain tensor (texels, 4), every level."""
+    torch = _torch()
+    _require_cuda(env, "env", 4)
+    env = env.contiguous()
+    h, w = env.shape[:2]
+    chain = torch.empty((chain_texels(w, h), 4), dtype=torch.float32, device=env.device)
+    _check(load().althea_ibl_build_env_chain(env.data_ptr(), w, h, chain.data_ptr(),
+                                             _stream_ptr(stream)))
+    return chain
+
+
+def build_env_chain_into(env, chain, stream=None) -> None:
+    """Builds the chain of env (CUDA (H, W, 4)) into a preallocated chain tensor."""
+    _require_cuda(env, "env", 4)
+    h, w = env.shape[:2]
+    if chain.numel() < chain_texels(w, h) * 4 or not chain.is_cuda or not chain.is_contiguous():
+        raise IBLError(ERR_INVALID_ARGUMENT, "chain tensor too small or not contiguous CUDA")
+    _check(load().althea_ibl_build_env_chain(env.contiguous().data_ptr(), w, h, chain.data_ptr(),
+                                             _stream_ptr(stream)))
+
+
+def chain_level(chain, w: int, h: int, level: int):
+    lw, lh = max(w >> level, 1), max(h >> level, 1)
+    off = chain_level_offset(w, h, level)
+    return chain[off:off + lw * lh].view(lh, lw, 4)
+
+
+def prefilter(chain, w: int, h: int, outs: List, roughness: List[float], samples: int,
+              generator: int = GEN_REF_HASH, stream=None) -> None:
+    """Writes each prefiltered mip into the given (h_m, w_m, 4) CUDA tensors."""
+    n = len(outs)
+    arr = (MipTarget * max(n, 1))()
+    for k, (o, r) in enumerate(zip(outs, roughness)):
+        _require_cuda(o, f"mip {k}", 4)
+        arr[k] = MipTarget(o.data_ptr(), _pitch(o, 4), o.shape[1], o.shape[0], float(r))
+    _check(load().althea_ibl_prefilter(chain.data_ptr(), w, h, arr, n, samples, generator,
+                                       _stream_ptr(stream)))
+
+
+def irradiance(chain, w: int, h: int, out, workspace=None, stream=None) -> None:
+    torch = _torch()
+    _require_cuda(out, "irradiance", 4)
+    oh, ow = out.shape[:2]
+    L = load()
+    need = L.althea_ibl_irradiance_workspace_size(w, h, ow, oh)
+    if need == 0:
+        _check(ERR_UNSUPPORTED if L.althea_ibl_last_error() else ERR_INVALID_ARGUMENT)
+    if workspace is None:
+        workspace = torch.empty(need, dtype=torch.uint8, device=out.device)
+    _check(L.althea_ibl_irradiance(chain.data_ptr(), w, h, out.data_ptr(), ow, oh, _pitch(out, 4),
+                                   workspace.data_ptr(), workspace.numel() *
+                                   workspace.element_size(), _stream_ptr(stream)))
+
+
+def brdf_lut(n: int, samples: int = 1024, orientation: int = LUT_ASSET, out=None, device=None,
+             stream=None):
+    torch = _torch()
+    if out is None:
+        out = torch.empty((n, n, 2), dtype=torch.float32, device=device or "cuda")
+    _require_cuda(out, "brdf lut", 2)
+    _check(load().althea_ibl_brdf_lut(out.data_ptr(), n, _pitch(out, 2), samples, orientation,
+                                      _stream_ptr(stream)))
+    return out
+
+
+# ---- context: the createResources mirror ----------------------------------------
+
+def reference_config(env_width: int, env_height: int) -> Config:
+    cfg = Config()
+    load().althea_ibl_config_reference(ctypes.byref(cfg), env_width, env_height)
+    return cfg
+
+
+def make_config(env_width, env_height, irradiance_size=None, mip_count=5, first_mip=None,
+                samples=10000, generator=GEN_REF_HASH, lut_size=0, lut_samples=1024,
+                lut_orientation=LUT_ASSET) -> Config:
+    cfg = reference_config(env_width, env_height)
+    if irradiance_size is not None:
+        cfg.irradiance_width, cfg.irradiance_height = irradiance_size
+    cfg.mip_count = mip_count
+    if first_mip is not None:
+        cfg.first_mip_width, cfg.first_mip_height = first_mip
+    cfg.samples = samples
+    cfg.generator = generator
+    cfg.lut_size = lut_size
+    cfg.lut_samples = lut_samples
+    cfg.lut_orientation = lut_orientation
+    return cfg
+
+
+class IBLHandles(NamedTuple):
+    environmentMapHandle: int
+    prefilteredMapHandle: int
+    irradianceMapHandle: int
+    brdfLutHandle: int
+
+
+@dataclass
+class IBLResources:
+    """The four images the renderer binds (env, prefiltered, irradiance, LUT)."""
+    environmentMap: object
+    prefilteredMap: List[object]
+    irradianceMap: object
+    brdfLut: Optional[object]
+    handles: Optional[IBLHandles] = None
+    _heap_ids: List[int] = field(default_factory=list)
+
+    def bind(self, assignment: list) -> list:
+        # Src/ImageBasedLighting.cpp:20-26 order.
+        assignment.extend([self.environmentMap, self.prefilteredMap, self.irradianceMap,
+                           self.brdfLut])
+        return assignment
+
+    def registerToHeap(self, heap: list) -> None:
+        ids = []
+        for img in (self.environmentMap, self.prefilteredMap, self.irradianceMap, self.brdfLut):
+            heap.append(img)
+            ids.append(len(heap) - 1)
+        self.handles = IBLHandles(*ids)
+
+    def getHandles(self) -> IBLHandles:
+        if self.handles is None:
+            raise IBLError(ERR_NOT_READY, "registerToHeap has not been called")
+        return self.handles
+
+
+class BakeContext:
+    """A resident env map plus its mip chain on one device (C context)."""
+
+    def __init__(self, cfg: Config):
+        self.cfg = cfg
+        self._ctx = ctypes.c_void_p()
+        _check(load().althea_ibl_create(ctypes.byref(cfg), ctypes.byref(self._ctx)))
+
+    def close(self):
+        if self._ctx:
+            load().althea_ibl_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def mip_info(self, m):
+        w, h, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        _check(load().althea_ibl_mip_info(self._ctx, m, ctypes.byref(w), ctypes.byref(h),
+                                          ctypes.byref(r)))
+        return w.value, h.value, r.value
+
+    def irradiance_size(self):
+        w, h = ctypes.c_int(), ctypes.c_int()
+        _check(load().althea_ibl_irradiance_size(self._ctx, ctypes.byref(w), ctypes.byref(h)))
+        return w.value, h.value
+
+    def upload_env(self, env, stream=None):
+        """env: (H, W, 4) float32, CUDA tensor or pinned/any host tensor."""
+        torch = _torch()
+        env = env.contiguous()
+        if tuple(env.shape) != (self.cfg.env_height, self.cfg.env_width, 4):
+            raise IBLError(ERR_INVALID_ARGUMENT, f"env shape {tuple(env.shape)}")
+        if env.dtype != torch.float32:
+            raise IBLError(ERR_INVALID_ARGUMENT, "env must be float32")
+        _check(load().althea_ibl_upload_env(self._ctx, env.data_ptr(), 1 if env.is_cuda else 0,
+                                            _stream_ptr(stream)))
+
+    def chain(self):
+        torch = _torch()
+        ptr = load().althea_ibl_env_chain(self._ctx)
+        n = chain_texels(self.cfg.env_width, self.cfg.env_height)
+        return _device_view(ptr, n * 4).view(n, 4)
+
+    def allocate_outputs(self, device="cuda"):
+        torch = _torch()
+        iw, ih = self.irradiance_size()
+        irr = torch.empty((ih, iw, 4), dtype=torch.float32, device=device)
+        mips = []
+        for m in range(self.cfg.mip_count):
+            w, h, _ = self.mip_info(m)
+            mips.append(torch.empty((h, w, 4), dtype=torch.float32, device=device))
+        lut = None
+        if self.cfg.lut_size > 0:
+            n = self.cfg.lut_size
+            lut = torch.empty((n, n, 2), dtype=torch.float32, device=device)
+        return irr, mips, lut
+
+    def bake(self, irr, mips, lut=None, stream=None):
+        o = Outputs()
+        _require_cuda(irr, "irradiance", 4)
+        o.irradiance_dev = irr.data_ptr()
+        o.irradiance_pitch_bytes = _pitch(irr, 4)
+        for m, t in enumerate(mips):
+            _require_cuda(t, f"mip {m}", 4)
+            o.mip_dev[m] = t.data_ptr()
+            o.mip_pitch_bytes[m] = _pitch(t, 4)
+        if lut is not None:
+            _require_cuda(lut, "lut", 2)
+            o.lut_dev = lut.data_ptr()
+            o.lut_pitch_bytes = _pitch(lut, 2)
+        _check(load().althea_ibl_bake(self._ctx, ctypes.byref(o), _stream_ptr(stream)))
+
+
+def _device_view(ptr: int, nfloats: int):
+    """A torch float32 view of library-owned device memory (no copy)."""
+    torch = _torch()
+
+    class _Holder:
+        __cuda_array_interface__ = {"shape": (nfloats,), "typestr": "<f4",
+                                    "data": (ptr, False), "version": 3}
+    return torch.as_tensor(_Holder(), device="cuda")
+
+
+class ImageBasedLighting:
+    """``ImageBasedLighting::createResources`` for the GB300 bake."""
+
+    @staticmethod
+    def createResources(env, cfg: Optional[Config] = None, stream=None) -> IBLResources:
+        """env: (H, W, 4) float32 (host or CUDA).  Bakes irradiance, the
+        prefiltered chain and (when cfg.lut_size > 0) the BRDF LUT."""
+        h, w = int(env.shape[0]), int(env.shape[1])
+        cfg = cfg or reference_config(w, h)
+        ctx = BakeContext(cfg)
+        try:
+            ctx.upload_env(env, stream)
+            irr, mips, lut = ctx.allocate_outputs()
+            ctx.bake(irr, mips, lut, stream)
+            env_dev = chain_level(ctx.chain(), w, h, 0).clone()
+        finally:
+            ctx.close()
+        return IBLResources(environmentMap=env_dev, prefilteredMap=mips, irradianceMap=irr,
+                            brdfLut=lut)
+
+    @staticmethod
+    def buildLayout() -> List[str]:
+        # Src/ImageBasedLighting.cpp:607-619: four texture bindings.
+        return ["environmentMap", "prefilteredMap", "irradianceMap", "brdfLut"]

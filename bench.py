@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Benchmark: IBL probe bakes per second on one GB300 (plain path).
+
+Workload (one "step" = one probe bake): a 4096x2048 RGBA32F equirect map
+(seeded synthetic: sky gradient x log-normal noise + 8 suns up to 1e4) ->
+env mip chain (13 levels) + 128x64 irradiance + 9-mip GGX chain from
+2048x1024 (roughness m/8) with N = 1024 reference-hash samples per texel +
+512x512 RG32F split-sum LUT (1024 Hammersley samples), all FP32.
+
+* value   : probes/s with the env level 0 resident in HBM (chain build +
+            prefilter + irradiance + LUT timed with CUDA events; L2 flushed
+            by a 256 MB write between steps, outside the events).
+* e2e     : probes/s through the public context API with host buffers:
+            pinned H2D upload of level 0, bake, D2H of every output.
+* roofline: the prefilter kernel (dominant), algorithmic gathered bytes
+            (128 B per trilinear sample, 64 B per roughness-0 texel, 16 B per
+            output texel) / its event-timed duration vs measured HBM peak.
+* cpu_baseline: the reference shaders compiled as C++ (oracle/_ref) -- or
+            the C restatement when that library is absent -- on every host
+            core, over a bounded sample of texels per mip, extrapolated to a
+            whole probe.
+
+``--impl reference`` times only that CPU implementation (rank 0).
+Multi-GPU: one process per GPU, each bakes its own probe (independent
+units, no collective) -> weak scaling; value = all probes / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "IBL probes/s at ≤1e-3 rel err vs FP64: tensor-core vs plain CUDA, 1 GB300"
+ENV_W, ENV_H = 4096, 2048
+IRR_W, IRR_H = 128, 64
+MIPS = 9
+FIRST_W, FIRST_H = 2048, 1024
+SAMPLES = 1024
+LUT_N, LUT_SAMPLES = 512, 1024
+WORKLOAD = ("4096x2048 RGBA32F env, 13-level chain, 128x64 irradiance, 9-mip GGX chain from "
+            "2048x1024 (roughness m/8), N=1024 ref-hash samples, 512x512 RG32F LUT, FP32")
+# DRAM bytes per prefilter launch from ncu (profiles/prefilter_c2_ncu.md); None until measured.
+NCU_PREFILTER_TRAFFIC = None
+
+
+def mip_sizes():
+    return [(max(FIRST_W >> m, 1), max(FIRST_H >> m, 1)) for m in range(MIPS)]
+
+
+def roughness():
+    return [m / (MIPS - 1) for m in range(MIPS)]
+
+
+def prefilter_algorithmic_bytes():
+    total = 0
+    for (w, h), r in zip(mip_sizes(), roughness()):
+        texels = w * h
+        total += texels * (64 if r == 0.0 else SAMPLES * 128) + texels * 16
+    return total
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([c.strip() for c in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 4 + i and r[4 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ----------------------------------------------------------------------------
+# CPU baseline (oracle/_ref = reference shaders as C++, else the C port)
+# ----------------------------------------------------------------------------
+def cpu_sample_probe_time(env, kind_pref="reference", scale=1.0):
+    """Times a bounded sample of a probe on all host cores; returns
+    (seconds per whole probe, kind, cores, sample description, seconds spent)."""
+    import oracle
+    use_ref = kind_pref == "reference" and oracle.ref_lib() is not None
+    kind = "reference" if use_ref else "port"
+    cores = os.cpu_count()
+    chain = oracle.ref_build_chain(env) if use_ref else oracle.build_chain(env)
+    rng = np.random.default_rng(123)
+    per_probe = 0.0
+    spent = 0.0
+    parts = []
+    for (ow, oh), r in zip(mip_sizes(), roughness()):
+        texels = ow * oh
+        k = min(texels, int((4096 if r > 0 else 8192) * scale))
+        idx = rng.choice(texels, size=k, replace=False)
+        xy = np.stack([idx % ow, idx // ow], 1).astype(np.int32)
+        t0 = time.perf_counter()
+        if use_ref:
+            oracle.ref_prefilter(chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, oracle.GEN_REF_HASH,
+                                 xy=xy, nthreads=cores)
+        else:
+            oracle.prefilter(chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, oracle.GEN_REF_HASH, xy=xy,
+                             nthreads=cores)
+        dt = time.perf_counter() - t0
+        spent += dt
+        per_probe += dt * texels / k
+        parts.append(f"mip{ow}x{oh}:{k}")
+    k = max(8, int(64 * scale))
+    idx = rng.choice(IRR_W * IRR_H, size=k, replace=False)
+    xy = np.stack([idx % IRR_W, idx // IRR_W], 1).astype(np.int32)
+    t0 = time.perf_counter()
+    if use_ref:
+        s = ENV_W // IRR_W  # env-size dispatch of the reference, strided texels
+        oracle.ref_irradiance_envsize(chain, ENV_W, ENV_H, xy * s, nthreads=cores)
+    else:
+        oracle.irradiance(chain, ENV_W, ENV_H, IRR_W, IRR_H, xy=xy, nthreads=cores)
+    dt = time.perf_counter() - t0
+    spent += dt
+    per_probe += dt * IRR_W * IRR_H / k
+    parts.append(f"irradiance:{k}")
+    # LUT: the reference has no generator; the C restatement times it.
+    t0 = time.perf_counter()
+    n_small = 64
+    oracle.brdf_lut_f32(n_small, LUT_SAMPLES, oracle.LUT_ASSET, nthreads=cores)
+    dt = time.perf_counter() - t0
+    spent += dt
+    per_probe += dt * (LUT_N * LUT_N) / (n_small * n_small)
+    parts.append(f"lut:{n_small}x{n_small}")
+    return per_probe, kind, cores, "texels per stage " + ",".join(parts), spent
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    from althea_gb300 import synth
+    env = synth.make_env(ENV_W, ENV_H, seed=0, sun_max=1e4)
+    for _ in range(args.warmup):
+        cpu_sample_probe_time(env, "reference", scale=0.25)
+    times = []
+    info = None
+    for _ in range(args.steps):
+        per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference", scale=0.25)
+        times.append(per_probe)
+        info = (kind, cores, sample)
+    sec = float(np.mean(times))
+    value = 1.0 / sec
+    line = {"metric": METRIC, "value": value, "unit": "probes/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "path": "reference compute shaders compiled as C++ "
+                       "(CPU, all host threads), extrapolated from a bounded texel sample"},
+            "cpu_baseline": {"value": value, "unit": "probes/s", "cores": info[1],
+                             "kind": info[0], "sample": info[2]},
+            "e2e": {"value": value, "unit": "probes/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    from althea_gb300 import ibl, synth
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    env = synth.make_env(ENV_W, ENV_H, seed=rank, sun_max=1e4)
+    env_d = torch.from_numpy(env).to(dev)
+    chain = torch.empty((ibl.chain_texels(ENV_W, ENV_H), 4), dtype=torch.float32, device=dev)
+    mips = [torch.empty((h, w, 4), dtype=torch.float32, device=dev) for w, h in mip_sizes()]
+    irr = torch.empty((IRR_H, IRR_W, 4), dtype=torch.float32, device=dev)
+    lut = torch.empty((LUT_N, LUT_N, 2), dtype=torch.float32, device=dev)
+    ws = torch.empty(ibl.load().althea_ibl_irradiance_workspace_size(ENV_W, ENV_H, IRR_W, IRR_H),
+                     dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    rough = roughness()
+    levels = ibl.chain_levels(ENV_W, ENV_H)
+    launches_per_step = (levels - 1) + 1 + 2 + 1
+
+    def step(ev):
+        ev[0].record(stream)
+        ibl.build_env_chain_into(env_d, chain, stream)
+        ev[1].record(stream)
+        ibl.prefilter(chain, ENV_W, ENV_H, mips, rough, SAMPLES, ibl.GEN_REF_HASH, stream)
+        ev[2].record(stream)
+        ibl.irradiance(chain, ENV_W, ENV_H, irr, ws, stream)
+        ev[3].record(stream)
+        ibl.brdf_lut(LUT_N, LUT_SAMPLES, ibl.LUT_ASSET, out=lut, stream=stream)
+        ev[4].record(stream)
+
+    def new_events():
+        return [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.fill_(1)
+            step(new_events())
+    torch.cuda.synchronize()
+
+    evs = []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                flush.fill_(1)  # evict L2 between timed steps (outside the events)
+                ev = new_events()
+                step(ev)
+                evs.append(ev)
+        torch.cuda.synchronize()
+        barrier()
+        wall = time.perf_counter() - t_wall
+    step_ms = [ev[0].elapsed_time(ev[4]) for ev in evs]
+    stage = np.array([[ev[i].elapsed_time(ev[i + 1]) for i in range(4)] for ev in evs])
+    total_ms = float(np.sum(step_ms))
+    if pg is not None:
+        t = torch.tensor([total_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = args.steps * world / (total_ms / 1e3)
+
+    # ---- end to end through the public context API (host buffers) ----------
+    cfg = ibl.make_config(ENV_W, ENV_H, irradiance_size=(IRR_W, IRR_H), mip_count=MIPS,
+                          first_mip=(FIRST_W, FIRST_H), samples=SAMPLES,
+                          generator=ibl.GEN_REF_HASH, lut_size=LUT_N, lut_samples=LUT_SAMPLES)
+    ctx = ibl.BakeContext(cfg)
+    host_env = torch.from_numpy(env).pin_memory()
+    e_irr, e_mips, e_lut = ctx.allocate_outputs(device=dev)
+    h_outs = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in [e_irr] + e_mips + [e_lut]]
+    h2d = host_env.numel() * 4
+    d2h = sum(t.numel() * 4 for t in h_outs)
+
+    def e2e_step():
+        ctx.upload_env(host_env, stream)
+        ctx.bake(e_irr, e_mips, e_lut, stream)
+        for hdst, dsrc in zip(h_outs, [e_irr] + e_mips + [e_lut]):
+            hdst.copy_(dsrc, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            e2e_step()
+    stream.synchronize()
+    barrier()
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e_start.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e_end.record(stream)
+    stream.synchronize()
+    barrier()
+    e2e_ms = e_start.elapsed_time(e_end)
+    if pg is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = args.steps * world / (e2e_ms / 1e3)
+    ctx.close()
+
+    if rank == 0:
+        peak, peak_kind = read_peaks()
+        pf_ms = float(np.mean(stage[:, 1]))
+        achieved = prefilter_algorithmic_bytes() / (pf_ms / 1e3) / 1e9
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference")
+            cpu = {"value": 1.0 / per_probe, "unit": "probes/s", "cores": cores, "kind": kind,
+                   "sample": sample + f" ({spent:.1f} s of CPU work)"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "probes/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded sky gradient x log-normal noise + 8 suns <= 1e4)",
+            "config": {"workload": WORKLOAD, "path": "plain (reference estimator, bit-identical "
+                       "to the reference shaders; <=1e-4 contract)",
+                       "global_batch": world, "parallelism": f"replicas x{world}",
+                       "l2": "flushed (256 MB write) between timed steps",
+                       "stage_ms": {"chain": float(np.mean(stage[:, 0])), "prefilter": pf_ms,
+                                    "irradiance": float(np.mean(stage[:, 2])),
+                                    "lut": float(np.mean(stage[:, 3]))}},
+            "e2e": {"value": e2e_value, "unit": "probes/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_per_step * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": NCU_PREFILTER_TRAFFIC,
+                         "kernel": "prefilter_kernel", "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": prefilter_algorithmic_bytes()},
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+            "wall_s": wall,
+        }
+        print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

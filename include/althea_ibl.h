@@ -1,0 +1,160 @@
+/*
+ * althea_ibl.h -- C ABI of the GB300 image-based-lighting precompute.
+ *
+ * Drop-in for the IBL bake of the Althea engine: the reference records two
+ * compute dispatches per bake inside
+ *   ImageBasedLighting::precomputeResources   (Src/ImageBasedLighting.cpp:137-412)
+ * reached from
+ *   ImageBasedLighting::createResources       (Include/Althea/ImageBasedLighting.h:46-49,
+ *                                              Src/ImageBasedLighting.cpp:415-605)
+ * and binds env / prefiltered / irradiance / BRDF-LUT images in that order
+ * (Src/ImageBasedLighting.cpp:20-26, Shaders/DeferredPass.frag:10-13).
+ *
+ * Conventions
+ *  - Images are RGBA32F (float4 per texel) unless a format says otherwise,
+ *    row-major with row 0 = v = 0, addressed with a row pitch in BYTES.
+ *  - Every pointer named *_dev is CUDA device memory owned by the caller.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *    stream).  All kernel entry points are asynchronous and stream ordered.
+ *  - Every function returns althea_ibl_status.  No C++ exception crosses this
+ *    boundary.  althea_ibl_last_error() returns the calling thread's last
+ *    error message (the reference throws std::runtime_error instead,
+ *    Src/ImageBasedLighting.cpp:423-425).
+ */
+#ifndef ALTHEA_IBL_H
+#define ALTHEA_IBL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ALTHEA_IBL_ABI_VERSION 1
+#define ALTHEA_IBL_MAX_LEVELS 16   /* env maps up to 32768 wide */
+#define ALTHEA_IBL_MAX_MIPS 16     /* prefiltered chain length */
+
+typedef enum {
+  ALTHEA_IBL_OK = 0,
+  ALTHEA_IBL_ERR_INVALID_ARGUMENT = 1,
+  ALTHEA_IBL_ERR_CUDA = 2,
+  ALTHEA_IBL_ERR_OUT_OF_MEMORY = 3,
+  ALTHEA_IBL_ERR_UNSUPPORTED = 4,
+  ALTHEA_IBL_ERR_BUDGET = 5,
+  ALTHEA_IBL_ERR_NOT_READY = 6
+} althea_ibl_status;
+
+/* Sample generator of the GGX prefilter.
+ * REF_HASH: the ShaderToy integer hash of PreFilterEnvMap.comp:38-44 seeded
+ *   with the texel position (:127), two draws per sample (:85) -- the
+ *   reference estimator, bit for bit.
+ * HAMMERSLEY: xi_i = (i/N, bitreverse(i) * 2^-32) in place of the two draws. */
+typedef enum { ALTHEA_IBL_GEN_REF_HASH = 0, ALTHEA_IBL_GEN_HAMMERSLEY = 1 } althea_ibl_generator;
+
+/* BRDF LUT row order.  ASSET: row 0 = roughness 1, the layout of the
+ * reference's Content/PrecomputedMaps/brdf_lut.png that its renderer binds
+ * today.  CORRECTED: row 0 = roughness 0, matching
+ * texture(brdfLut, vec2(NdotV, roughness)) in Shaders/PBR/PBRMaterial.glsl:110. */
+typedef enum { ALTHEA_IBL_LUT_ASSET = 0, ALTHEA_IBL_LUT_CORRECTED = 1 } althea_ibl_lut_orientation;
+
+/* One prefiltered mip: replaces one dispatch of PreFilterEnvMap.comp with
+ * push constants {envMapWidth, envMapHeight, width, height, roughness}
+ * (PrefilterEnvMapPushConstants, Src/ImageBasedLighting.cpp:123-129,376-395). */
+typedef struct {
+  float* out_dev;      /* RGBA32F, width x height */
+  size_t pitch_bytes;  /* >= width * 16, multiple of 16 */
+  int width, height;
+  float roughness;     /* reference: i / 4 for mip i of 5 */
+} althea_ibl_mip_target;
+
+/* ---- environment mip chain ------------------------------------------------
+ * Replaces Image::generateMipMaps (Src/Image.cpp:135-239: vkCmdBlitImage with
+ * VK_FILTER_LINEAR per level) for the RGBA32F env image created at
+ * Src/ImageBasedLighting.cpp:156-166 with computeMipCount levels
+ * (Src/Utilities.cpp:97-100).  The chain is every level back to back, level 0
+ * first, tightly packed (row pitch = level width * 16 bytes). */
+int althea_ibl_chain_levels(int env_width, int env_height);
+size_t althea_ibl_chain_texels(int env_width, int env_height);
+size_t althea_ibl_chain_level_offset(int env_width, int env_height, int level);
+/* level0_dev may equal chain_dev (level 0 is then used in place). */
+int althea_ibl_build_env_chain(const float* level0_dev, int env_width, int env_height,
+                               float* chain_dev, void* stream);
+
+/* ---- GGX prefilter (PreFilterEnvMap.comp:126-177) ----------------------------
+ * All listed mips in one launch.  samples = MAX_SAMPLES of the shader (:5; the
+ * reference uses 10000), also used by the source-LOD rule (:158). */
+int althea_ibl_prefilter(const float* chain_dev, int env_width, int env_height,
+                         const althea_ibl_mip_target* mips, int mip_count, int samples,
+                         int generator, void* stream);
+
+/* ---- diffuse irradiance (GenIrradianceMap.comp:106-155) -------------------
+ * Output size is free (the reference dispatches it at env size,
+ * Src/ImageBasedLighting.cpp:208-221,328-343); the 300 x int(300 H / W) grid
+ * and the LOD log2(W / 300) come from the env size as in the shader.
+ * Needs a caller-provided device workspace of
+ * althea_ibl_irradiance_workspace_size() bytes for per-block partial sums. */
+size_t althea_ibl_irradiance_workspace_size(int env_width, int env_height, int out_width,
+                                            int out_height);
+int althea_ibl_irradiance(const float* chain_dev, int env_width, int env_height, float* out_dev,
+                          int out_width, int out_height, size_t out_pitch_bytes,
+                          void* workspace_dev, size_t workspace_bytes, void* stream);
+
+/* ---- split-sum BRDF LUT ----------------------------------------------------
+ * Computes what the reference loads from Content/PrecomputedMaps/brdf_lut.png
+ * (Src/ImageBasedLighting.cpp:570-603): RG32F n x n, R = scale, G = bias of
+ * the split-sum integral (GGX alpha = roughness^2, Smith k = alpha/2,
+ * Hammersley samples). */
+int althea_ibl_brdf_lut(float* out_dev, int n, size_t pitch_bytes, int samples, int orientation,
+                        void* stream);
+
+/* ---- bake context: the createResources / precomputeResources mirror ------- */
+typedef struct althea_ibl_context althea_ibl_context;
+
+typedef struct {
+  int env_width, env_height;      /* resident env map size */
+  int irradiance_width, irradiance_height;   /* 0 = env size (reference) */
+  int mip_count;                  /* prefiltered mips (reference: 5) */
+  int first_mip_width, first_mip_height;     /* 0 = env size / 2 (reference) */
+  int samples;                    /* reference: 10000 */
+  int generator;                  /* althea_ibl_generator */
+  int lut_size;                   /* 0 = no LUT */
+  int lut_samples;
+  int lut_orientation;            /* althea_ibl_lut_orientation */
+} althea_ibl_config;
+
+/* Fills the reference's own settings for an env map of the given size. */
+void althea_ibl_config_reference(althea_ibl_config* cfg, int env_width, int env_height);
+
+typedef struct {
+  float* irradiance_dev;
+  size_t irradiance_pitch_bytes;
+  float* mip_dev[ALTHEA_IBL_MAX_MIPS];
+  size_t mip_pitch_bytes[ALTHEA_IBL_MAX_MIPS];
+  float* lut_dev;                 /* RG32F; may be NULL when lut_size == 0 */
+  size_t lut_pitch_bytes;
+} althea_ibl_outputs;
+
+int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_context** out);
+int althea_ibl_destroy(althea_ibl_context* ctx);
+/* Mip m size and roughness as the context bakes them. */
+int althea_ibl_mip_info(const althea_ibl_context* ctx, int mip, int* width, int* height,
+                        float* roughness);
+int althea_ibl_irradiance_size(const althea_ibl_context* ctx, int* width, int* height);
+/* Uploads level 0 (host or device memory, RGBA32F, tightly packed) into the
+ * context's resident chain and rebuilds the mip chain. */
+int althea_ibl_upload_env(althea_ibl_context* ctx, const float* rgba, int src_is_device,
+                          void* stream);
+/* Resident chain (device), for callers that bind the env map itself. */
+const float* althea_ibl_env_chain(const althea_ibl_context* ctx);
+/* Irradiance + every prefiltered mip (+ LUT when configured) into caller
+ * buffers: the dispatch sequence of Src/ImageBasedLighting.cpp:315-402. */
+int althea_ibl_bake(althea_ibl_context* ctx, const althea_ibl_outputs* outs, void* stream);
+
+const char* althea_ibl_last_error(void);
+int althea_ibl_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ALTHEA_IBL_H */
