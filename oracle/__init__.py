@@ -186,6 +186,16 @@ def quad_irradiance(level0, ow, oh, xy, nthreads=0):
     return out
 
 
+def builtin(fn: str, a, b=None):
+    """Evaluates a portable GLSL built-in (sin, cos, atan, atan2, log2)."""
+    code = {"sin": 0, "cos": 1, "atan": 2, "atan2": 3, "log2": 4}[fn]
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(a if b is None else b, dtype=np.float32)
+    out = np.empty_like(a)
+    lib().oracle_builtin_eval(code, _fp(a), _fp(b), _fp(out), len(a))
+    return out
+
+
 def rng_stream(sx, sy, count):
     out = np.empty(count, dtype=np.float32)
     lib().oracle_rng_stream(ctypes.c_uint32(sx), ctypes.c_uint32(sy), count, _fp(out))

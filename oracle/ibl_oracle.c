@@ -626,3 +626,17 @@ void oracle_quad_irradiance_texels(const float* level0, int w, int h, int ow,
   }
   quad_tables_free(&tb);
 }
+
+/* Evaluates one portable GLSL built-in over an array (tests of their
+ * accuracy): fn 0 sin, 1 cos, 2 atan, 3 atan2(a, b), 4 log2. */
+void oracle_builtin_eval(int fn, const float* a, const float* b, float* out, int n) {
+  for (int i = 0; i < n; ++i) {
+    switch (fn) {
+      case 0: out[i] = agb_sin(a[i]); break;
+      case 1: out[i] = agb_cos(a[i]); break;
+      case 2: out[i] = agb_atan(a[i]); break;
+      case 3: out[i] = agb_atan2(a[i], b[i]); break;
+      default: out[i] = agb_log2(a[i]); break;
+    }
+  }
+}

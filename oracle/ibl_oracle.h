@@ -76,6 +76,9 @@ void oracle_rng_stream(uint32_t sx, uint32_t sy, int count, float* out);
 
 int oracle_max_threads(void);
 
+/* Portable GLSL built-in over an array: 0 sin, 1 cos, 2 atan, 3 atan2(a,b), 4 log2. */
+void oracle_builtin_eval(int fn, const float* a, const float* b, float* out, int n);
+
 #ifdef __cplusplus
 }
 #endif
