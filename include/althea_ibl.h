@@ -100,6 +100,26 @@ int althea_ibl_irradiance(const float* chain_dev, int env_width, int env_height,
                           int out_width, int out_height, size_t out_pitch_bytes,
                           void* workspace_dev, size_t workspace_bytes, void* stream);
 
+/* ---- irradiance without device allocation ---------------------------------
+ * No counterpart in the reference: an addition for callers that cannot call
+ * cudaMalloc (a renderer that owns all device memory through its own
+ * allocator and budget, a plug-in with a fixed memory envelope, code inside a
+ * frame or real-time callback where an allocation may stall the device).
+ * Same kernels and results as althea_ibl_irradiance, but the partial sums
+ * live in a fixed array of ALTHEA_IBL_NOALLOC_SCRATCH_BYTES inside the
+ * library, held on every device that loads the library until exit; the call
+ * allocates nothing.  Outputs whose partial sums do not fit (above about
+ * 260,000 texels: 512 x 256 fits, 1024 x 512 does not) are rejected with
+ * ALTHEA_IBL_ERR_UNSUPPORTED.
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the array: calls whose kernels overlap on the GPU
+ * race and must be serialised by the caller. */
+#define ALTHEA_IBL_NOALLOC_SCRATCH_BYTES (4 * 1024 * 1024)
+int althea_ibl_irradiance_noalloc(const float* chain_dev, int env_width, int env_height,
+                                  float* out_dev, int out_width, int out_height,
+                                  size_t out_pitch_bytes, void* stream);
+
 /* ---- split-sum BRDF LUT ----------------------------------------------------
  * Computes what the reference loads from Content/PrecomputedMaps/brdf_lut.png
  * (Src/ImageBasedLighting.cpp:570-603): RG32F n x n, R = scale, G = bias of
