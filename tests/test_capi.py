@@ -1,0 +1,77 @@
+"""CPU tests of the C ABI: the library loads, exports every declared symbol,
+and its host-side logic (sizes, configs, argument checks) works without a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from althea_gb300 import ibl
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", f)).read()
+            names |= set(re.findall(r"\b(althea_ibl_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported():
+    L = ibl.load()
+    syms = declared_symbols()
+    assert len(syms) >= 19
+    for s in syms:
+        assert hasattr(L, s), s
+
+
+def test_chain_geometry():
+    assert ibl.chain_levels(4096, 2048) == 13
+    assert ibl.chain_texels(4096, 2048) == sum(max(4096 >> l, 1) * max(2048 >> l, 1)
+                                               for l in range(13))
+    assert ibl.chain_level_offset(4096, 2048, 1) == 4096 * 2048
+    assert ibl.chain_levels(37, 19) == 6
+    assert ibl.load().althea_ibl_abi_version() == 1
+
+
+def test_reference_config_matches_reference_bake():
+    c = ibl.reference_config(4096, 2048)
+    # Src/ImageBasedLighting.cpp:184-221 and PreFilterEnvMap.comp:5
+    assert (c.irradiance_width, c.irradiance_height) == (4096, 2048)
+    assert c.mip_count == 5 and (c.first_mip_width, c.first_mip_height) == (2048, 1024)
+    assert c.samples == 10000 and c.generator == ibl.GEN_REF_HASH
+
+
+def test_irradiance_workspace_sizes():
+    L = ibl.load()
+    assert L.althea_ibl_irradiance_workspace_size(4096, 2048, 128, 64) > 0
+    # 300 x int(300*H/W) grid: W > 300 H gives no phi steps -> unsupported
+    assert L.althea_ibl_irradiance_workspace_size(1000, 1, 8, 8) == 0
+
+
+def test_argument_checks_without_gpu():
+    L = ibl.load()
+    assert L.althea_ibl_build_env_chain(None, 4, 4, None, None) == ibl.ERR_INVALID_ARGUMENT
+    assert L.althea_ibl_build_env_chain(16, 0, 4, 16, None) == ibl.ERR_INVALID_ARGUMENT
+    assert b"env size" in L.althea_ibl_last_error()
+    assert L.althea_ibl_prefilter(None, 8, 8, None, 0, 16, 0, None) == ibl.ERR_INVALID_ARGUMENT
+    assert L.althea_ibl_brdf_lut(None, 8, 64, 16, 0, None) == ibl.ERR_INVALID_ARGUMENT
+    assert L.althea_ibl_brdf_lut(16, 8, 64, 16, 7, None) == ibl.ERR_INVALID_ARGUMENT
+    assert L.althea_ibl_irradiance(16, 1000, 1, 16, 8, 8, 128, 16, 1 << 20, None) == \
+        ibl.ERR_UNSUPPORTED
+    assert L.althea_ibl_irradiance_noalloc(16, 64, 32, None, 8, 8, 128, None) == \
+        ibl.ERR_INVALID_ARGUMENT
+    bad = ibl.Config()
+    ctx = ctypes.c_void_p()
+    assert L.althea_ibl_create(ctypes.byref(bad), ctypes.byref(ctx)) == ibl.ERR_INVALID_ARGUMENT
+    assert not ctx.value
+    assert L.althea_ibl_bake(None, None, None) == ibl.ERR_INVALID_ARGUMENT
+
+
+def test_python_errors_carry_status():
+    with pytest.raises(ibl.IBLError) as e:
+        ibl._check(ibl.ERR_UNSUPPORTED)
+    assert e.value.status == ibl.ERR_UNSUPPORTED
