@@ -135,6 +135,17 @@ AGB_FN float agb_cos(float x) {
   return ((q + 1) & 2) ? -v : v;
 }
 
+/* Both at once: one reduction, the same results as agb_sin / agb_cos. */
+AGB_FN void agb_sincos(float x, float* sn, float* cs) {
+  float r;
+  int q = agb_reduce_pio2(x, &r);
+  float s = agb_sin_poly(r), c = agb_cos_poly(r);
+  float vs = (q & 1) ? c : s;
+  float vc = (q & 1) ? s : c;
+  *sn = (q & 2) ? -vs : vs;
+  *cs = ((q + 1) & 2) ? -vc : vc;
+}
+
 /* atan on t in [0, 1]. */
 AGB_FN float agb_atan01(float t) {
   int red = t > AGB_TWO_MINUS_SQRT3;
@@ -176,19 +187,8 @@ AGB_FN float agb_atan2(float y, float x) {
   return agb_copysign(a, y);
 }
 
-/* GLSL log2: -inf at 0, NaN below 0, +inf at +inf. */
-AGB_FN float agb_log2(float x) {
-  if (x != x) return x;
-  if (x < 0.0f) return agb_float(0x7fc00000u);
-  if (x == 0.0f) return agb_float(0xff800000u);
-  uint32_t b = agb_bits(x);
-  if (b == 0x7f800000u) return x;
-  int e = 0;
-  if (b < 0x00800000u) { /* subnormal: scale by 2^23 */
-    x = x * 8388608.0f;
-    b = agb_bits(x);
-    e = -23;
-  }
+/* log2 of a positive normal finite x (the common case of agb_log2). */
+AGB_FN float agb_log2_core(uint32_t b, int e) {
   e += (int)(b >> 23) - 127;
   float m = agb_float((b & 0x007fffffu) | 0x3f800000u);
   if (m > AGB_SQRT2) {
@@ -205,5 +205,35 @@ AGB_FN float agb_log2(float x) {
   float l = AGB_FMA(s * s2, p, s) * AGB_TWO_OVER_LN2;
   return (float)e + l;
 }
+
+/* GLSL log2: -inf at 0, NaN below 0, +inf at +inf. */
+AGB_FN float agb_log2(float x) {
+  uint32_t b = agb_bits(x);
+  if (b - 0x00800000u < 0x7f000000u) return agb_log2_core(b, 0); /* positive normal */
+  if (x != x) return x;
+  if (x < 0.0f) return agb_float(0x7fc00000u);
+  if (x == 0.0f) return agb_float(0xff800000u);
+  if (b == 0x7f800000u) return x;
+  /* positive subnormal: scale by 2^23 */
+  return agb_log2_core(agb_bits(x * 8388608.0f), -23);
+}
+
+/* a / b correctly rounded, given r = the correctly rounded 1/b (Markstein's
+ * theorem: q0 = a*r is within one ulp of a/b and the fma-computed residual
+ * a - q0*b is exact, so q0 + residual*r rounds to the IEEE quotient; zero
+ * numerators keep their sign).  Valid while a/b neither overflows nor
+ * underflows.  Saves the full division where the denominator is shared or
+ * constant. */
+AGB_FN float agb_div_rcp(float a, float b, float r) {
+  float q0 = a * r;
+  float e = AGB_FMA(-q0, b, a);
+  float q = AGB_FMA(e, r, q0);
+  return a == 0.0f ? q0 : q;
+}
+
+/* Correctly rounded reciprocals of 2*pi and pi as single-precision values
+ * (1 / 6.2831855f and 1 / 3.1415927f). */
+#define AGB_RCP_TWO_PI_F 0x1.45f306p-3f
+#define AGB_RCP_PI_F 0x1.45f306p-2f
 
 #endif /* ALTHEA_GLSL_BUILTINS_H */

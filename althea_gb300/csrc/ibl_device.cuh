@@ -65,11 +65,13 @@ __host__ __device__ inline void make_table(int w, int h, ChainTable* t) {
 // Index wrap for REPEAT.  Texel coordinates normally lie in [-1, n]; the
 // general branch keeps any input (even from NaN) in bounds.
 __device__ __forceinline__ int wrap_repeat(int i, int n) {
-  if ((unsigned)i < (unsigned)n) return i;
-  if (i == -1) return n - 1;
-  if (i == n) return 0;
-  int r = i % n;
-  return r < 0 ? r + n : r;
+  int r = i < 0 ? i + n : i;  // -1 -> n-1
+  r = r >= n ? r - n : r;     // n -> 0
+  if ((unsigned)r >= (unsigned)n) {
+    r = i % n;
+    r = r < 0 ? r + n : r;
+  }
+  return r;
 }
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
@@ -141,8 +143,10 @@ __device__ __forceinline__ Float3 sample_env(const float4* __restrict__ chain,
   } else {
     pitch = -0.5f * kPi;
   }
-  float u = yaw / (2.0f * kPi) + 0.5f;
-  float v = pitch / kPi + 0.5f;
+  // yaw / (2.0 * PI) + 0.5 and pitch / PI + 0.5, with the IEEE quotients
+  // formed from the correctly rounded constant reciprocals.
+  float u = agb_div_rcp(yaw, 2.0f * kPi, AGB_RCP_TWO_PI_F) + 0.5f;
+  float v = agb_div_rcp(pitch, kPi, AGB_RCP_PI_F) + 0.5f;
   return texture_lod(chain, t, u, v, mip);
 }
 
@@ -152,8 +156,10 @@ __device__ __forceinline__ Float3 texel_dir(int x, int y, int ow, int oh) {
   float v = (float)y / (float)oh;
   float yaw = kPi * (2.0f * u - 1.0f);
   float pitch = kPi * (v - 0.5f);
-  float cp = agb_cos(pitch);
-  return f3(cp * agb_cos(yaw), agb_sin(pitch), cp * agb_sin(yaw));
+  float sp, cp, sy, cy;
+  agb_sincos(pitch, &sp, &cp);
+  agb_sincos(yaw, &sy, &cy);
+  return f3(cp * cy, sp, cp * sy);
 }
 
 // coordinateSystem / LocalToWorld (PreFilterEnvMap.comp:22-34).
@@ -174,6 +180,14 @@ __device__ __forceinline__ Float3 to_world(Float3 t, Float3 b, Float3 n, Float3 
 }
 
 __device__ __forceinline__ float glsl_max(float x, float y) { return x < y ? y : x; }
+
+// normalize(v) = v / length(v): three IEEE quotients sharing one correctly
+// rounded reciprocal.
+__device__ __forceinline__ Float3 normalize3(Float3 l) {
+  float len = sqrtf((l.x * l.x + l.y * l.y) + l.z * l.z);
+  float r = 1.0f / len;
+  return f3(agb_div_rcp(l.x, len, r), agb_div_rcp(l.y, len, r), agb_div_rcp(l.z, len, r));
+}
 
 // rng() of PreFilterEnvMap.comp:38-44: the seed advances by one per call, so
 // draw k (1-based) is a pure function of seed0 + k.
@@ -197,7 +211,9 @@ __device__ __forceinline__ Float3 sample_ggx(float xi_x, float xi_y, float a2) {
   float phi = 2.0f * kPi * xi_x;
   float cos_t = sqrtf((1.0f - xi_y) / (1.0f + (a2 - 1.0f) * xi_y));
   float sin_t = sqrtf(1.0f - cos_t * cos_t);
-  return f3(agb_cos(phi) * sin_t, agb_sin(phi) * sin_t, cos_t);
+  float sp, cp;
+  agb_sincos(phi, &sp, &cp);
+  return f3(cp * sin_t, sp * sin_t, cos_t);
 }
 
 // distributionGGX (PreFilterEnvMap.comp:78-82).

@@ -11,11 +11,10 @@
 namespace ibl {
 
 struct IrrPlan {
-  int phi;       // int(300 * H / W)
-  int tiles_x;   // 8-texel-wide tiles per row
-  int tiles;     // 8x4 tiles in the output
-  int gb;        // 256-thread blocks per tile
-  size_t workspace;
+  int phi;             // int(300 * H / W)
+  long long texels;    // output texels
+  int gb;              // 256-thread blocks per output texel
+  size_t workspace;    // texels * gb partial sums (float4)
 };
 
 int set_error(int status, const char* fmt, ...);

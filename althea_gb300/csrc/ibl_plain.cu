@@ -105,6 +105,7 @@ struct PrefilterParams {
   int samples;
   int generator;
   int njobs;
+  int tabulate;  // Hammersley and samples <= kMaxTabulatedSamples
   PrefilterJob jobs[ALTHEA_IBL_MAX_MIPS];
 };
 
@@ -121,22 +122,26 @@ __device__ __forceinline__ void prefilter_texel_degenerate(const float4* __restr
   // :147-167 computes.
   float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, ndotl = 0.0f;
   bool have = false;
+#pragma unroll 4
   for (int i = 0; i < samples; ++i) {
-    float xi_x, xi_y;
+    // Only xi.y decides whether a sample survives; xi.x is drawn for the
+    // first kept sample alone.
+    float xi_y;
     if (gen == ALTHEA_IBL_GEN_HAMMERSLEY) {
-      hammersley(i, samples, xi_x, xi_y);
+      xi_y = __uint2float_rn(__brev((uint32_t)i)) * (1.0f / 4294967296.0f);
     } else {
-      xi_x = hash_float(hash_bits(sx + 2u * (uint32_t)i + 1u, sy + 2u * (uint32_t)i + 1u));
       xi_y = hash_float(hash_bits(sx + 2u * (uint32_t)i + 2u, sy + 2u * (uint32_t)i + 2u));
     }
     if (xi_y == 1.0f) continue;  // NaN sample, dropped by NdotL > 0
     if (!have) {
+      float xi_x = gen == ALTHEA_IBL_GEN_HAMMERSLEY
+                       ? (float)i / (float)samples
+                       : hash_float(hash_bits(sx + 2u * (uint32_t)i + 1u,
+                                              sy + 2u * (uint32_t)i + 1u));
       Float3 hv = to_world(t, b, n, sample_ggx(xi_x, xi_y, 0.0f));
       float vdh = (n.x * hv.x + n.y * hv.y) + n.z * hv.z;
       float k = 2.0f * vdh;
-      Float3 l = f3(k * hv.x - n.x, k * hv.y - n.y, k * hv.z - n.z);
-      float len = sqrtf((l.x * l.x + l.y * l.y) + l.z * l.z);
-      l = f3(l.x / len, l.y / len, l.z / len);
+      Float3 l = normalize3(f3(k * hv.x - n.x, k * hv.y - n.y, k * hv.z - n.z));
       ndotl = glsl_max((n.x * l.x + n.y * l.y) + n.z * l.z, 0.0f);
       if (ndotl > 0.0f) {
         Float3 c = sample_env(chain, tab, l, 0.0f);
@@ -155,9 +160,15 @@ __device__ __forceinline__ void prefilter_texel_degenerate(const float4* __restr
   }
 }
 
+// Hammersley xi does not depend on the texel, so neither does sampleGGX's
+// local half-vector: blocks of a roughness > 0 mip tabulate it once in shared
+// memory when it fits (same operations, same values).
+constexpr int kMaxTabulatedSamples = 2048;
+
 __global__ void __launch_bounds__(kPfTileX* kPfTileY) prefilter_kernel(const PrefilterParams p) {
   __shared__ ChainTable tab;
   __shared__ PrefilterJob job;
+  extern __shared__ float h_local[];  // 3 * samples floats when tabulated
   if (threadIdx.x == 0) {
     make_table(p.w, p.h, &tab);
     int sel = 0;
@@ -169,6 +180,19 @@ __global__ void __launch_bounds__(kPfTileX* kPfTileY) prefilter_kernel(const Pre
       if (k == sel) job = p.jobs[k];
   }
   __syncthreads();
+  const bool tabulated = p.tabulate && job.roughness != 0.0f;
+  if (tabulated) {
+    const float a2t = job.roughness * job.roughness;
+    for (int i = threadIdx.x; i < p.samples; i += blockDim.x) {
+      float xi_x, xi_y;
+      hammersley(i, p.samples, xi_x, xi_y);
+      Float3 hl = sample_ggx(xi_x, xi_y, a2t);
+      h_local[3 * i] = hl.x;
+      h_local[3 * i + 1] = hl.y;
+      h_local[3 * i + 2] = hl.z;
+    }
+    __syncthreads();
+  }
   int local = (int)blockIdx.x - job.block_begin;
   int x = (local % job.tiles_x) * kPfTileX + (int)(threadIdx.x % kPfTileX);
   int y = (local / job.tiles_x) * kPfTileY + (int)(threadIdx.x / kPfTileX);
@@ -189,35 +213,40 @@ __global__ void __launch_bounds__(kPfTileX* kPfTileY) prefilter_kernel(const Pre
                                p.generator, acc, total);
   } else {
     const float sa_texel = 4.0f * kPi / (6.0f * (float)p.w * (float)p.h);
+    const float rcp_sa_texel = 1.0f / sa_texel;
     const float fsamples = (float)samples;
     uint32_t sx = (uint32_t)x, sy = (uint32_t)y;
 #pragma unroll 1
     for (int i = 0; i < samples; ++i) {
-      float xi_x, xi_y;
-      if (p.generator == ALTHEA_IBL_GEN_HAMMERSLEY) {
-        hammersley(i, samples, xi_x, xi_y);
+      Float3 hl;
+      if (tabulated) {
+        hl = f3(h_local[3 * i], h_local[3 * i + 1], h_local[3 * i + 2]);
       } else {
-        sx += 1u;
-        sy += 1u;
-        xi_x = hash_float(hash_bits(sx, sy));
-        sx += 1u;
-        sy += 1u;
-        xi_y = hash_float(hash_bits(sx, sy));
+        float xi_x, xi_y;
+        if (p.generator == ALTHEA_IBL_GEN_HAMMERSLEY) {
+          hammersley(i, samples, xi_x, xi_y);
+        } else {
+          sx += 1u;
+          sy += 1u;
+          xi_x = hash_float(hash_bits(sx, sy));
+          sx += 1u;
+          sy += 1u;
+          xi_y = hash_float(hash_bits(sx, sy));
+        }
+        hl = sample_ggx(xi_x, xi_y, a2);
       }
-      Float3 hv = to_world(t, b, n, sample_ggx(xi_x, xi_y, a2));
+      Float3 hv = to_world(t, b, n, hl);
       // V = R = N (:136-137): V.H, N.H and H.V are one and the same sum.
       float vdh = (n.x * hv.x + n.y * hv.y) + n.z * hv.z;
       float k = 2.0f * vdh;
-      Float3 l = f3(k * hv.x - n.x, k * hv.y - n.y, k * hv.z - n.z);
-      float len = sqrtf((l.x * l.x + l.y * l.y) + l.z * l.z);
-      l = f3(l.x / len, l.y / len, l.z / len);
+      Float3 l = normalize3(f3(k * hv.x - n.x, k * hv.y - n.y, k * hv.z - n.z));
       float ndotl = glsl_max((n.x * l.x + n.y * l.y) + n.z * l.z, 0.0f);
       if (ndotl > 0.0f) {
         float ndoth = glsl_max(vdh, 0.0f);
         float d = distribution_ggx(ndoth, a2);
         float pdf = d * ndoth / (4.0f * ndoth + 0.00001f);
         float sa_sample = 1.0f / (fsamples * pdf + 0.0001f);
-        float mip = 0.5f * agb_log2(sa_sample / sa_texel);
+        float mip = 0.5f * agb_log2(agb_div_rcp(sa_sample, sa_texel, rcp_sa_texel));
         Float3 c = sample_env(chain, tab, l, mip);
         acc[0] += c.x * ndotl;
         acc[1] += c.y * ndotl;
@@ -257,19 +286,24 @@ int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_targ
     blocks += j.tiles_x * ((j.oh + kPfTileY - 1) / kPfTileY);
   }
   if (blocks == 0) return ALTHEA_IBL_OK;
-  prefilter_kernel<<<blocks, kPfTileX * kPfTileY, 0, st>>>(p);
+  p.tabulate = generator == ALTHEA_IBL_GEN_HAMMERSLEY && samples <= kMaxTabulatedSamples;
+  size_t smem = p.tabulate ? 3 * (size_t)samples * sizeof(float) : 0;
+  prefilter_kernel<<<blocks, kPfTileX * kPfTileY, smem, st>>>(p);
   return cuda_status(cudaGetLastError(), "prefilter_kernel launch");
 }
 
 // ---------------------------------------------------------------------------
-// Irradiance (GenIrradianceMap.comp:106-155).  The 300 x Nphi grid of one
-// texel is split over G = 8*GB thread groups: a block = one tile of 8x4
-// output texels (the 32 lanes of a warp, so a warp's gathers stay close) x
-// 8 warps (groups); each thread sums a contiguous chunk of the grid in grid
-// order, the block adds its 8 warps in order into a partial, and a second
-// kernel adds the GB partials in order.  Deterministic.
+// Irradiance (GenIrradianceMap.comp:106-155).  One output texel's 300 x Nphi
+// grid is split over G = 8*GB warps (GB blocks of 8 warps per texel), each
+// warp taking a contiguous band of theta rows.  Inside a warp the 32 lanes
+// cover a 4 (theta) x 8 (phi) patch of neighbouring grid directions, so one
+// gather instruction touches a compact patch of the env level.  Each lane sums
+// its samples in grid order; lanes are combined by a fixed xor-shuffle tree,
+// warps in order by the block, and the GB block partials in order by a second
+// kernel: deterministic, and within float rounding of the serial sum.
 // ---------------------------------------------------------------------------
-constexpr int kIrrTileX = 8, kIrrTileY = 4, kIrrWarps = 8;
+constexpr int kIrrWarps = 8;
+constexpr int kPatchT = 4, kPatchP = 8;
 constexpr int kThetaSamples = 300;  // GenIrradianceMap.comp:119
 constexpr int kMaxPhiSamples = 4096;
 
@@ -281,111 +315,102 @@ __host__ __device__ inline int irr_phi_samples(int w, int h) {
 IrrPlan irr_plan(int w, int h, int ow, int oh) {
   IrrPlan pl;
   pl.phi = irr_phi_samples(w, h);
-  pl.tiles_x = (ow + kIrrTileX - 1) / kIrrTileX;
-  pl.tiles = pl.tiles_x * ((oh + kIrrTileY - 1) / kIrrTileY);
-  long long pairs = (long long)kThetaSamples * (pl.phi > 0 ? pl.phi : 1);
-  int target_blocks = 152 * 8;
-  int gb = (target_blocks + pl.tiles - 1) / pl.tiles;
-  int gb_max = (int)(pairs / (32 * kIrrWarps));  // >= 32 samples per thread
+  long long texels = (long long)ow * oh;
+  pl.texels = texels;
+  const long long target_blocks = 152LL * 8;
+  long long gb = (target_blocks + texels - 1) / texels;
+  const long long gb_max = kThetaSamples / (kPatchT * kIrrWarps);  // >= 4 theta rows a warp
   if (gb > gb_max) gb = gb_max;
   if (gb < 1) gb = 1;
-  pl.gb = gb;
-  pl.workspace = (size_t)pl.tiles * gb * 32 * sizeof(float4);
+  pl.gb = (int)gb;
+  pl.workspace = (size_t)texels * (size_t)gb * sizeof(float4);
   return pl;
 }
 
 __global__ void __launch_bounds__(32 * kIrrWarps) irradiance_partial_kernel(
-    const float4* __restrict__ chain, int w, int h, int ow, int oh, int tiles_x, int gb_count,
-    int phi_samples, float4* __restrict__ partial) {
+    const float4* __restrict__ chain, int w, int h, int ow, int oh, int gb_count, int phi_samples,
+    float4* __restrict__ partial) {
   __shared__ ChainTable tab;
   __shared__ float cos_t[kThetaSamples], sin_t[kThetaSamples];
-  __shared__ float cos_p[kMaxPhiSamples], sin_p[kMaxPhiSamples];
-  __shared__ float part[kIrrWarps][32][3];
+  __shared__ float part[kIrrWarps][3];
+  extern __shared__ float phi_table[];  // 2 * phi_samples floats
+  float* cos_p = phi_table;
+  float* sin_p = phi_table + phi_samples;
   if (threadIdx.x == 0) make_table(w, h, &tab);
   for (int i = threadIdx.x; i < kThetaSamples; i += blockDim.x) {
     // theta = i * 2 * PI / thetaSamples (:127): int i*2, then float.
     float theta = (float)(i * 2) * kPi / (float)kThetaSamples;
-    cos_t[i] = agb_cos(theta);
-    sin_t[i] = agb_sin(theta);
+    agb_sincos(theta, &sin_t[i], &cos_t[i]);
   }
   for (int j = threadIdx.x; j < phi_samples; j += blockDim.x) {
     float phi = (float)j * 0.5f * kPi / (float)phi_samples;  // :132
-    cos_p[j] = agb_cos(phi);
-    sin_p[j] = agb_sin(phi);
+    agb_sincos(phi, &sin_p[j], &cos_p[j]);
   }
   __syncthreads();
 
-  const int tile = blockIdx.x / gb_count;
+  const long long texel = blockIdx.x / gb_count;
   const int gb = blockIdx.x % gb_count;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int x = (tile % tiles_x) * kIrrTileX + (lane % kIrrTileX);
-  const int y = (tile / tiles_x) * kIrrTileY + (lane / kIrrTileX);
-  const bool active = x < ow && y < oh;
+  const int x = (int)(texel % ow), y = (int)(texel / ow);
+  Float3 n = texel_dir(x, y, ow, oh);
+  Float3 t, b;
+  local_frame(n, t, b);
+  const float mip = agb_log2((float)w / (float)kThetaSamples);  // :124
+  const int groups = gb_count * kIrrWarps;
+  const int g = gb * kIrrWarps + warp;
+  const int row0 = (int)((long long)g * kThetaSamples / groups);
+  const int row1 = (int)((long long)(g + 1) * kThetaSamples / groups);
+  const int lt = lane / kPatchP, lp = lane % kPatchP;
   float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-  if (active) {
-    Float3 n = texel_dir(x, y, ow, oh);
-    Float3 t, b;
-    local_frame(n, t, b);
-    const float mip = agb_log2((float)w / (float)kThetaSamples);  // :124
-    const long long pairs = (long long)kThetaSamples * phi_samples;
-    const long long groups = (long long)gb_count * kIrrWarps;
-    const long long chunk = (pairs + groups - 1) / groups;
-    long long f0 = ((long long)gb * kIrrWarps + warp) * chunk;
-    long long f1 = f0 + chunk < pairs ? f0 + chunk : pairs;
-    if (f0 < f1) {
-      int i = (int)(f0 / phi_samples), j = (int)(f0 % phi_samples);
-      float ct = cos_t[i], st = sin_t[i];
 #pragma unroll 1
-      for (long long f = f0; f < f1; ++f) {
-        float cp = cos_p[j], sp = sin_p[j];
-        Float3 d = to_world(t, b, n, f3(ct * sp, st * sp, cp));
-        Float3 c = sample_env(chain, tab, d, mip);
-        a0 += c.x * cp * sp;
-        a1 += c.y * cp * sp;
-        a2 += c.z * cp * sp;
-        if (++j == phi_samples) {
-          j = 0;
-          ++i;
-          if (i < kThetaSamples) {
-            ct = cos_t[i];
-            st = sin_t[i];
-          }
-        }
-      }
+  for (int i = row0 + lt; i < row1; i += kPatchT) {
+    const float ct = cos_t[i], st = sin_t[i];
+#pragma unroll 1
+    for (int j = lp; j < phi_samples; j += kPatchP) {
+      const float cp = cos_p[j], sp = sin_p[j];
+      Float3 d = to_world(t, b, n, f3(ct * sp, st * sp, cp));
+      Float3 c = sample_env(chain, tab, d, mip);
+      a0 += c.x * cp * sp;
+      a1 += c.y * cp * sp;
+      a2 += c.z * cp * sp;
     }
   }
-  part[warp][lane][0] = a0;
-  part[warp][lane][1] = a1;
-  part[warp][lane][2] = a2;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+  }
+  if (lane == 0) {
+    part[warp][0] = a0;
+    part[warp][1] = a1;
+    part[warp][2] = a2;
+  }
   __syncthreads();
-  if (warp == 0) {
-    float s0 = part[0][lane][0], s1 = part[0][lane][1], s2 = part[0][lane][2];
+  if (threadIdx.x == 0) {
+    float s0 = part[0][0], s1 = part[0][1], s2 = part[0][2];
 #pragma unroll
     for (int k = 1; k < kIrrWarps; ++k) {
-      s0 += part[k][lane][0];
-      s1 += part[k][lane][1];
-      s2 += part[k][lane][2];
+      s0 += part[k][0];
+      s1 += part[k][1];
+      s2 += part[k][2];
     }
-    partial[((long long)tile * gb_count + gb) * 32 + lane] = make_float4(s0, s1, s2, 0.0f);
+    partial[texel * gb_count + gb] = make_float4(s0, s1, s2, 0.0f);
   }
 }
 
 __global__ void __launch_bounds__(256) irradiance_finish_kernel(const float4* __restrict__ partial,
-                                                                int ow, int oh, int tiles_x,
-                                                                int tiles, int gb_count,
+                                                                int ow, int oh, int gb_count,
                                                                 int phi_samples,
                                                                 float4* __restrict__ out,
                                                                 long long pitch) {
-  int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= tiles * 32) return;
-  int tile = g / 32, lane = g % 32;
-  int x = (tile % tiles_x) * kIrrTileX + (lane % kIrrTileX);
-  int y = (tile / tiles_x) * kIrrTileY + (lane / kIrrTileX);
-  if (x >= ow || y >= oh) return;
-  const float4* p = partial + (long long)tile * gb_count * 32 + lane;
+  long long texel = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (texel >= (long long)ow * oh) return;
+  int x = (int)(texel % ow), y = (int)(texel / ow);
+  const float4* p = partial + texel * gb_count;
   float4 s = p[0];
   for (int k = 1; k < gb_count; ++k) {
-    float4 q = p[(long long)k * 32];
+    float4 q = p[k];
     s.x += q.x;
     s.y += q.y;
     s.z += q.z;
@@ -403,14 +428,24 @@ int launch_irradiance(const float* chain, int w, int h, float* out, int ow, int 
                       size_t pitch_bytes, void* ws, cudaStream_t st) {
   IrrPlan pl = irr_plan(w, h, ow, oh);
   float4* partial = reinterpret_cast<float4*>(ws);
-  irradiance_partial_kernel<<<pl.tiles * pl.gb, 32 * kIrrWarps, 0, st>>>(
-      reinterpret_cast<const float4*>(chain), w, h, ow, oh, pl.tiles_x, pl.gb, pl.phi, partial);
-  int n = pl.tiles * 32;
-  irradiance_finish_kernel<<<(n + 255) / 256, 256, 0, st>>>(
-      partial, ow, oh, pl.tiles_x, pl.tiles, pl.gb, pl.phi, reinterpret_cast<float4*>(out),
+  long long blocks = pl.texels * pl.gb;
+  if (blocks > 0x7fffffffLL)
+    return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "irradiance output too large");
+  size_t smem = 2 * (size_t)pl.phi * sizeof(float);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(irradiance_partial_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "irradiance smem attribute");
+  }
+  irradiance_partial_kernel<<<(unsigned)blocks, 32 * kIrrWarps, smem, st>>>(
+      reinterpret_cast<const float4*>(chain), w, h, ow, oh, pl.gb, pl.phi, partial);
+  long long n = pl.texels;
+  irradiance_finish_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+      partial, ow, oh, pl.gb, pl.phi, reinterpret_cast<float4*>(out),
       (long long)(pitch_bytes / sizeof(float4)));
   return cuda_status(cudaGetLastError(), "irradiance kernels launch");
 }
+
 
 // ---------------------------------------------------------------------------
 // Split-sum BRDF LUT (Karis 2013, IntegrateBRDF).  One thread per texel, N

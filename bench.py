@@ -47,7 +47,14 @@ FIRST_W, FIRST_H = 2048, 1024
 SAMPLES = 1024
 LUT_N, LUT_SAMPLES = 512, 1024
 WORKLOAD = ("4096x2048 RGBA32F env, 13-level chain, 128x64 irradiance, 9-mip GGX chain from "
-            "2048x1024 (roughness m/8), N=1024 ref-hash samples, 512x512 RG32F LUT, FP32")
+            "2048x1024 (roughness m/8), N=1024 {gen} samples, 512x512 RG32F LUT, FP32")
+# Sample generator of the prefilter: 1 = Hammersley (the benchmark configurations'
+# choice), 0 = the reference shader's hash RNG.  Set from --generator.
+GENERATOR = 1
+
+
+def workload():
+    return WORKLOAD.format(gen="Hammersley" if GENERATOR == 1 else "reference-hash")
 # DRAM bytes per prefilter launch from ncu (profiles/prefilter_c2_ncu.md); None until measured.
 NCU_PREFILTER_TRAFFIC = None
 
@@ -150,10 +157,10 @@ def cpu_sample_probe_time(env, kind_pref="reference", scale=1.0):
         xy = np.stack([idx % ow, idx // ow], 1).astype(np.int32)
         t0 = time.perf_counter()
         if use_ref:
-            oracle.ref_prefilter(chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, oracle.GEN_REF_HASH,
+            oracle.ref_prefilter(chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, GENERATOR,
                                  xy=xy, nthreads=cores)
         else:
-            oracle.prefilter(chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, oracle.GEN_REF_HASH, xy=xy,
+            oracle.prefilter(chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, GENERATOR, xy=xy,
                              nthreads=cores)
         dt = time.perf_counter() - t0
         spent += dt
@@ -190,11 +197,11 @@ def run_reference(args):
     from althea_gb300 import synth
     env = synth.make_env(ENV_W, ENV_H, seed=0, sun_max=1e4)
     for _ in range(args.warmup):
-        cpu_sample_probe_time(env, "reference", scale=0.25)
+        cpu_sample_probe_time(env, "reference", scale=8.0)
     times = []
     info = None
     for _ in range(args.steps):
-        per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference", scale=0.25)
+        per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference", scale=8.0)
         times.append(per_probe)
         info = (kind, cores, sample)
     sec = float(np.mean(times))
@@ -203,7 +210,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "path": "reference compute shaders compiled as C++ "
+            "config": {"workload": workload(), "path": "reference compute shaders compiled as C++ "
                        "(CPU, all host threads), extrapolated from a bounded texel sample"},
             "cpu_baseline": {"value": value, "unit": "probes/s", "cores": info[1],
                              "kind": info[0], "sample": info[2]},
@@ -251,7 +258,7 @@ def run_ours(args):
         ev[0].record(stream)
         ibl.build_env_chain_into(env_d, chain, stream)
         ev[1].record(stream)
-        ibl.prefilter(chain, ENV_W, ENV_H, mips, rough, SAMPLES, ibl.GEN_REF_HASH, stream)
+        ibl.prefilter(chain, ENV_W, ENV_H, mips, rough, SAMPLES, GENERATOR, stream)
         ev[2].record(stream)
         ibl.irradiance(chain, ENV_W, ENV_H, irr, ws, stream)
         ev[3].record(stream)
@@ -293,7 +300,7 @@ def run_ours(args):
     # ---- end to end through the public context API (host buffers) ----------
     cfg = ibl.make_config(ENV_W, ENV_H, irradiance_size=(IRR_W, IRR_H), mip_count=MIPS,
                           first_mip=(FIRST_W, FIRST_H), samples=SAMPLES,
-                          generator=ibl.GEN_REF_HASH, lut_size=LUT_N, lut_samples=LUT_SAMPLES)
+                          generator=GENERATOR, lut_size=LUT_N, lut_samples=LUT_SAMPLES)
     ctx = ibl.BakeContext(cfg)
     host_env = torch.from_numpy(env).pin_memory()
     e_irr, e_mips, e_lut = ctx.allocate_outputs(device=dev)
@@ -334,7 +341,7 @@ def run_ours(args):
         achieved = prefilter_algorithmic_bytes() / (pf_ms / 1e3) / 1e9
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
-            per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference")
+            per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference", scale=40.0)
             cpu = {"value": 1.0 / per_probe, "unit": "probes/s", "cores": cores, "kind": kind,
                    "sample": sample + f" ({spent:.1f} s of CPU work)"}
         line = {
@@ -342,7 +349,7 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded sky gradient x log-normal noise + 8 suns <= 1e4)",
-            "config": {"workload": WORKLOAD, "path": "plain (reference estimator, bit-identical "
+            "config": {"workload": workload(), "path": "plain (reference estimator, bit-identical "
                        "to the reference shaders; <=1e-4 contract)",
                        "global_batch": world, "parallelism": f"replicas x{world}",
                        "l2": "flushed (256 MB write) between timed steps",
@@ -373,7 +380,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--generator", default="hammersley", choices=["hammersley", "ref-hash"])
     args = ap.parse_args()
+    global GENERATOR
+    GENERATOR = 1 if args.generator == "hammersley" else 0
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
