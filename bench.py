@@ -341,7 +341,7 @@ def run_ours(args):
         achieved = prefilter_algorithmic_bytes() / (pf_ms / 1e3) / 1e9
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
-            per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference", scale=40.0)
+            per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference", scale=100.0)
             cpu = {"value": 1.0 / per_probe, "unit": "probes/s", "cores": cores, "kind": kind,
                    "sample": sample + f" ({spent:.1f} s of CPU work)"}
         line = {
