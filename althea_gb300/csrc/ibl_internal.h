@@ -24,7 +24,9 @@ const char* last_error();
 int check_env(int w, int h);
 int check_image(const void* p, int w, int h, size_t pitch, size_t texel_bytes, const char* what);
 int check_irradiance_args(int w, int h, int ow, int oh);
-IrrPlan irr_plan(int w, int h, int ow, int oh);
+// target_blocks: how many 256-thread blocks the split should aim for
+// (<= 0: 8 per SM of a 152-SM GB300).
+IrrPlan irr_plan(int w, int h, int ow, int oh, int target_blocks = 0);
 
 int launch_build_chain(const float* level0, int w, int h, float* chain, cudaStream_t st);
 int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_target* mips,

@@ -11,8 +11,8 @@
 #include <cstring>
 
 #include "althea_ibl.h"
-#include "ibl_device.cuh"
 #include "ibl_internal.h"
+#include "ibl_texel.cuh"
 
 namespace ibl {
 
@@ -46,24 +46,7 @@ __global__ void __launch_bounds__(256) blit_level_kernel(const float4* __restric
   int x = blockIdx.x * 32 + (threadIdx.x & 31);
   int y = blockIdx.y * 8 + (threadIdx.x >> 5);
   if (x >= dw || y >= dh) return;
-  float kx = (float)sw / (float)dw, ky = (float)sh / (float)dh;
-  float u = ((float)x + 0.5f) * kx - 0.5f;
-  float v = ((float)y + 0.5f) * ky - 0.5f;
-  float fx = floorf(u), fy = floorf(v);
-  float a = u - fx, b = v - fy;
-  int i0 = min(max((int)fx, 0), sw - 1), i1 = min(max((int)fx + 1, 0), sw - 1);
-  int j0 = min(max((int)fy, 0), sh - 1), j1 = min(max((int)fy + 1, 0), sh - 1);
-  const float4* r0 = src + (long long)j0 * sw;
-  const float4* r1 = src + (long long)j1 * sw;
-  float4 t00 = __ldg(r0 + i0), t10 = __ldg(r0 + i1), t01 = __ldg(r1 + i0), t11 = __ldg(r1 + i1);
-  float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b);
-  float w01 = (1.0f - a) * b, w11 = a * b;
-  float4 o;
-  o.x = ((w00 * t00.x + w10 * t10.x) + w01 * t01.x) + w11 * t11.x;
-  o.y = ((w00 * t00.y + w10 * t10.y) + w01 * t01.y) + w11 * t11.y;
-  o.z = ((w00 * t00.z + w10 * t10.z) + w01 * t01.z) + w11 * t11.z;
-  o.w = ((w00 * t00.w + w10 * t10.w) + w01 * t01.w) + w11 * t11.w;
-  dst[(long long)y * dw + x] = o;
+  dst[(long long)y * dw + x] = blit_texel(src, sw, sh, dw, dh, x, y);
 }
 
 int launch_build_chain(const float* level0, int w, int h, float* chain, cudaStream_t st) {
@@ -109,62 +92,6 @@ struct PrefilterParams {
   PrefilterJob jobs[ALTHEA_IBL_MAX_MIPS];
 };
 
-__device__ __forceinline__ void prefilter_texel_degenerate(const float4* __restrict__ chain,
-                                                           const ChainTable& tab, Float3 n,
-                                                           Float3 t, Float3 b, uint32_t sx,
-                                                           uint32_t sy, int samples, int gen,
-                                                           float* acc, float& total) {
-  // roughness == 0: a2 = 0 makes sampleGGX return (cos(phi)*0, sin(phi)*0, 1),
-  // so every sample with xi.y < 1 yields the same H = n, the same L and the
-  // same texel value; xi.y == 1 gives 0/0 and the sample fails NdotL > 0
-  // (:163).  Evaluate the first kept sample once, then repeat the serial
-  // float accumulation for every kept sample, which is what the loop of
-  // :147-167 computes.
-  float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, ndotl = 0.0f;
-  bool have = false;
-#pragma unroll 4
-  for (int i = 0; i < samples; ++i) {
-    // Only xi.y decides whether a sample survives; xi.x is drawn for the
-    // first kept sample alone.
-    float xi_y;
-    if (gen == ALTHEA_IBL_GEN_HAMMERSLEY) {
-      xi_y = __uint2float_rn(__brev((uint32_t)i)) * (1.0f / 4294967296.0f);
-    } else {
-      xi_y = hash_float(hash_bits(sx + 2u * (uint32_t)i + 2u, sy + 2u * (uint32_t)i + 2u));
-    }
-    if (xi_y == 1.0f) continue;  // NaN sample, dropped by NdotL > 0
-    if (!have) {
-      float xi_x = gen == ALTHEA_IBL_GEN_HAMMERSLEY
-                       ? (float)i / (float)samples
-                       : hash_float(hash_bits(sx + 2u * (uint32_t)i + 1u,
-                                              sy + 2u * (uint32_t)i + 1u));
-      Float3 hv = to_world(t, b, n, sample_ggx(xi_x, xi_y, 0.0f));
-      float vdh = (n.x * hv.x + n.y * hv.y) + n.z * hv.z;
-      float k = 2.0f * vdh;
-      Float3 l = normalize3(f3(k * hv.x - n.x, k * hv.y - n.y, k * hv.z - n.z));
-      ndotl = glsl_max((n.x * l.x + n.y * l.y) + n.z * l.z, 0.0f);
-      if (ndotl > 0.0f) {
-        Float3 c = sample_env(chain, tab, l, 0.0f);
-        c0 = c.x * ndotl;
-        c1 = c.y * ndotl;
-        c2 = c.z * ndotl;
-      }
-      have = true;
-    }
-    if (ndotl > 0.0f) {
-      acc[0] += c0;
-      acc[1] += c1;
-      acc[2] += c2;
-      total += ndotl;
-    }
-  }
-}
-
-// Hammersley xi does not depend on the texel, so neither does sampleGGX's
-// local half-vector: blocks of a roughness > 0 mip tabulate it once in shared
-// memory when it fits (same operations, same values).
-constexpr int kMaxTabulatedSamples = 2048;
-
 __global__ void __launch_bounds__(kPfTileX* kPfTileY) prefilter_kernel(const PrefilterParams p) {
   __shared__ ChainTable tab;
   __shared__ PrefilterJob job;
@@ -182,85 +109,16 @@ __global__ void __launch_bounds__(kPfTileX* kPfTileY) prefilter_kernel(const Pre
   __syncthreads();
   const bool tabulated = p.tabulate && job.roughness != 0.0f;
   if (tabulated) {
-    const float a2t = job.roughness * job.roughness;
-    for (int i = threadIdx.x; i < p.samples; i += blockDim.x) {
-      float xi_x, xi_y;
-      hammersley(i, p.samples, xi_x, xi_y);
-      Float3 hl = sample_ggx(xi_x, xi_y, a2t);
-      h_local[3 * i] = hl.x;
-      h_local[3 * i + 1] = hl.y;
-      h_local[3 * i + 2] = hl.z;
-    }
+    tabulate_hammersley(h_local, p.samples, job.roughness);
     __syncthreads();
   }
   int local = (int)blockIdx.x - job.block_begin;
   int x = (local % job.tiles_x) * kPfTileX + (int)(threadIdx.x % kPfTileX);
   int y = (local / job.tiles_x) * kPfTileY + (int)(threadIdx.x / kPfTileX);
   if (x >= job.ow || y >= job.oh) return;
-
-  const float4* __restrict__ chain = p.chain;
-  const int samples = p.samples;
-  Float3 n = texel_dir(x, y, job.ow, job.oh);
-  Float3 t, b;
-  local_frame(n, t, b);
-  const float roughness = job.roughness;
-  const float a2 = roughness * roughness;
-  float acc[3] = {0.0f, 0.0f, 0.0f};
-  float total = 0.0f;
-
-  if (roughness == 0.0f) {
-    prefilter_texel_degenerate(chain, tab, n, t, b, (uint32_t)x, (uint32_t)y, samples,
-                               p.generator, acc, total);
-  } else {
-    const float sa_texel = 4.0f * kPi / (6.0f * (float)p.w * (float)p.h);
-    const float rcp_sa_texel = 1.0f / sa_texel;
-    const float fsamples = (float)samples;
-    uint32_t sx = (uint32_t)x, sy = (uint32_t)y;
-#pragma unroll 1
-    for (int i = 0; i < samples; ++i) {
-      Float3 hl;
-      if (tabulated) {
-        hl = f3(h_local[3 * i], h_local[3 * i + 1], h_local[3 * i + 2]);
-      } else {
-        float xi_x, xi_y;
-        if (p.generator == ALTHEA_IBL_GEN_HAMMERSLEY) {
-          hammersley(i, samples, xi_x, xi_y);
-        } else {
-          sx += 1u;
-          sy += 1u;
-          xi_x = hash_float(hash_bits(sx, sy));
-          sx += 1u;
-          sy += 1u;
-          xi_y = hash_float(hash_bits(sx, sy));
-        }
-        hl = sample_ggx(xi_x, xi_y, a2);
-      }
-      Float3 hv = to_world(t, b, n, hl);
-      // V = R = N (:136-137): V.H, N.H and H.V are one and the same sum.
-      float vdh = (n.x * hv.x + n.y * hv.y) + n.z * hv.z;
-      float k = 2.0f * vdh;
-      Float3 l = normalize3(f3(k * hv.x - n.x, k * hv.y - n.y, k * hv.z - n.z));
-      float ndotl = glsl_max((n.x * l.x + n.y * l.y) + n.z * l.z, 0.0f);
-      if (ndotl > 0.0f) {
-        float ndoth = glsl_max(vdh, 0.0f);
-        float d = distribution_ggx(ndoth, a2);
-        float pdf = d * ndoth / (4.0f * ndoth + 0.00001f);
-        float sa_sample = 1.0f / (fsamples * pdf + 0.0001f);
-        float mip = 0.5f * agb_log2(agb_div_rcp(sa_sample, sa_texel, rcp_sa_texel));
-        Float3 c = sample_env(chain, tab, l, mip);
-        acc[0] += c.x * ndotl;
-        acc[1] += c.y * ndotl;
-        acc[2] += c.z * ndotl;
-        total += ndotl;
-      }
-    }
-  }
-  float4 o;
-  o.x = acc[0] / total;
-  o.y = acc[1] / total;
-  o.z = acc[2] / total;
-  o.w = 1.0f;
-  job.out[(long long)y * job.pitch + x] = o;
+  job.out[(long long)y * job.pitch + x] =
+      prefilter_texel(p.chain, tab, p.w, p.h, x, y, job.ow, job.oh, job.roughness, p.samples,
+                      p.generator, tabulated ? h_local : nullptr);
 }
 
 int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
@@ -294,36 +152,22 @@ int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_targ
 
 // ---------------------------------------------------------------------------
 // Irradiance (GenIrradianceMap.comp:106-155).  One output texel's 300 x Nphi
-// grid is split over G = 8*GB warps (GB blocks of 8 warps per texel), each
-// warp taking a contiguous band of theta rows.  Inside a warp the 32 lanes
-// cover a 4 (theta) x 8 (phi) patch of neighbouring grid directions, so one
-// gather instruction touches a compact patch of the env level.  Each lane sums
-// its samples in grid order; lanes are combined by a fixed xor-shuffle tree,
-// warps in order by the block, and the GB block partials in order by a second
-// kernel: deterministic, and within float rounding of the serial sum.
+// grid is cut into 32 fixed bands of theta rows, summed by warps whose 32
+// lanes cover a 4 (theta) x 8 (phi) patch of neighbouring grid directions
+// (so one gather instruction touches a compact patch of the env level); band
+// sums are combined by one fixed binary tree.  GB = 1, 2 or 4 blocks share a
+// texel, each reducing an aligned subtree; a second kernel applies the top
+// levels.  Deterministic, independent of GB, and within float rounding of the
+// shader's serial sum.
 // ---------------------------------------------------------------------------
-constexpr int kIrrWarps = 8;
-constexpr int kPatchT = 4, kPatchP = 8;
-constexpr int kThetaSamples = 300;  // GenIrradianceMap.comp:119
-constexpr int kMaxPhiSamples = 4096;
-
-__host__ __device__ inline int irr_phi_samples(int w, int h) {
-  // int(pushConstants.height * thetaSamples / pushConstants.width) (:120-121)
-  return (int)((float)h * (float)kThetaSamples / (float)w);
-}
-
-IrrPlan irr_plan(int w, int h, int ow, int oh) {
+IrrPlan irr_plan(int w, int h, int ow, int oh, int target_blocks) {
   IrrPlan pl;
   pl.phi = irr_phi_samples(w, h);
   long long texels = (long long)ow * oh;
   pl.texels = texels;
-  const long long target_blocks = 152LL * 8;
-  long long gb = (target_blocks + texels - 1) / texels;
-  const long long gb_max = kThetaSamples / (kPatchT * kIrrWarps);  // >= 4 theta rows a warp
-  if (gb > gb_max) gb = gb_max;
-  if (gb < 1) gb = 1;
-  pl.gb = (int)gb;
-  pl.workspace = (size_t)texels * (size_t)gb * sizeof(float4);
+  if (target_blocks <= 0) target_blocks = 152 * 8;
+  pl.gb = irradiance_split(texels, target_blocks);
+  pl.workspace = (size_t)texels * (size_t)pl.gb * sizeof(float4);
   return pl;
 }
 
@@ -332,71 +176,21 @@ __global__ void __launch_bounds__(32 * kIrrWarps) irradiance_partial_kernel(
     float4* __restrict__ partial) {
   __shared__ ChainTable tab;
   __shared__ float cos_t[kThetaSamples], sin_t[kThetaSamples];
-  __shared__ float part[kIrrWarps][3];
+  __shared__ float band_smem[kBands][3];
   extern __shared__ float phi_table[];  // 2 * phi_samples floats
   float* cos_p = phi_table;
   float* sin_p = phi_table + phi_samples;
   if (threadIdx.x == 0) make_table(w, h, &tab);
-  for (int i = threadIdx.x; i < kThetaSamples; i += blockDim.x) {
-    // theta = i * 2 * PI / thetaSamples (:127): int i*2, then float.
-    float theta = (float)(i * 2) * kPi / (float)kThetaSamples;
-    agb_sincos(theta, &sin_t[i], &cos_t[i]);
-  }
-  for (int j = threadIdx.x; j < phi_samples; j += blockDim.x) {
-    float phi = (float)j * 0.5f * kPi / (float)phi_samples;  // :132
-    agb_sincos(phi, &sin_p[j], &cos_p[j]);
-  }
+  irradiance_tables(cos_t, sin_t, cos_p, sin_p, phi_samples);
   __syncthreads();
 
   const long long texel = blockIdx.x / gb_count;
   const int gb = blockIdx.x % gb_count;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int x = (int)(texel % ow), y = (int)(texel / ow);
-  Float3 n = texel_dir(x, y, ow, oh);
-  Float3 t, b;
-  local_frame(n, t, b);
-  const float mip = agb_log2((float)w / (float)kThetaSamples);  // :124
-  const int groups = gb_count * kIrrWarps;
-  const int g = gb * kIrrWarps + warp;
-  const int row0 = (int)((long long)g * kThetaSamples / groups);
-  const int row1 = (int)((long long)(g + 1) * kThetaSamples / groups);
-  const int lt = lane / kPatchP, lp = lane % kPatchP;
-  float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-#pragma unroll 1
-  for (int i = row0 + lt; i < row1; i += kPatchT) {
-    const float ct = cos_t[i], st = sin_t[i];
-#pragma unroll 1
-    for (int j = lp; j < phi_samples; j += kPatchP) {
-      const float cp = cos_p[j], sp = sin_p[j];
-      Float3 d = to_world(t, b, n, f3(ct * sp, st * sp, cp));
-      Float3 c = sample_env(chain, tab, d, mip);
-      a0 += c.x * cp * sp;
-      a1 += c.y * cp * sp;
-      a2 += c.z * cp * sp;
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-  }
-  if (lane == 0) {
-    part[warp][0] = a0;
-    part[warp][1] = a1;
-    part[warp][2] = a2;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float s0 = part[0][0], s1 = part[0][1], s2 = part[0][2];
-#pragma unroll
-    for (int k = 1; k < kIrrWarps; ++k) {
-      s0 += part[k][0];
-      s1 += part[k][1];
-      s2 += part[k][2];
-    }
-    partial[texel * gb_count + gb] = make_float4(s0, s1, s2, 0.0f);
-  }
+  const int count = kBands / gb_count;
+  Float3 s = irradiance_block_bands(chain, tab, w, (int)(texel % ow), (int)(texel / ow), ow, oh,
+                                    gb * count, count, phi_samples, cos_t, sin_t, cos_p, sin_p,
+                                    band_smem);
+  if (threadIdx.x == 0) partial[texel * gb_count + gb] = make_float4(s.x, s.y, s.z, 0.0f);
 }
 
 __global__ void __launch_bounds__(256) irradiance_finish_kernel(const float4* __restrict__ partial,
@@ -407,21 +201,8 @@ __global__ void __launch_bounds__(256) irradiance_finish_kernel(const float4* __
   long long texel = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (texel >= (long long)ow * oh) return;
   int x = (int)(texel % ow), y = (int)(texel / ow);
-  const float4* p = partial + texel * gb_count;
-  float4 s = p[0];
-  for (int k = 1; k < gb_count; ++k) {
-    float4 q = p[k];
-    s.x += q.x;
-    s.y += q.y;
-    s.z += q.z;
-  }
-  // vec4(PI * irradiance / float(thetaSamples) / float(phiSamples), 1.0) (:145)
-  float4 o;
-  o.x = kPi * s.x / (float)kThetaSamples / (float)phi_samples;
-  o.y = kPi * s.y / (float)kThetaSamples / (float)phi_samples;
-  o.z = kPi * s.z / (float)kThetaSamples / (float)phi_samples;
-  o.w = 1.0f;
-  out[(long long)y * pitch + x] = o;
+  Float3 s = combine_partials(partial + texel * gb_count, gb_count);
+  out[(long long)y * pitch + x] = irradiance_finish(s.x, s.y, s.z, phi_samples);
 }
 
 int launch_irradiance(const float* chain, int w, int h, float* out, int ow, int oh,
@@ -445,8 +226,6 @@ int launch_irradiance(const float* chain, int w, int h, float* out, int ow, int 
       (long long)(pitch_bytes / sizeof(float4)));
   return cuda_status(cudaGetLastError(), "irradiance kernels launch");
 }
-
-
 // ---------------------------------------------------------------------------
 // Split-sum BRDF LUT (Karis 2013, IntegrateBRDF).  One thread per texel, N
 // Hammersley samples in order; FP32 (it is not a contraction).

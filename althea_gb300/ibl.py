@@ -63,6 +63,33 @@ class Outputs(ctypes.Structure):
                 ("lut_dev", ctypes.c_void_p), ("lut_pitch_bytes", ctypes.c_size_t)]
 
 
+class Probe(ctypes.Structure):
+    _fields_ = [("level0_dev", ctypes.c_void_p), ("chain_dev", ctypes.c_void_p),
+                ("env_width", ctypes.c_int), ("env_height", ctypes.c_int),
+                ("irradiance_dev", ctypes.c_void_p), ("irradiance_width", ctypes.c_int),
+                ("irradiance_height", ctypes.c_int), ("irradiance_pitch_bytes", ctypes.c_size_t),
+                ("mip_count", ctypes.c_int), ("mip_dev", ctypes.c_void_p * MAX_MIPS),
+                ("mip_pitch_bytes", ctypes.c_size_t * MAX_MIPS),
+                ("mip_width", ctypes.c_int * MAX_MIPS), ("mip_height", ctypes.c_int * MAX_MIPS),
+                ("mip_roughness", ctypes.c_float * MAX_MIPS)]
+
+
+class BatchParams(ctypes.Structure):
+    _fields_ = [("samples", ctypes.c_int), ("generator", ctypes.c_int),
+                ("lut_dev", ctypes.c_void_p), ("lut_size", ctypes.c_int),
+                ("lut_pitch_bytes", ctypes.c_size_t), ("lut_samples", ctypes.c_int),
+                ("lut_orientation", ctypes.c_int), ("flags", ctypes.c_int)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "probes", "prefilter_jobs", "prefilter_tiles", "irradiance_blocks", "tile_x", "tile_y",
+        "persistent_blocks", "irradiance_target_blocks", "tuned", "graph")]
+
+
+BATCH_AUTOTUNE = 1
+BATCH_GRAPH = 2
+
 _lib = None
 
 
@@ -102,6 +129,11 @@ def load(build_if_missing: bool = True):
         "althea_ibl_upload_env": (i, [vp, vp, i, vp]),
         "althea_ibl_env_chain": (vp, [vp]),
         "althea_ibl_bake": (i, [vp, ctypes.POINTER(Outputs), vp]),
+        "althea_ibl_batch_create": (i, [ctypes.POINTER(Probe), i, ctypes.POINTER(BatchParams), vp,
+                                        ctypes.POINTER(vp)]),
+        "althea_ibl_batch_run": (i, [vp, vp]),
+        "althea_ibl_batch_describe": (i, [vp, ctypes.POINTER(BatchInfo)]),
+        "althea_ibl_batch_destroy": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -394,3 +426,106 @@ class ImageBasedLighting:
     def buildLayout() -> List[str]:
         # Src/ImageBasedLighting.cpp:607-619: four texture bindings.
         return ["environmentMap", "prefilteredMap", "irradianceMap", "brdfLut"]
+
+
+# ---- batches -------------------------------------------------------------------
+
+@dataclass
+class ProbeSpec:
+    """One probe of a batch: its env size, chain of mips and irradiance size."""
+    env_width: int
+    env_height: int
+    mip_sizes: List[tuple]
+    roughness: List[float]
+    irradiance_size: Optional[tuple] = (32, 16)
+
+
+def spec_for(env_width: int, env_height: int, mip_count: Optional[int] = None,
+             irradiance_size=(32, 16)) -> ProbeSpec:
+    """Batch-config probe: mips from W/2, mip_count = log2(W) - 3 by default,
+    roughness m/(M-1)."""
+    if mip_count is None:
+        mip_count = max(1, env_width.bit_length() - 1 - 3)
+    sizes = [(max((env_width >> 1) >> m, 1), max((env_height >> 1) >> m, 1))
+             for m in range(mip_count)]
+    rough = [m / (mip_count - 1) if mip_count > 1 else 0.0 for m in range(mip_count)]
+    return ProbeSpec(env_width, env_height, sizes, rough, irradiance_size)
+
+
+class ProbeBatch:
+    """Device buffers and a batch plan for many probes (althea_ibl_batch_*).
+
+    ``levels0``: per-probe CUDA (H, W, 4) env tensors (the chain is rebuilt from
+    them on every run).  Outputs are allocated here and exposed as
+    ``chains``, ``mips`` (list of lists), ``irradiance`` and ``lut``."""
+
+    def __init__(self, specs: List[ProbeSpec], levels0: List, samples: int = 1024,
+                 generator: int = GEN_HAMMERSLEY, lut_size: int = 0, lut_samples: int = 1024,
+                 lut_orientation: int = LUT_ASSET, autotune: bool = True, graph: bool = True,
+                 stream=None, device="cuda"):
+        torch = _torch()
+        self.specs = specs
+        self.levels0 = levels0
+        self.chains, self.mips, self.irradiance = [], [], []
+        n = len(specs)
+        self._probes = (Probe * max(n, 1))()
+        for i, (s, env) in enumerate(zip(specs, levels0)):
+            _require_cuda(env, f"env {i}", 4)
+            if tuple(env.shape[:2]) != (s.env_height, s.env_width):
+                raise IBLError(ERR_INVALID_ARGUMENT, f"env {i} shape {tuple(env.shape)}")
+            chain = torch.empty((chain_texels(s.env_width, s.env_height), 4),
+                                dtype=torch.float32, device=device)
+            mips = [torch.empty((h, w, 4), dtype=torch.float32, device=device)
+                    for w, h in s.mip_sizes]
+            irr = None
+            if s.irradiance_size is not None:
+                iw, ih = s.irradiance_size
+                irr = torch.empty((ih, iw, 4), dtype=torch.float32, device=device)
+            self.chains.append(chain)
+            self.mips.append(mips)
+            self.irradiance.append(irr)
+            p = self._probes[i]
+            p.level0_dev = env.data_ptr()
+            p.chain_dev = chain.data_ptr()
+            p.env_width, p.env_height = s.env_width, s.env_height
+            if irr is not None:
+                p.irradiance_dev = irr.data_ptr()
+                p.irradiance_width, p.irradiance_height = s.irradiance_size
+                p.irradiance_pitch_bytes = _pitch(irr, 4)
+            p.mip_count = len(mips)
+            for m, (t, r) in enumerate(zip(mips, s.roughness)):
+                p.mip_dev[m] = t.data_ptr()
+                p.mip_pitch_bytes[m] = _pitch(t, 4)
+                p.mip_width[m], p.mip_height[m] = t.shape[1], t.shape[0]
+                p.mip_roughness[m] = float(r)
+        self.lut = None
+        params = BatchParams()
+        params.samples, params.generator = samples, generator
+        if lut_size > 0:
+            self.lut = torch.empty((lut_size, lut_size, 2), dtype=torch.float32, device=device)
+            params.lut_dev, params.lut_size = self.lut.data_ptr(), lut_size
+            params.lut_pitch_bytes = _pitch(self.lut, 2)
+            params.lut_samples, params.lut_orientation = lut_samples, lut_orientation
+        params.flags = (BATCH_AUTOTUNE if autotune else 0) | (BATCH_GRAPH if graph else 0)
+        self._plan = ctypes.c_void_p()
+        _check(load().althea_ibl_batch_create(self._probes, n, ctypes.byref(params),
+                                              _stream_ptr(stream), ctypes.byref(self._plan)))
+
+    def run(self, stream=None) -> None:
+        _check(load().althea_ibl_batch_run(self._plan, _stream_ptr(stream)))
+
+    def info(self) -> BatchInfo:
+        inf = BatchInfo()
+        _check(load().althea_ibl_batch_describe(self._plan, ctypes.byref(inf)))
+        return inf
+
+    def close(self) -> None:
+        if self._plan:
+            load().althea_ibl_batch_destroy(self._plan)
+            self._plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

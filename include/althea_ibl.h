@@ -171,6 +171,66 @@ const float* althea_ibl_env_chain(const althea_ibl_context* ctx);
  * buffers: the dispatch sequence of Src/ImageBasedLighting.cpp:315-402. */
 int althea_ibl_bake(althea_ibl_context* ctx, const althea_ibl_outputs* outs, void* stream);
 
+/* ---- batched bakes -----------------------------------------------------------
+ * No single counterpart in the reference, which bakes one probe per
+ * createResources call (Src/GlobalResources.cpp:18-22); a batch bakes many
+ * probes of uneven size and mip count as one CUDA-graph launch:
+ *   env chains (one launch per level index over all probes), a persistent
+ *   prefilter kernel draining a (probe, mip, tile) work queue, a batched
+ *   irradiance and an optional shared LUT.
+ * Results are identical to baking each probe alone with the stateless calls.
+ * With ALTHEA_IBL_BATCH_AUTOTUNE the plan times its candidate tile shapes and
+ * irradiance split factors once per batch shape and caches the choice (in
+ * memory, and in the file named by $ALTHEA_IBL_TUNE_CACHE when set). */
+typedef struct {
+  const float* level0_dev;   /* env level 0; NULL if chain_dev already holds the chain */
+  float* chain_dev;          /* althea_ibl_chain_texels(W, H) RGBA32F texels */
+  int env_width, env_height;
+  float* irradiance_dev;     /* may be NULL: no irradiance for this probe */
+  int irradiance_width, irradiance_height;
+  size_t irradiance_pitch_bytes;
+  int mip_count;
+  float* mip_dev[ALTHEA_IBL_MAX_MIPS];
+  size_t mip_pitch_bytes[ALTHEA_IBL_MAX_MIPS];
+  int mip_width[ALTHEA_IBL_MAX_MIPS], mip_height[ALTHEA_IBL_MAX_MIPS];
+  float mip_roughness[ALTHEA_IBL_MAX_MIPS];
+} althea_ibl_probe;
+
+#define ALTHEA_IBL_BATCH_AUTOTUNE 1
+#define ALTHEA_IBL_BATCH_GRAPH 2
+
+typedef struct {
+  int samples;
+  int generator;
+  float* lut_dev;            /* shared RG32F LUT, or NULL */
+  int lut_size;
+  size_t lut_pitch_bytes;
+  int lut_samples;
+  int lut_orientation;
+  int flags;                 /* ALTHEA_IBL_BATCH_* */
+} althea_ibl_batch_params;
+
+typedef struct {
+  int probes, prefilter_jobs, prefilter_tiles, irradiance_blocks;
+  int tile_x, tile_y;        /* prefilter tile chosen */
+  int persistent_blocks;     /* prefilter grid */
+  int irradiance_target_blocks;
+  int tuned;                 /* 1 if the choice came from timing (now or cached) */
+  int graph;                 /* 1 once the bake is a captured CUDA graph */
+} althea_ibl_batch_info;
+
+typedef struct althea_ibl_batch althea_ibl_batch;
+
+/* Builds the plan (copies the probe table to the device; autotunes when
+ * asked, which runs the batch on `stream`).  Probe buffers must outlive it. */
+int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
+                            const althea_ibl_batch_params* params, void* stream,
+                            althea_ibl_batch** out);
+/* Bakes every probe (chains when level0_dev is set, mips, irradiance, LUT). */
+int althea_ibl_batch_run(althea_ibl_batch* batch, void* stream);
+int althea_ibl_batch_describe(const althea_ibl_batch* batch, althea_ibl_batch_info* info);
+int althea_ibl_batch_destroy(althea_ibl_batch* batch);
+
 const char* althea_ibl_last_error(void);
 int althea_ibl_abi_version(void);
 
