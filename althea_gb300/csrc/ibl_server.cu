@@ -1,0 +1,351 @@
+// ibl_server.cu -- continuous probe re-baking under a device-memory budget.
+//
+// Requests arrive at any time (althea_ibl_server_submit).  A request is
+// admitted as soon as a slot (a CUDA stream) is free and its device block
+// (env chain + outputs + irradiance scratch) fits the budget; otherwise it
+// waits in FIFO order and is admitted by a later submit or poll once earlier
+// requests retire.  Admitted requests run concurrently, one stream each:
+//   H2D env -> chain build -> prefilter (all mips) -> irradiance -> D2H
+// and a host callback on the stream stamps the completion time.  Device
+// blocks come from a pool with exact-size free lists: memory is allocated once
+// per size class and reused, so the request path issues no cudaFree (which
+// would synchronise the device); free blocks of other sizes are released only
+// when a new size class would otherwise exceed the budget.
+//
+// Host code only; the kernels are the single-probe ones (ibl_plain.cu), whose
+// results do not depend on what else runs on the device.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <deque>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "althea_ibl.h"
+#include "ibl_internal.h"
+
+namespace {
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct Layout {
+  size_t chain_off, mips_off, irr_off, ws_off, total;
+  size_t mips_bytes, irr_bytes, ws_bytes;
+  int mip_w[ALTHEA_IBL_MAX_MIPS], mip_h[ALTHEA_IBL_MAX_MIPS];
+};
+
+struct Slot {
+  cudaStream_t stream = nullptr;
+  bool busy = false;
+  std::atomic<int> done{0};
+  double done_s = 0.0;
+  althea_ibl_completion info{};
+  void* block = nullptr;
+  size_t bytes = 0;
+  int status = ALTHEA_IBL_OK;
+};
+
+struct Pending {
+  althea_ibl_request req;
+  double submit_s;
+};
+
+}  // namespace
+
+struct althea_ibl_server {
+  althea_ibl_server_config cfg{};
+  std::vector<Slot*> slots;
+  std::deque<Pending> queue;
+  std::vector<althea_ibl_completion> finished;  // retired, not yet returned
+  std::map<size_t, std::vector<void*>> free_blocks;
+  size_t reserved = 0, in_use = 0, peak = 0;
+  uint64_t completed = 0, rejected = 0;
+};
+
+namespace {
+
+void CUDART_CB on_done(void* p) {
+  Slot* s = static_cast<Slot*>(p);
+  s->done_s = now_s();
+  s->done.store(1, std::memory_order_release);
+}
+
+Layout layout_for(const althea_ibl_server* s, int w, int h, int mips) {
+  Layout L{};
+  size_t off = 0;
+  L.chain_off = off;
+  off = align256(off + althea_ibl_chain_texels(w, h) * 16);
+  L.mips_off = off;
+  size_t mb = 0;
+  int fw = w >> 1 < 1 ? 1 : w >> 1, fh = h >> 1 < 1 ? 1 : h >> 1;
+  for (int m = 0; m < mips; ++m) {
+    L.mip_w[m] = (fw >> m) < 1 ? 1 : (fw >> m);
+    L.mip_h[m] = (fh >> m) < 1 ? 1 : (fh >> m);
+    mb += (size_t)L.mip_w[m] * L.mip_h[m] * 16;
+  }
+  L.mips_bytes = mb;
+  off = align256(off + mb);
+  L.irr_off = off;
+  L.irr_bytes = (size_t)s->cfg.irradiance_width * s->cfg.irradiance_height * 16;
+  off = align256(off + L.irr_bytes);
+  L.ws_off = off;
+  L.ws_bytes = ibl::irr_plan(w, h, s->cfg.irradiance_width, s->cfg.irradiance_height).workspace;
+  off = align256(off + L.ws_bytes);
+  L.total = off;
+  return L;
+}
+
+// Block of exactly `bytes` from the pool; false when it cannot fit now.
+bool pool_acquire(althea_ibl_server* s, size_t bytes, void** out) {
+  if (s->in_use + bytes > s->cfg.budget_bytes) return false;
+  auto it = s->free_blocks.find(bytes);
+  if (it != s->free_blocks.end() && !it->second.empty()) {
+    *out = it->second.back();
+    it->second.pop_back();
+    s->in_use += bytes;
+    if (s->in_use > s->peak) s->peak = s->in_use;
+    return true;
+  }
+  // A new block: release idle blocks of other sizes until it fits.
+  while (s->reserved + bytes > s->cfg.budget_bytes) {
+    bool freed = false;
+    for (auto& kv : s->free_blocks) {
+      if (!kv.second.empty()) {
+        cudaFree(kv.second.back());
+        kv.second.pop_back();
+        s->reserved -= kv.first;
+        freed = true;
+        break;
+      }
+    }
+    if (!freed) return false;
+  }
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  s->reserved += bytes;
+  s->in_use += bytes;
+  if (s->in_use > s->peak) s->peak = s->in_use;
+  *out = p;
+  return true;
+}
+
+void pool_release(althea_ibl_server* s, void* p, size_t bytes) {
+  s->free_blocks[bytes].push_back(p);
+  s->in_use -= bytes;
+}
+
+int start(althea_ibl_server* s, Slot* slot, const Pending& pend, const Layout& L) {
+  const althea_ibl_request& r = pend.req;
+  cudaStream_t st = slot->stream;
+  char* base = static_cast<char*>(slot->block);
+  float* chain = reinterpret_cast<float*>(base + L.chain_off);
+  int status = ALTHEA_IBL_OK;
+  cudaError_t e = cudaMemcpyAsync(chain, r.env_host, (size_t)r.env_width * r.env_height * 16,
+                                  cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) status = ibl::cuda_status(e, "server env upload");
+  if (!status) status = ibl::launch_build_chain(chain, r.env_width, r.env_height, chain, st);
+  althea_ibl_mip_target mips[ALTHEA_IBL_MAX_MIPS];
+  size_t off = L.mips_off;
+  for (int m = 0; m < r.mip_count; ++m) {
+    mips[m].out_dev = reinterpret_cast<float*>(base + off);
+    mips[m].pitch_bytes = (size_t)L.mip_w[m] * 16;
+    mips[m].width = L.mip_w[m];
+    mips[m].height = L.mip_h[m];
+    mips[m].roughness = r.mip_count > 1 ? (float)m / (float)(r.mip_count - 1) : 0.0f;
+    off += (size_t)L.mip_w[m] * L.mip_h[m] * 16;
+  }
+  if (!status)
+    status = ibl::launch_prefilter(chain, r.env_width, r.env_height, mips, r.mip_count,
+                                   s->cfg.samples, s->cfg.generator, st);
+  if (!status && r.irradiance_host)
+    status = ibl::launch_irradiance(chain, r.env_width, r.env_height,
+                                    reinterpret_cast<float*>(base + L.irr_off),
+                                    s->cfg.irradiance_width, s->cfg.irradiance_height,
+                                    (size_t)s->cfg.irradiance_width * 16, base + L.ws_off, st);
+  if (!status && r.mips_host && L.mips_bytes) {
+    e = cudaMemcpyAsync(r.mips_host, base + L.mips_off, L.mips_bytes, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) status = ibl::cuda_status(e, "server mips download");
+  }
+  if (!status && r.irradiance_host) {
+    e = cudaMemcpyAsync(r.irradiance_host, base + L.irr_off, L.irr_bytes, cudaMemcpyDeviceToHost,
+                        st);
+    if (e != cudaSuccess) status = ibl::cuda_status(e, "server irradiance download");
+  }
+  slot->status = status;
+  slot->done.store(0, std::memory_order_relaxed);
+  e = cudaLaunchHostFunc(st, on_done, slot);
+  if (e != cudaSuccess) {
+    // No callback queued: wait here so the slot can still be retired.
+    cudaStreamSynchronize(st);
+    on_done(slot);
+    if (!slot->status) slot->status = ibl::cuda_status(e, "server completion callback");
+  }
+  return status;
+}
+
+void admit(althea_ibl_server* s) {
+  while (!s->queue.empty()) {
+    const Pending& head = s->queue.front();
+    Layout L = layout_for(s, head.req.env_width, head.req.env_height, head.req.mip_count);
+    if (L.total > s->cfg.budget_bytes) {  // can never fit
+      althea_ibl_completion c{};
+      c.tag = head.req.tag;
+      c.status = ALTHEA_IBL_ERR_BUDGET;
+      c.submit_s = c.start_s = c.done_s = head.submit_s;
+      s->finished.push_back(c);
+      s->rejected++;
+      s->queue.pop_front();
+      continue;
+    }
+    Slot* free_slot = nullptr;
+    for (Slot* sl : s->slots)
+      if (!sl->busy) {
+        free_slot = sl;
+        break;
+      }
+    if (!free_slot) return;
+    void* block = nullptr;
+    if (!pool_acquire(s, L.total, &block)) return;  // FIFO: wait for memory
+    free_slot->busy = true;
+    free_slot->block = block;
+    free_slot->bytes = L.total;
+    free_slot->info.tag = head.req.tag;
+    free_slot->info.submit_s = head.submit_s;
+    free_slot->info.start_s = now_s();
+    start(s, free_slot, head, L);
+    s->queue.pop_front();
+  }
+}
+
+void retire(althea_ibl_server* s) {
+  for (Slot* sl : s->slots) {
+    if (!sl->busy || !sl->done.load(std::memory_order_acquire)) continue;
+    althea_ibl_completion c = sl->info;
+    c.done_s = sl->done_s;
+    c.status = sl->status;
+    s->finished.push_back(c);
+    pool_release(s, sl->block, sl->bytes);
+    sl->block = nullptr;
+    sl->busy = false;
+    s->completed++;
+  }
+}
+
+int check_request(const althea_ibl_server* s, const althea_ibl_request* r) {
+  if (!r || !r->env_host) return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null request");
+  int st = ibl::check_env(r->env_width, r->env_height);
+  if (st) return st;
+  if (r->mip_count < 1 || r->mip_count > ALTHEA_IBL_MAX_MIPS)
+    return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "request mip_count %d", r->mip_count);
+  if (r->irradiance_host)
+    return ibl::check_irradiance_args(r->env_width, r->env_height, s->cfg.irradiance_width,
+                                      s->cfg.irradiance_height);
+  return ALTHEA_IBL_OK;
+}
+
+}  // namespace
+
+extern "C" double althea_ibl_server_now(void) { return now_s(); }
+
+extern "C" int althea_ibl_server_create(const althea_ibl_server_config* cfg,
+                                        althea_ibl_server** out) {
+  if (!cfg || !out) return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (cfg->max_inflight < 1 || cfg->max_inflight > 256 || cfg->budget_bytes == 0 ||
+      cfg->samples < 1 || cfg->samples > (1 << 24) ||
+      (cfg->generator != ALTHEA_IBL_GEN_REF_HASH && cfg->generator != ALTHEA_IBL_GEN_HAMMERSLEY) ||
+      cfg->irradiance_width < 1 || cfg->irradiance_height < 1)
+    return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "server config");
+  althea_ibl_server* s = new (std::nothrow) althea_ibl_server();
+  if (!s) return ibl::set_error(ALTHEA_IBL_ERR_OUT_OF_MEMORY, "host allocation");
+  s->cfg = *cfg;
+  for (int i = 0; i < cfg->max_inflight; ++i) {
+    Slot* sl = new (std::nothrow) Slot();
+    if (!sl || cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete sl;
+      althea_ibl_server_destroy(s);
+      return ibl::set_error(ALTHEA_IBL_ERR_CUDA, "server stream creation");
+    }
+    s->slots.push_back(sl);
+  }
+  *out = s;
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" size_t althea_ibl_server_request_bytes(const althea_ibl_server* s, int w, int h,
+                                                  int mips) {
+  if (!s || ibl::check_env(w, h) || mips < 1 || mips > ALTHEA_IBL_MAX_MIPS) return 0;
+  return layout_for(s, w, h, mips).total;
+}
+
+extern "C" int althea_ibl_server_submit(althea_ibl_server* s, const althea_ibl_request* r) {
+  if (!s) return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null server");
+  int st = check_request(s, r);
+  if (st) return st;
+  if (layout_for(s, r->env_width, r->env_height, r->mip_count).total > s->cfg.budget_bytes) {
+    s->rejected++;
+    return ibl::set_error(ALTHEA_IBL_ERR_BUDGET, "request needs more device memory than the "
+                                                 "server budget of %zu bytes",
+                          s->cfg.budget_bytes);
+  }
+  s->queue.push_back(Pending{*r, now_s()});
+  retire(s);
+  admit(s);
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_server_poll(althea_ibl_server* s, althea_ibl_completion* out, int max,
+                                      int* n) {
+  if (!s || !n || (max > 0 && !out))
+    return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
+  retire(s);
+  admit(s);
+  int k = 0;
+  while (k < max && !s->finished.empty()) {
+    out[k++] = s->finished.front();
+    s->finished.erase(s->finished.begin());
+  }
+  *n = k;
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_server_get_stats(const althea_ibl_server* s, althea_ibl_server_stats* st) {
+  if (!s || !st) return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
+  int inflight = 0;
+  for (Slot* sl : s->slots) inflight += sl->busy ? 1 : 0;
+  st->inflight = inflight;
+  st->queued = (int)s->queue.size();
+  st->bytes_in_use = s->in_use;
+  st->bytes_reserved = s->reserved;
+  st->peak_bytes_in_use = s->peak;
+  st->completed = s->completed;
+  st->rejected = s->rejected;
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_server_destroy(althea_ibl_server* s) {
+  if (!s) return ALTHEA_IBL_OK;
+  for (Slot* sl : s->slots) {
+    if (sl->stream) cudaStreamSynchronize(sl->stream);
+  }
+  retire(s);
+  for (Slot* sl : s->slots) {
+    if (sl->block) cudaFree(sl->block);
+    if (sl->stream) cudaStreamDestroy(sl->stream);
+    delete sl;
+  }
+  for (auto& kv : s->free_blocks)
+    for (void* p : kv.second) cudaFree(p);
+  delete s;
+  return ALTHEA_IBL_OK;
+}

@@ -90,6 +90,31 @@ class BatchInfo(ctypes.Structure):
 BATCH_AUTOTUNE = 1
 BATCH_GRAPH = 2
 
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int),
+                ("samples", ctypes.c_int), ("generator", ctypes.c_int),
+                ("irradiance_width", ctypes.c_int), ("irradiance_height", ctypes.c_int)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("env_host", ctypes.c_void_p), ("env_width", ctypes.c_int),
+                ("env_height", ctypes.c_int), ("mip_count", ctypes.c_int),
+                ("irradiance_host", ctypes.c_void_p), ("mips_host", ctypes.c_void_p),
+                ("tag", ctypes.c_uint64)]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [("tag", ctypes.c_uint64), ("status", ctypes.c_int), ("submit_s", ctypes.c_double),
+                ("start_s", ctypes.c_double), ("done_s", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("inflight", ctypes.c_int), ("queued", ctypes.c_int),
+                ("bytes_in_use", ctypes.c_size_t), ("bytes_reserved", ctypes.c_size_t),
+                ("peak_bytes_in_use", ctypes.c_size_t), ("completed", ctypes.c_uint64),
+                ("rejected", ctypes.c_uint64)]
+
 _lib = None
 
 
@@ -134,6 +159,13 @@ def load(build_if_missing: bool = True):
         "althea_ibl_batch_run": (i, [vp, vp]),
         "althea_ibl_batch_describe": (i, [vp, ctypes.POINTER(BatchInfo)]),
         "althea_ibl_batch_destroy": (i, [vp]),
+        "althea_ibl_server_create": (i, [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]),
+        "althea_ibl_server_submit": (i, [vp, ctypes.POINTER(Request)]),
+        "althea_ibl_server_poll": (i, [vp, ctypes.POINTER(Completion), i, ctypes.POINTER(i)]),
+        "althea_ibl_server_get_stats": (i, [vp, ctypes.POINTER(ServerStats)]),
+        "althea_ibl_server_request_bytes": (sz, [vp, i, i, i]),
+        "althea_ibl_server_now": (ctypes.c_double, []),
+        "althea_ibl_server_destroy": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -1,0 +1,150 @@
+"""Probe re-bake serving over the native server (althea_ibl_server_*).
+
+``ProbeServer`` owns one server: requests carry host (pinned) env maps and host
+output buffers; the server admits them by slot and HBM budget, overlaps their
+work on the device and reports completion times on its steady clock.
+``run_poisson`` replays a Poisson arrival stream against a server and returns
+latency percentiles and throughput.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+from dataclasses import dataclass
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from . import ibl
+
+
+@dataclass
+class RequestBuffers:
+    env: object            # pinned (H, W, 4) float32 host tensor
+    mips: object           # pinned flat float32 host tensor (all mips back to back)
+    irradiance: object     # pinned (ih, iw, 4) float32 host tensor
+    mip_sizes: List[tuple]
+
+
+def mip_sizes_for(w: int, h: int, mip_count: int) -> List[tuple]:
+    fw, fh = max(w >> 1, 1), max(h >> 1, 1)
+    return [(max(fw >> m, 1), max(fh >> m, 1)) for m in range(mip_count)]
+
+
+class ProbeServer:
+    def __init__(self, budget_bytes: int, max_inflight: int = 8, samples: int = 1024,
+                 generator: int = ibl.GEN_HAMMERSLEY, irradiance_size=(32, 16)):
+        self.cfg = ibl.ServerConfig(budget_bytes, max_inflight, samples, generator,
+                                    irradiance_size[0], irradiance_size[1])
+        self.irradiance_size = irradiance_size
+        self._s = ctypes.c_void_p()
+        ibl._check(ibl.load().althea_ibl_server_create(ctypes.byref(self.cfg),
+                                                       ctypes.byref(self._s)))
+        self._keep: Dict[int, RequestBuffers] = {}
+        self._done = (ibl.Completion * 256)()
+
+    def buffers(self, env_np: np.ndarray, mip_count: int) -> RequestBuffers:
+        """Pinned host buffers for one request (env copied in)."""
+        import torch
+        h, w = env_np.shape[:2]
+        env = torch.from_numpy(np.ascontiguousarray(env_np)).pin_memory()
+        sizes = mip_sizes_for(w, h, mip_count)
+        mips = torch.empty(sum(a * b * 4 for a, b in sizes), dtype=torch.float32).pin_memory()
+        iw, ih = self.irradiance_size
+        irr = torch.empty((ih, iw, 4), dtype=torch.float32).pin_memory()
+        return RequestBuffers(env, mips, irr, sizes)
+
+    def submit(self, tag: int, buf: RequestBuffers) -> None:
+        h, w = buf.env.shape[:2]
+        req = ibl.Request(buf.env.data_ptr(), w, h, len(buf.mip_sizes), buf.irradiance.data_ptr(),
+                          buf.mips.data_ptr(), tag)
+        self._keep[tag] = buf
+        ibl._check(ibl.load().althea_ibl_server_submit(self._s, ctypes.byref(req)))
+
+    def poll(self) -> List[ibl.Completion]:
+        n = ctypes.c_int()
+        out = []
+        while True:
+            ibl._check(ibl.load().althea_ibl_server_poll(self._s, self._done, len(self._done),
+                                                         ctypes.byref(n)))
+            for k in range(n.value):
+                c = self._done[k]
+                out.append(ibl.Completion(c.tag, c.status, c.submit_s, c.start_s, c.done_s))
+            if n.value < len(self._done):
+                return out
+
+    def stats(self) -> ibl.ServerStats:
+        st = ibl.ServerStats()
+        ibl._check(ibl.load().althea_ibl_server_get_stats(self._s, ctypes.byref(st)))
+        return st
+
+    def request_bytes(self, w: int, h: int, mip_count: int) -> int:
+        return ibl.load().althea_ibl_server_request_bytes(self._s, w, h, mip_count)
+
+    def drain(self, timeout_s: float = 120.0) -> List[ibl.Completion]:
+        out = []
+        t0 = time.monotonic()
+        while True:
+            out += self.poll()
+            st = self.stats()
+            if st.inflight == 0 and st.queued == 0:
+                return out + self.poll()
+            if time.monotonic() - t0 > timeout_s:
+                raise TimeoutError("server did not drain")
+            time.sleep(0.0002)
+
+    def release(self, tag: int) -> Optional[RequestBuffers]:
+        return self._keep.pop(tag, None)
+
+    def close(self) -> None:
+        if self._s:
+            ibl.load().althea_ibl_server_destroy(self._s)
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def now() -> float:
+    return ibl.load().althea_ibl_server_now()
+
+
+def run_poisson(server: ProbeServer, pool: List[RequestBuffers], rate: float, n_requests: int,
+                seed: int = 0) -> dict:
+    """Submits n_requests at Poisson arrival times (rate per second), cycling
+    through the prepared request buffers, and returns latency statistics.
+    Latency = completion (host callback on the request's stream) - arrival."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=n_requests)
+    arrivals = np.cumsum(gaps)
+    t0 = now()
+    done: Dict[int, ibl.Completion] = {}
+    arrival_abs = {}
+    in_use = {}  # pool slot -> tag using it (a buffer is reused only after it completes)
+    for i in range(n_requests):
+        target = t0 + arrivals[i]
+        k = i % len(pool)
+        while True:
+            for c in server.poll():
+                done[c.tag] = c
+                in_use = {s: t for s, t in in_use.items() if t != c.tag}
+            if now() >= target and k not in in_use:
+                break
+            time.sleep(0.00005)
+        arrival_abs[i] = target
+        in_use[k] = i
+        server.submit(i, pool[k])
+    for c in server.drain():
+        done[c.tag] = c
+    t_end = max(c.done_s for c in done.values())
+    lat = np.array([done[i].done_s - arrival_abs[i] for i in range(n_requests)
+                    if done[i].status == ibl.OK])
+    st = server.stats()
+    return {"rate": rate, "requests": n_requests, "ok": int(len(lat)),
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "mean_ms": float(lat.mean() * 1e3),
+            "throughput": n_requests / (t_end - t0),
+            "peak_bytes": int(st.peak_bytes_in_use)}

@@ -451,6 +451,45 @@ def run_batch(args):
     return 0
 
 
+def run_serve(args):
+    """Poisson stream of re-bake requests (sizes as in the batch workload, suns
+    re-seeded per request from a pool of prepared maps) against the native
+    server under an HBM budget; p50/p99 latency and throughput per rate."""
+    from althea_gb300 import serving, synth
+    world, rank, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    server = serving.ProbeServer(budget_bytes=int(args.budget_gb * (1 << 30)),
+                                 max_inflight=args.inflight, samples=SAMPLES,
+                                 generator=GENERATOR, irradiance_size=(32, 16))
+    rng = np.random.default_rng(rank)
+    pool = []
+    for k in range(args.pool):
+        w = int(rng.choice([256, 512, 1024, 2048]))
+        env = synth.make_env(w, w // 2, seed=5000 + 100 * rank + k)
+        pool.append(server.buffers(env, max(1, w.bit_length() - 1 - 3)))
+    serving.run_poisson(server, pool, rate=200.0, n_requests=min(64, 4 * len(pool)), seed=1)
+    rows = []
+    for rate in args.rates:
+        n = int(min(args.requests, max(64, rate * args.seconds)))
+        rows.append(serving.run_poisson(server, pool, rate=rate, n_requests=n, seed=int(rate)))
+    server.close()
+    best = max(r["throughput"] for r in rows)
+    line = {"metric": METRIC, "value": best, "unit": "probes/s", "n_gpus": world,
+            "steps": len(rows), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"serving: Poisson re-bake requests, sizes uniform over "
+                                   f"256..2048 wide (2:1), log2(W)-3 mips, 32x16 irradiance, "
+                                   f"N=1024, {args.inflight} slots, {args.budget_gb} GB budget, "
+                                   f"{args.pool} pre-generated maps (suns re-seeded per map), "
+                                   "latency = completion callback - arrival, host pinned I/O",
+                       "path": "plain"},
+            "serving": rows}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -459,9 +498,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--generator", default="hammersley", choices=["hammersley", "ref-hash"])
-    ap.add_argument("--workload", default="probe", choices=["probe", "batch"],
-                    help="probe: one 4096x2048 bake per step (default); batch: many probes")
+    ap.add_argument("--workload", default="probe", choices=["probe", "batch", "serve"],
+                    help="probe: one 4096x2048 bake per step (default); batch: many probes; "
+                         "serve: Poisson request stream against the server")
     ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--rates", type=float, nargs="+", default=[50, 200, 500, 1000, 2000])
+    ap.add_argument("--requests", type=int, default=10000)
+    ap.add_argument("--seconds", type=float, default=4.0, help="per-rate cap on arrival time")
+    ap.add_argument("--budget-gb", type=float, default=40.0)
+    ap.add_argument("--inflight", type=int, default=16)
+    ap.add_argument("--pool", type=int, default=32)
     args = ap.parse_args()
     global GENERATOR
     GENERATOR = 1 if args.generator == "hammersley" else 0
@@ -469,6 +515,8 @@ def main():
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

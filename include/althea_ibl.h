@@ -231,6 +231,61 @@ int althea_ibl_batch_run(althea_ibl_batch* batch, void* stream);
 int althea_ibl_batch_describe(const althea_ibl_batch* batch, althea_ibl_batch_info* info);
 int althea_ibl_batch_destroy(althea_ibl_batch* batch);
 
+/* ---- serving: continuous re-bakes under an HBM budget -------------------------
+ * No counterpart in the reference (one synchronous bake at start-up,
+ * Src/GlobalResources.cpp:18-22).  A server admits probe re-bake requests as
+ * they arrive: a request starts as soon as a slot (a CUDA stream) is free and
+ * its device memory (env chain, outputs, scratch) fits the budget; requests
+ * that do not fit wait in FIFO order.  Admitted requests run concurrently on
+ * their own streams; buffers are recycled through a size-class pool (no
+ * cudaFree on the request path).  Results are identical whether a request runs
+ * alone or among others (the kernels are deterministic and independent of
+ * concurrency).  The API is single-threaded: call submit/poll from one thread. */
+typedef struct {
+  size_t budget_bytes;       /* device memory the server may hold */
+  int max_inflight;          /* requests on the GPU at once (streams) */
+  int samples, generator;    /* prefilter sample count and generator */
+  int irradiance_width, irradiance_height;
+} althea_ibl_server_config;
+
+typedef struct {
+  const float* env_host;     /* RGBA32F level 0, host memory (pinned for overlap) */
+  int env_width, env_height;
+  int mip_count;             /* mips from W/2 x H/2, roughness m/(M-1) */
+  float* irradiance_host;    /* irradiance_width*height*4 floats, or NULL */
+  float* mips_host;          /* every mip back to back (sum of w*h*4 floats) */
+  uint64_t tag;
+} althea_ibl_request;
+
+typedef struct {
+  uint64_t tag;
+  int status;                /* althea_ibl_status of the request */
+  double submit_s, start_s, done_s;   /* steady-clock seconds */
+} althea_ibl_completion;
+
+typedef struct {
+  int inflight, queued;
+  size_t bytes_in_use, bytes_reserved, peak_bytes_in_use;
+  uint64_t completed, rejected;
+} althea_ibl_server_stats;
+
+typedef struct althea_ibl_server althea_ibl_server;
+
+int althea_ibl_server_create(const althea_ibl_server_config* cfg, althea_ibl_server** out);
+/* Queues the request and admits what fits; never blocks on the GPU.  A request
+ * whose memory alone exceeds the budget is refused with ALTHEA_IBL_ERR_BUDGET. */
+int althea_ibl_server_submit(althea_ibl_server* s, const althea_ibl_request* req);
+/* Retires finished requests (returning up to max completions), frees their
+ * slots and memory, and admits queued requests that now fit. */
+int althea_ibl_server_poll(althea_ibl_server* s, althea_ibl_completion* out, int max, int* n);
+int althea_ibl_server_get_stats(const althea_ibl_server* s, althea_ibl_server_stats* st);
+/* Device memory a request of this size holds while in flight. */
+size_t althea_ibl_server_request_bytes(const althea_ibl_server* s, int env_width, int env_height,
+                                       int mip_count);
+double althea_ibl_server_now(void);   /* the steady clock used in completions */
+/* Waits for everything in flight, then releases all device memory. */
+int althea_ibl_server_destroy(althea_ibl_server* s);
+
 const char* althea_ibl_last_error(void);
 int althea_ibl_abi_version(void);
 
