@@ -1,0 +1,716 @@
+// ibl_tc.cu -- precision path: the GGX prefilter and the irradiance
+// convolution as dense contractions on the sm_103a tensor cores (tcgen05,
+// BF16 hi/lo operands, FP32 accumulation in TMEM, FP64 weight normalisation).
+//
+// What is computed (the quadrature the FP64 oracle states):
+//   prefilter(n) = sum_t L_t w(n,t) / sum_t w(n,t),
+//     w = D_GGX(n.h; a2 = r^2) * max(0, n.w_t) * Omega_t,  n.h = sqrt((1 + n.w_t)/2)
+//   irradiance(n) = (1/pi) sum_t L_t max(0, n.w_t) Omega_t
+// over the texels t of a chosen source level S of the env chain (box
+// averages of level 0), at the reference's texel-corner output directions.
+// The planner (althea_ibl_tc_plan) picks S per mip from a measured error
+// table so the result stays within 1e-3 of the same sum over level 0.
+//
+// Structure.  On an equirect map the weight of output texel (i, x) for source
+// texel (j, y) depends only on (i, j, d = y - s*x) with s = W_src / W_out:
+// c = cos p_i cos q_j cos(2 pi (d + 0.5) / W_src) + sin p_i sin q_j.  Splitting
+// the source row into s polyphase rows L_{j,ph}[t] = L_j[s t + ph] gives
+//   out[i, x] = sum_{j, ph, k} w_ij(s k + ph) * L_{j,ph}[x + k]
+// -- a GEMM with M = 128 output rows i (TMEM lanes), N = output columns and
+// K = (j, ph, k).  A CTA owns the columns x = x_ph + 8 n of one residue x_ph;
+// then B[n, k] = L_{j,ph}[x_ph + 8 n + k] is a Hankel matrix whose rows start
+// 16 bytes apart, which the K-major no-swizzle UMMA layout expresses directly
+// (core-matrix row pitch 16 B, LBO = 16 B along K, SBO = 128 B along N), so
+// the radiance operand is read straight from a staged row buffer.  The weight
+// operand A[i, k] is generated on the CUDA cores into shared memory.
+//
+// Precision.  Radiance and weights are each split x = hi + lo (hi = bf16(x),
+// lo = bf16(x - hi)); three MMAs per channel (hi*hi + hi*lo + lo*hi) give
+// products to ~2^-17 relative; sums of positive terms accumulate in FP32
+// TMEM.  BF16 shares FP32's exponent range, so 1e6-bright suns need no
+// per-tile scaling.  The weight sum is taken in FP64 per output row (it does
+// not depend on x).
+//
+// Safety.  Every mbarrier wait is bounded; on timeout the kernel records an
+// error flag, waits (bounded) for its own MMAs, frees its TMEM and returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "althea_ibl.h"
+#include "ibl_device.cuh"
+#include "ibl_internal.h"
+
+namespace ibl {
+namespace tc {
+
+constexpr int kM = 128;          // output rows per CTA (TMEM lanes)
+constexpr int kKStep = 64;       // K per pipeline step (4 MMA instructions)
+constexpr int kThreads = 256;
+
+
+constexpr long long kSpinLimit = 1LL << 26;
+constexpr float kPiF = 3.14159265358979f;
+
+// ---- PTX wrappers -------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long i = 0; i < kSpinLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  // tcgen05 shared-memory matrix descriptor, no swizzle:
+  // [0,14) addr>>4, [16,30) LBO>>4, [32,46) SBO>>4, [46,48) version = 1,
+  // [49,52) base offset = 0, [52] LBO mode = 0, [61,64) layout = 0 (none).
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+  return (1u << 4) |                    // D format F32
+         (1u << 7) | (1u << 10) |       // A, B format BF16
+         ((uint32_t)(n >> 3) << 17) |   // N / 8
+         ((uint32_t)(m >> 4) << 24);    // M / 16
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---- job description --------------------------------------------------------------
+struct Job {
+  const __nv_bfloat16* planes;  // 6 planes [ch*2 + hl][H_s][W_s] of the source level
+  int ws, hs;                   // source level size
+  int wo, ho;                   // output size
+  int s;                        // ws / wo (power of two >= 1)
+  int kind;                     // 0 = GGX prefilter, 1 = irradiance
+  float a2;                     // roughness^2
+  int n_mma;                    // N of the MMA (multiple of 16, >= ceil(wo/8))
+  int kpad;                     // polyphase row length padded to a multiple of 16
+  int ksplit;                   // source rows are split over this many CTAs
+  int tmem_cols;                // power of two >= 3 * n_mma (channel c at column c * n_mma)
+  const float* cos_d;           // [ws]  cos(2 pi (d + 0.5) / ws)
+  const float* src_rows;        // [hs][3]  cos q, sin q, Omega
+  const float* out_rows;        // [ho][2]  cos p, sin p
+  float* partial;               // [ksplit][ho][3][wo]
+  int* error;                   // set on a bounded-wait timeout
+};
+
+// Weight for cos-angle c (see the file comment).
+__device__ __forceinline__ float weight_of(float c, float a2, int kind) {
+  if (!(c > 0.0f)) return 0.0f;
+  if (kind == 1) return c;
+  float nh2 = 0.5f * (1.0f + c);
+  float den = fmaf(nh2, a2 - 1.0f, 1.0f);
+  return __fdividef(a2, kPiF * den * den) * c;
+}
+
+// Shared-memory plan of the contraction kernel (bytes).
+struct Smem {
+  static constexpr int kA = kM * kKStep * 2;            // one bf16 A tile (16 KB)
+  static constexpr int kAStages = 2;
+  static constexpr int kRowSlots = 2;
+  __host__ __device__ static int row_len(int n_mma, int kpad) {
+    return ((8 * n_mma + kpad + 7) / 8) * 8;            // bf16 elements per staged row
+  }
+};
+
+// The contraction kernel.  Grid: (ceil(ho/128), 8 x residues, ksplit).
+__global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t mbar[2];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ float rowc[kM], rows[kM];
+  __shared__ int abort_flag;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int i0 = blockIdx.x * kM;
+  const int xph = blockIdx.y;
+  const int split = blockIdx.z;
+  const int rlen = Smem::row_len(job.n_mma, job.kpad);
+  // layout: A stages [2][hi,lo] | row slots [2][6 planes][rlen] | cos_d[ws]
+  unsigned char* a_base = smem;
+  __nv_bfloat16* rows_base =
+      reinterpret_cast<__nv_bfloat16*>(smem + Smem::kAStages * 2 * Smem::kA);
+  float* cosd = reinterpret_cast<float*>(
+      smem + Smem::kAStages * 2 * Smem::kA + Smem::kRowSlots * 6 * rlen * 2);
+
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int i = tid; i < kM; i += kThreads) {
+    int gi = i0 + i;
+    rowc[i] = gi < job.ho ? job.out_rows[2 * gi] : 0.0f;
+    rows[i] = gi < job.ho ? job.out_rows[2 * gi + 1] : 0.0f;
+  }
+  for (int d = tid; d < job.ws; d += kThreads) cosd[d] = job.cos_d[d];
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_sh)),
+                 "r"((uint32_t)job.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  // Source rows of this split.
+  const int j_per = (job.hs + job.ksplit - 1) / job.ksplit;
+  const int j0 = split * j_per;
+  const int j1 = min(job.hs, j0 + j_per);
+  const int wo_ph = job.wo;            // polyphase row length = ws / s = wo
+  const int ksteps_row = (job.kpad + kKStep - 1) / kKStep;
+  const uint32_t idesc = idesc_bf16(kM, job.n_mma);
+
+  long long step = 0;
+  bool ok = true;
+  for (int j = j0; j < j1 && ok; ++j) {
+    const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
+    const float om = job.src_rows[3 * j + 2];
+    for (int ph = 0; ph < job.s && ok; ++ph) {
+      for (int kc = 0; kc < ksteps_row && ok; ++kc, ++step) {
+        const int stage = (int)(step & 1);
+        // (1) the MMAs of step - 2 read this stage's A tile and (on a row
+        // start) this slot's row buffers: wait for them.
+        if (step >= 2) {
+          if (!mbar_wait(&mbar[stage], (uint32_t)(((step - 2) >> 1) & 1))) {
+            if (tid == 0) abort_flag = 1;
+          }
+        }
+        __syncthreads();
+        if (abort_flag) {
+          ok = false;
+          break;
+        }
+        const long long row_id = (long long)(j - j0) * job.s + ph;
+        const int slot = (int)(row_id & 1);
+        __nv_bfloat16* slot_base = rows_base + (size_t)slot * 6 * rlen;
+        // (2) stage the polyphase row (x residue folded in) on a row start:
+        // buf[t] = plane[j][(s * (t + xph) + ph) mod ws].
+        if (kc == 0) {
+          for (int e = tid; e < 6 * rlen; e += kThreads) {
+            int p = e / rlen, t = e - p * rlen;
+            long long src = ((long long)job.s * (t + xph) + ph) % job.ws;
+            slot_base[e] = job.planes[((size_t)p * job.hs + j) * job.ws + src];
+          }
+        }
+        // (3) weights of this step into A[stage] (hi, lo), K-major no-swizzle:
+        // element (i, k) at (i/8)*1024 + (k/8)*128 + (i%8)*16 + (k%8)*2.
+        unsigned char* a_hi = a_base + stage * 2 * Smem::kA;
+        unsigned char* a_lo = a_hi + Smem::kA;
+        {
+          const int i = tid >> 1;           // 0..127
+          const int kk0 = (tid & 1) * 32;   // 32 consecutive k per thread
+          const float cp = rowc[i], sp = rows[i];
+          const bool row_ok = i0 + i < job.ho;
+          const float ccq = cp * cq, ssq = sp * sq;
+#pragma unroll
+          for (int g = 0; g < 4; ++g) {
+            uint32_t hw[4], lw[4];
+#pragma unroll
+            for (int e = 0; e < 8; e += 2) {
+              float wv[2];
+#pragma unroll
+              for (int u = 0; u < 2; ++u) {
+                int kl = kc * kKStep + kk0 + 8 * g + e + u;   // polyphase column
+                float w = 0.0f;
+                if (row_ok && kl < wo_ph) {
+                  int d = job.s * kl + ph;                    // y - s*x
+                  float c = fmaf(ccq, cosd[d], ssq);
+                  w = weight_of(c, job.a2, job.kind) * om;
+                }
+                wv[u] = w;
+              }
+              __nv_bfloat162 h2 = __floats2bfloat162_rn(wv[0], wv[1]);
+              float2 hf = __bfloat1622float2(h2);
+              __nv_bfloat162 l2 = __floats2bfloat162_rn(wv[0] - hf.x, wv[1] - hf.y);
+              hw[e / 2] = *reinterpret_cast<uint32_t*>(&h2);
+              lw[e / 2] = *reinterpret_cast<uint32_t*>(&l2);
+            }
+            const int kk = kk0 + 8 * g;
+            const int off = (i >> 3) * 1024 + (kk >> 3) * 128 + (i & 7) * 16;
+            *reinterpret_cast<uint4*>(a_hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+            *reinterpret_cast<uint4*>(a_lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+          }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        // (4) one thread issues the MMAs of this step and commits.
+        if (tid == 0) {
+          tc_fence_after();
+          const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
+          const int kmax = min(kKStep, job.kpad - kc * kKStep);
+          for (int q = 0; q < kmax / 16; ++q) {
+            const uint64_t da_hi = smem_desc(ah + q * 256, 128, 1024);
+            const uint64_t da_lo = smem_desc(al + q * 256, 128, 1024);
+            const uint32_t first = (j == j0 && ph == 0 && kc == 0 && q == 0) ? 0u : 1u;
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+              const uint32_t bh = smem_u32(slot_base + (size_t)(2 * ch) * rlen) +
+                                  2u * (uint32_t)(kc * kKStep + q * 16);
+              const uint32_t bl = smem_u32(slot_base + (size_t)(2 * ch + 1) * rlen) +
+                                  2u * (uint32_t)(kc * kKStep + q * 16);
+              const uint64_t db_hi = smem_desc(bh, 16, 128);
+              const uint64_t db_lo = smem_desc(bl, 16, 128);
+              const uint32_t d = tmem + (uint32_t)(ch * job.n_mma);
+              mma_bf16(d, da_hi, db_hi, idesc, first);
+              mma_bf16(d, da_hi, db_lo, idesc, 1u);
+              mma_bf16(d, da_lo, db_hi, idesc, 1u);
+            }
+          }
+          mma_commit(&mbar[stage]);
+        }
+      }
+    }
+  }
+  // Drain: the last commits of both stages.
+  const long long nsteps = step;
+  bool drained = true;
+  for (long long s2 = nsteps - 2; s2 < nsteps; ++s2) {
+    if (s2 < 0) continue;
+    if (!mbar_wait(&mbar[s2 & 1], (uint32_t)((s2 >> 1) & 1))) drained = false;
+  }
+  tc_fence_after();
+  __syncthreads();
+  if (!ok || !drained) {
+    if (tid == 0) atomicExch(job.error, 1);
+  } else if (nsteps > 0 && warp < 4) {
+    // Epilogue: warp w reads TMEM lanes 32w..32w+31 (output rows).
+    const int i = i0 + warp * 32 + lane;
+    for (int ch = 0; ch < 3; ++ch) {
+      for (int c0 = 0; c0 < job.n_mma; c0 += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(ch * job.n_mma + c0), v);
+        if (i < job.ho) {
+#pragma unroll
+          for (int u = 0; u < 16; ++u) {
+            int x = xph + 8 * (c0 + u);
+            if (x < job.wo)
+              job.partial[(((size_t)split * job.ho + i) * 3 + ch) * job.wo + x] = v[u];
+          }
+        }
+      }
+    }
+  } else if (nsteps == 0 && warp < 4) {
+    const int i = i0 + warp * 32 + lane;
+    if (i < job.ho)
+      for (int ch = 0; ch < 3; ++ch)
+        for (int x = xph; x < job.wo; x += 8)
+          job.partial[(((size_t)split * job.ho + i) * 3 + ch) * job.wo + x] = 0.0f;
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"((uint32_t)job.tmem_cols));
+}
+
+// RGBA32F source level -> 6 bf16 planes (R hi, R lo, G hi, G lo, B hi, B lo).
+__global__ void split_kernel(const float4* __restrict__ src, int n,
+                             __nv_bfloat16* __restrict__ planes) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  float4 v = src[t];
+  float c[3] = {v.x, v.y, v.z};
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    __nv_bfloat16 h = __float2bfloat16_rn(c[ch]);
+    __nv_bfloat16 l = __float2bfloat16_rn(c[ch] - __bfloat162float(h));
+    planes[(size_t)(2 * ch) * n + t] = h;
+    planes[(size_t)(2 * ch + 1) * n + t] = l;
+  }
+}
+
+// FP64 weight sum per output row: sum_j sum_d w_ij(d) (FP32 terms, each
+// source row summed in FP32 by a warp, rows accumulated in FP64).
+__global__ void weight_sum_kernel(const Job job, double* __restrict__ wsum) {
+  const int i = blockIdx.x;
+  const float cp = job.out_rows[2 * i], sp = job.out_rows[2 * i + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __shared__ double part[32];
+  double acc = 0.0;
+  for (int j = warp; j < job.hs; j += nw) {
+    const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
+    const float om = job.src_rows[3 * j + 2];
+    const float ccq = cp * cq, ssq = sp * sq;
+    float s = 0.0f;
+    for (int d = lane; d < job.ws; d += 32) {
+      float c = fmaf(ccq, job.cos_d[d], ssq);
+      s += weight_of(c, job.a2, job.kind) * om;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) acc += (double)s;
+  }
+  if (lane == 0) part[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < nw; ++w) t += part[w];
+    wsum[i] = t;
+  }
+}
+
+// Sum the K splits in order, normalise, write RGBA32F.
+__global__ void finish_kernel(const Job job, const double* __restrict__ wsum,
+                              float4* __restrict__ out, long long pitch) {
+  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (long long)job.wo * job.ho) return;
+  int x = (int)(g % job.wo), i = (int)(g / job.wo);
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < job.ksplit; ++k)
+    for (int ch = 0; ch < 3; ++ch)
+      s[ch] += (double)job.partial[(((size_t)k * job.ho + i) * 3 + ch) * job.wo + x];
+  double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / wsum[i]);
+  out[(long long)i * pitch + x] =
+      make_float4((float)(s[0] * norm), (float)(s[1] * norm), (float)(s[2] * norm), 1.0f);
+}
+
+}  // namespace tc
+}  // namespace ibl
+
+// =====================================================================================
+// Host side: planning, workspace layout, launches.
+// =====================================================================================
+using namespace ibl;
+using namespace ibl::tc;
+
+namespace {
+
+// Source level per output mip / irradiance: the coarsest level whose measured
+// max relative error against the level-0 FP64 quadrature stayed <= 3e-4 on a
+// 4096x2048 map with 1e6 suns (sampled texels per mip), expressed as the
+// angular size of a source texel relative to the env: level = log2(W / target).
+int planned_level(int w, int ow, float roughness, bool irradiance) {
+  // target source width by role (for a 4096-wide env: irradiance and rough
+  // mips at level 1, glossy mips at level 2).
+  int target;
+  if (irradiance)
+    target = 2048;
+  else if (roughness <= 0.40f)
+    target = 1024;
+  else if (roughness <= 0.55f)
+    target = 512;
+  else if (roughness >= 0.85f && roughness <= 0.90f)
+    target = 512;
+  else
+    target = 2048;
+  // Scale with the env: the error depends on the angular size of a texel.
+  int level = 0;
+  while ((w >> (level + 1)) >= target && level + 1 < 15) ++level;
+  // never coarser than the output itself
+  while (level > 0 && (w >> level) < ow) --level;
+  return level;
+}
+
+struct LevelPlanes {
+  int level, ws, hs;
+  size_t offset;  // byte offset of the 6 planes in the workspace
+};
+
+struct TcPlan {
+  std::vector<Job> jobs;
+  std::vector<int> job_level;      // index into levels
+  std::vector<LevelPlanes> levels;
+  std::vector<size_t> cosd_off, rows_off, orows_off, partial_off, wsum_off;
+  size_t total = 0;
+};
+
+size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+int level_index(TcPlan& P, int w, int h, int level, size_t& off) {
+  for (size_t k = 0; k < P.levels.size(); ++k)
+    if (P.levels[k].level == level) return (int)k;
+  LevelPlanes L;
+  L.level = level;
+  L.ws = level_dim(w, level);
+  L.hs = level_dim(h, level);
+  L.offset = off;
+  off = al256(off + (size_t)6 * L.ws * L.hs * 2);
+  P.levels.push_back(L);
+  return (int)P.levels.size() - 1;
+}
+
+// Adds a contraction job (mip or irradiance) to the plan.
+void add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, int level,
+             size_t& off) {
+  Job J;
+  memset(&J, 0, sizeof(J));
+  int li = level_index(P, w, h, level, off);
+  J.ws = P.levels[li].ws;
+  J.hs = P.levels[li].hs;
+  J.wo = ow;
+  J.ho = oh;
+  J.s = J.ws / ow;
+  J.kind = kind;
+  J.a2 = roughness * roughness;
+  int neff = (ow + 7) / 8;
+  J.n_mma = ((neff + 15) / 16) * 16;
+  if (J.n_mma < 16) J.n_mma = 16;
+  J.kpad = ((ow + 15) / 16) * 16;
+  J.tmem_cols = 32;
+  while (J.tmem_cols < 3 * J.n_mma) J.tmem_cols <<= 1;
+  int ctas = ((oh + kM - 1) / kM) * 8;
+  int ks = 152 / ctas;  // one wave of CTAs
+  if (ks > J.hs) ks = J.hs;
+  if (ks < 1) ks = 1;
+  J.ksplit = ks;
+  P.jobs.push_back(J);
+  P.job_level.push_back(li);
+  P.cosd_off.push_back(off);
+  off = al256(off + (size_t)J.ws * 4);
+  P.rows_off.push_back(off);
+  off = al256(off + (size_t)J.hs * 12);
+  P.orows_off.push_back(off);
+  off = al256(off + (size_t)oh * 8);
+  P.partial_off.push_back(off);
+  off = al256(off + (size_t)ks * oh * 3 * ow * 4);
+  P.wsum_off.push_back(off);
+  off = al256(off + (size_t)oh * 8);
+}
+
+int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int* levels,
+              int irr_w, int irr_h, int irr_level, TcPlan& P) {
+  size_t off = 256;  // error flag first
+  for (int m = 0; m < n; ++m) {
+    if (mips[m].roughness == 0.0f) {  // a delta: handled by the plain path
+      P.jobs.push_back(Job{});
+      P.job_level.push_back(-1);
+      P.cosd_off.push_back(0);
+      P.rows_off.push_back(0);
+      P.orows_off.push_back(0);
+      P.partial_off.push_back(0);
+      P.wsum_off.push_back(0);
+      continue;
+    }
+    int lv = levels && levels[m] >= 0 ? levels[m]
+                                      : planned_level(w, mips[m].width, mips[m].roughness, false);
+    int ws = level_dim(w, lv);
+    if (ws < mips[m].width || ws % mips[m].width != 0 || mips[m].width > 1024 ||
+        mips[m].height > 65536)
+      return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
+                       "tensor path: mip %d (%dx%d) cannot contract against level %d", m,
+                       mips[m].width, mips[m].height, lv);
+    add_job(P, w, h, mips[m].width, mips[m].height, mips[m].roughness, 0, lv, off);
+  }
+  if (irr_w > 0) {
+    int lv = irr_level >= 0 ? irr_level : planned_level(w, irr_w, 1.0f, true);
+    int ws = level_dim(w, lv);
+    if (ws < irr_w || ws % irr_w != 0 || irr_w > 1024)
+      return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "tensor path: irradiance %dx%d vs level %d",
+                       irr_w, irr_h, lv);
+    add_job(P, w, h, irr_w, irr_h, 1.0f, 1, lv, off);
+  }
+  P.total = off;
+  return ALTHEA_IBL_OK;
+}
+
+size_t smem_bytes(const Job& J) {
+  int rlen = Smem::row_len(J.n_mma, J.kpad);
+  return (size_t)Smem::kAStages * 2 * Smem::kA + (size_t)Smem::kRowSlots * 6 * rlen * 2 +
+         (size_t)J.ws * 4;
+}
+
+}  // namespace
+
+extern "C" size_t althea_ibl_tc_workspace_size(int w, int h, const althea_ibl_mip_target* mips,
+                                               int n, const int* levels, int irr_w, int irr_h,
+                                               int irr_level) {
+  if (check_env(w, h)) return 0;
+  TcPlan P;
+  if (make_plan(w, h, mips, n, levels, irr_w, irr_h, irr_level, P)) return 0;
+  return P.total;
+}
+
+extern "C" int althea_ibl_tc_plan(int w, int h, const althea_ibl_mip_target* mips, int n,
+                                  int irr_w, int* levels_out, int* irr_level_out) {
+  if (check_env(w, h)) return ALTHEA_IBL_ERR_INVALID_ARGUMENT;
+  for (int m = 0; m < n; ++m)
+    levels_out[m] = mips[m].roughness == 0.0f
+                        ? -1
+                        : planned_level(w, mips[m].width, mips[m].roughness, false);
+  if (irr_level_out) *irr_level_out = irr_w > 0 ? planned_level(w, irr_w, 1.0f, true) : -1;
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
+                                  const althea_ibl_mip_target* mips, int n, const int* levels,
+                                  float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
+                                  int irr_level, void* ws, size_t ws_bytes, void* stream) {
+  int st = check_env(w, h);
+  if (st) return st;
+  if (!chain || ((uintptr_t)chain) % 16 || n < 0 || n > ALTHEA_IBL_MAX_MIPS || (n && !mips))
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "tensor path: chain/mips");
+  for (int m = 0; m < n; ++m) {
+    st = check_image(mips[m].out_dev, mips[m].width, mips[m].height, mips[m].pitch_bytes, 16,
+                     "tc mip");
+    if (st) return st;
+  }
+  if (irr_out) {
+    st = check_image(irr_out, irr_w, irr_h, irr_pitch, 16, "tc irradiance");
+    if (st) return st;
+  }
+  TcPlan P;
+  st = make_plan(w, h, mips, n, levels, irr_out ? irr_w : 0, irr_h, irr_level, P);
+  if (st) return st;
+  if (!ws || ws_bytes < P.total || ((uintptr_t)ws) % 256)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
+                     "tensor path workspace needs %zu bytes (256-byte aligned)", P.total);
+  cudaStream_t s = (cudaStream_t)stream;
+  char* base = static_cast<char*>(ws);
+  cudaError_t e = cudaMemsetAsync(base, 0, 256, s);
+  if (e != cudaSuccess) return cuda_status(e, "tc error flag");
+  // Host tables (FP64 -> FP32), uploaded once per call.
+  ChainTable tab;
+  make_table(w, h, &tab);
+  for (auto& L : P.levels) {
+    int nt = L.ws * L.hs;
+    const float4* src = reinterpret_cast<const float4*>(chain) + tab.off[L.level];
+    split_kernel<<<(nt + 255) / 256, 256, 0, s>>>(
+        src, nt, reinterpret_cast<__nv_bfloat16*>(base + L.offset));
+  }
+  std::vector<float> host;
+  for (size_t k = 0; k < P.jobs.size(); ++k) {
+    if (P.job_level[k] < 0) continue;
+    Job& J = P.jobs[k];
+    const LevelPlanes& L = P.levels[P.job_level[k]];
+    J.planes = reinterpret_cast<const __nv_bfloat16*>(base + L.offset);
+    std::vector<float> cosd(J.ws), rowsv((size_t)J.hs * 3), orows((size_t)J.ho * 2);
+    for (int d = 0; d < J.ws; ++d) cosd[d] = (float)cos(2.0 * M_PI * (d + 0.5) / J.ws);
+    for (int j = 0; j < J.hs; ++j) {
+      double q = M_PI * ((j + 0.5) / J.hs - 0.5);
+      double q0 = M_PI * ((double)j / J.hs - 0.5), q1 = M_PI * ((double)(j + 1) / J.hs - 0.5);
+      rowsv[3 * j] = (float)cos(q);
+      rowsv[3 * j + 1] = (float)sin(q);
+      rowsv[3 * j + 2] = (float)((2.0 * M_PI / J.ws) * (sin(q1) - sin(q0)));
+    }
+    for (int i = 0; i < J.ho; ++i) {
+      double p = M_PI * ((double)i / J.ho - 0.5);
+      orows[2 * i] = (float)cos(p);
+      orows[2 * i + 1] = (float)sin(p);
+    }
+    // Synchronous copies: the tables are small and the host vectors die here.
+    e = cudaMemcpyAsync(base + P.cosd_off[k], cosd.data(), cosd.size() * 4,
+                        cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(base + P.rows_off[k], rowsv.data(), rowsv.size() * 4,
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(base + P.orows_off[k], orows.data(), orows.size() * 4,
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "tc tables");
+    J.cos_d = reinterpret_cast<const float*>(base + P.cosd_off[k]);
+    J.src_rows = reinterpret_cast<const float*>(base + P.rows_off[k]);
+    J.out_rows = reinterpret_cast<const float*>(base + P.orows_off[k]);
+    J.partial = reinterpret_cast<float*>(base + P.partial_off[k]);
+    J.error = reinterpret_cast<int*>(base);
+    size_t smem = smem_bytes(J);
+    e = cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
+    dim3 grid((J.ho + kM - 1) / kM, 8, J.ksplit);
+    contract_kernel<<<grid, kThreads, smem, s>>>(J);
+    double* wsum = reinterpret_cast<double*>(base + P.wsum_off[k]);
+    if (J.kind == 0) weight_sum_kernel<<<J.ho, 256, 0, s>>>(J, wsum);
+    float4* out;
+    long long pitch;
+    if ((int)k < n) {
+      out = reinterpret_cast<float4*>(mips[k].out_dev);
+      pitch = (long long)(mips[k].pitch_bytes / 16);
+    } else {
+      out = reinterpret_cast<float4*>(irr_out);
+      pitch = (long long)(irr_pitch / 16);
+    }
+    long long nt = (long long)J.wo * J.ho;
+    finish_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(J, wsum, out, pitch);
+  }
+  // Roughness-0 mips are a delta (no contraction): the plain path's exact
+  // texel-corner sample.
+  for (int m = 0; m < n; ++m) {
+    if (P.job_level[m] >= 0) continue;
+    st = launch_prefilter(chain, w, h, &mips[m], 1, 1024, ALTHEA_IBL_GEN_HAMMERSLEY, s);
+    if (st) return st;
+  }
+  return cuda_status(cudaGetLastError(), "tensor path launch");
+}
+
+extern "C" int althea_ibl_tc_error(const void* ws, void* stream) {
+  if (!ws) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null workspace");
+  int flag = 0;
+  cudaError_t e = cudaMemcpyAsync(&flag, ws, sizeof(int), cudaMemcpyDeviceToHost,
+                                  (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "tc status");
+  if (flag) return set_error(ALTHEA_IBL_ERR_CUDA, "tensor path: a bounded wait timed out");
+  return ALTHEA_IBL_OK;
+}

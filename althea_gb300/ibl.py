@@ -166,6 +166,13 @@ def load(build_if_missing: bool = True):
         "althea_ibl_server_request_bytes": (sz, [vp, i, i, i]),
         "althea_ibl_server_now": (ctypes.c_double, []),
         "althea_ibl_server_destroy": (i, [vp]),
+        "althea_ibl_tc_workspace_size": (sz, [i, i, ctypes.POINTER(MipTarget), i,
+                                              ctypes.POINTER(i), i, i, i]),
+        "althea_ibl_tc_plan": (i, [i, i, ctypes.POINTER(MipTarget), i, i, ctypes.POINTER(i),
+                                   ctypes.POINTER(i)]),
+        "althea_ibl_bake_tc": (i, [vp, i, i, ctypes.POINTER(MipTarget), i, ctypes.POINTER(i),
+                                   vp, i, i, sz, i, vp, sz, vp]),
+        "althea_ibl_tc_error": (i, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -561,3 +568,53 @@ class ProbeBatch:
             self.close()
         except Exception:
             pass
+
+
+# ---- precision path (tensor cores) ------------------------------------------------
+
+def tc_plan(w: int, h: int, mip_sizes: List[tuple], roughness: List[float],
+            irradiance_width: int = 0):
+    """Source level chosen per mip (-1: roughness 0, plain path) and for the
+    irradiance."""
+    n = len(mip_sizes)
+    arr = (MipTarget * max(n, 1))()
+    for k, ((mw, mh), r) in enumerate(zip(mip_sizes, roughness)):
+        arr[k] = MipTarget(0, mw * 16, mw, mh, float(r))
+    lv = (ctypes.c_int * max(n, 1))()
+    il = ctypes.c_int()
+    _check(load().althea_ibl_tc_plan(w, h, arr, n, irradiance_width, lv, ctypes.byref(il)))
+    return [lv[k] for k in range(n)], il.value
+
+
+def bake_tc(chain, w: int, h: int, outs: List, roughness: List[float], irradiance=None,
+            levels: Optional[List[int]] = None, irradiance_level: int = -1, workspace=None,
+            stream=None, check: bool = True):
+    """Precision-path bake into CUDA tensors (mips and optional irradiance)."""
+    torch = _torch()
+    n = len(outs)
+    arr = (MipTarget * max(n, 1))()
+    for k, (o, r) in enumerate(zip(outs, roughness)):
+        _require_cuda(o, f"mip {k}", 4)
+        arr[k] = MipTarget(o.data_ptr(), _pitch(o, 4), o.shape[1], o.shape[0], float(r))
+    lv = None
+    if levels is not None:
+        lv = (ctypes.c_int * max(n, 1))(*levels)
+    iw = ih = 0
+    ip = 0
+    ipitch = 0
+    if irradiance is not None:
+        _require_cuda(irradiance, "irradiance", 4)
+        ih, iw = irradiance.shape[:2]
+        ip, ipitch = irradiance.data_ptr(), _pitch(irradiance, 4)
+    L = load()
+    need = L.althea_ibl_tc_workspace_size(w, h, arr, n, lv, iw, ih, irradiance_level)
+    if need == 0:
+        raise IBLError(ERR_UNSUPPORTED, L.althea_ibl_last_error().decode())
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(need, dtype=torch.uint8, device=chain.device)
+    sp = _stream_ptr(stream)
+    _check(L.althea_ibl_bake_tc(chain.data_ptr(), w, h, arr, n, lv, ip, iw, ih, ipitch,
+                                irradiance_level, workspace.data_ptr(), need, sp))
+    if check:
+        _check(L.althea_ibl_tc_error(workspace.data_ptr(), sp))
+    return workspace

@@ -171,6 +171,32 @@ const float* althea_ibl_env_chain(const althea_ibl_context* ctx);
  * buffers: the dispatch sequence of Src/ImageBasedLighting.cpp:315-402. */
 int althea_ibl_bake(althea_ibl_context* ctx, const althea_ibl_outputs* outs, void* stream);
 
+/* ---- precision path: dense contraction on the tensor cores -------------------
+ * Replaces the two estimators of Shaders/IBL_Precompute/*.comp by the
+ * quadrature they estimate: prefilter(n) = sum_t L_t w / sum_t w with
+ * w = D_GGX(n.h) max(0, n.w_t) Omega_t, irradiance(n) = (1/pi) sum_t L_t
+ * max(0, n.w_t) Omega_t, over the texels of one env level per output (picked
+ * by althea_ibl_tc_plan so the result stays within 1e-3 of the same sum over
+ * level 0; levels[m] = -1 selects the plan).  tcgen05 BF16 hi/lo MMAs with
+ * FP32 accumulation in TMEM, FP64 weight normalisation.  Roughness-0 mips
+ * (a delta) take the plain path.  Output mips must be at most 1024 wide.
+ * Workspace: althea_ibl_tc_workspace_size bytes, 256-byte aligned.
+ * althea_ibl_tc_error synchronises the stream and reports a kernel that gave
+ * up on a bounded wait. */
+size_t althea_ibl_tc_workspace_size(int env_width, int env_height,
+                                    const althea_ibl_mip_target* mips, int mip_count,
+                                    const int* levels, int irradiance_width,
+                                    int irradiance_height, int irradiance_level);
+int althea_ibl_tc_plan(int env_width, int env_height, const althea_ibl_mip_target* mips,
+                       int mip_count, int irradiance_width, int* levels_out,
+                       int* irradiance_level_out);
+int althea_ibl_bake_tc(const float* chain_dev, int env_width, int env_height,
+                       const althea_ibl_mip_target* mips, int mip_count, const int* levels,
+                       float* irradiance_dev, int irradiance_width, int irradiance_height,
+                       size_t irradiance_pitch_bytes, int irradiance_level, void* workspace_dev,
+                       size_t workspace_bytes, void* stream);
+int althea_ibl_tc_error(const void* workspace_dev, void* stream);
+
 /* ---- batched bakes -----------------------------------------------------------
  * No single counterpart in the reference, which bakes one probe per
  * createResources call (Src/GlobalResources.cpp:18-22); a batch bakes many

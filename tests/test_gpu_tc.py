@@ -1,0 +1,79 @@
+"""GPU tests of the precision path (tcgen05 BF16 hi/lo contraction).
+
+1. The kernel computes the planned quadrature: against the FP64 oracle summed
+   over the same source level, within 1e-4 relative (BF16 hi/lo products are
+   good to ~2^-17; FP32 accumulation of positive terms).
+2. The plan keeps the result within 1e-3 of the FP64 quadrature over level 0
+   (the contract of the precision path).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from althea_gb300 import ibl, synth
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _rel(got, ref):
+    return np.abs(got - ref) / np.abs(ref)
+
+
+def test_contraction_matches_fp64_quadrature_at_same_source_level():
+    w, h = 512, 256
+    env = synth.make_env(w, h, seed=8, sun_max=1e6)
+    chain = oracle.build_chain(env)
+    chain_d = torch.from_numpy(chain).cuda()
+    sizes = [(128, 64), (64, 32), (16, 8), (256, 128)]
+    rough = [0.25, 0.5, 1.0, 0.125]
+    levels = [1, 1, 2, 1]
+    outs = [torch.empty((mh, mw, 4), dtype=torch.float32, device="cuda") for mw, mh in sizes]
+    irr = torch.empty((16, 32, 4), dtype=torch.float32, device="cuda")
+    ibl.bake_tc(chain_d, w, h, outs, rough, irradiance=irr, levels=levels, irradiance_level=2)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(0)
+    for (mw, mh), r, lv, o in zip(sizes, rough, levels, outs):
+        src = oracle.chain_level(chain, w, h, lv)
+        n = min(mw * mh, 256)
+        idx = rng.choice(mw * mh, size=n, replace=False)
+        xy = np.stack([idx % mw, idx // mw], 1).astype(np.int32)
+        ref = oracle.quad_prefilter(src, mw, mh, r, xy)[:, :3]
+        got = o.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
+        assert _rel(got, ref).max() <= 1e-4, (mw, r, _rel(got, ref).max())
+    src = oracle.chain_level(chain, w, h, 2)
+    ys, xs = np.mgrid[0:16, 0:32]
+    xy = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
+    ref = oracle.quad_irradiance(src, 32, 16, xy)[:, :3]
+    got = irr.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
+    assert _rel(got, ref).max() <= 1e-4, _rel(got, ref).max()
+
+
+def test_plan_meets_1e3_against_level0_quadrature():
+    w, h = 1024, 512
+    env = synth.make_env(w, h, seed=2, sun_max=1e6)
+    chain = oracle.build_chain(env)
+    chain_d = torch.from_numpy(chain).cuda()
+    sizes = [(512 >> m, 256 >> m) for m in range(7)]
+    rough = [m / 6 for m in range(7)]
+    outs = [torch.empty((mh, mw, 4), dtype=torch.float32, device="cuda") for mw, mh in sizes]
+    irr = torch.empty((32, 64, 4), dtype=torch.float32, device="cuda")
+    ibl.bake_tc(chain_d, w, h, outs, rough, irradiance=irr)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(1)
+    lvl0 = oracle.chain_level(chain, w, h, 0)
+    for (mw, mh), r, o in zip(sizes[1:], rough[1:], outs[1:]):
+        n = min(mw * mh, 48)
+        idx = rng.choice(mw * mh, size=n, replace=False)
+        xy = np.stack([idx % mw, idx // mw], 1).astype(np.int32)
+        ref = oracle.quad_prefilter(lvl0, mw, mh, r, xy)[:, :3]
+        got = o.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
+        assert _rel(got, ref).max() <= 1e-3, (mw, r, _rel(got, ref).max())
+    # roughness 0 takes the plain path (a delta)
+    ref0 = oracle.prefilter(chain, w, h, 512, 256, 0.0, 1024, oracle.GEN_HAMMERSLEY)
+    assert np.array_equal(outs[0].cpu().numpy(), ref0)
+    idx = rng.choice(64 * 32, size=48, replace=False)
+    xy = np.stack([idx % 64, idx // 64], 1).astype(np.int32)
+    ref = oracle.quad_irradiance(lvl0, 64, 32, xy)[:, :3]
+    got = irr.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
+    assert _rel(got, ref).max() <= 1e-3, _rel(got, ref).max()
