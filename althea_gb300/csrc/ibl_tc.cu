@@ -50,7 +50,9 @@ namespace tc {
 
 constexpr int kM = 128;          // output rows per CTA (TMEM lanes)
 constexpr int kKStep = 64;       // K per pipeline step (4 MMA instructions)
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;   // direct kernel
+constexpr int kHThreads = 512;  // Hankel kernel
+constexpr int kDrain = 128;     // MMA steps per TMEM accumulation chain
 
 
 constexpr long long kSpinLimit = 1LL << 26;
@@ -154,10 +156,14 @@ struct Job {
   int kpad;                     // polyphase row length padded to a multiple of 16
   int ksplit;                   // source rows are split over this many CTAs
   int tmem_cols;                // power of two >= 3 * n_mma (channel c at column c * n_mma)
+  int direct;                   // 1: direct kernel (M = output texels, N = radiance planes)
   const float* cos_d;           // [ws]  cos(2 pi (d + 0.5) / ws)
   const float* src_rows;        // [hs][3]  cos q, sin q, Omega
   const float* out_rows;        // [ho][2]  cos p, sin p
+  const float* src_cols;        // [ws][2]  cos, sin of source column yaw (direct kernel)
+  const float* out_cols;        // [wo][2]  cos, sin of output column yaw (direct kernel)
   float* partial;               // [ksplit][ho][3][wo]
+  double* wsum_part;            // [ksplit][ho*wo] weight sums (direct kernel)
   int* error;                   // set on a bounded-wait timeout
 };
 
@@ -180,8 +186,12 @@ struct Smem {
   }
 };
 
-// The contraction kernel.  Grid: (ceil(ho/128), 8 x residues, ksplit).
-__global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
+// The contraction kernel (Hankel form).  Grid: (ceil(ho/128), 8 x residues,
+// ksplit); 512 threads generate weights, thread 0 issues the MMAs.  Every
+// kDrain steps the TMEM accumulators are drained into the CTA's FP32 partial
+// sums (IEEE round-to-nearest adds) and restarted, which keeps the tensor
+// core's accumulation chains short.
+__global__ void __launch_bounds__(kHThreads, 1) contract_kernel(const Job job) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t mbar[2];
   __shared__ uint32_t tmem_base_sh;
@@ -206,12 +216,12 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int i = tid; i < kM; i += kThreads) {
+  for (int i = tid; i < kM; i += kHThreads) {
     int gi = i0 + i;
     rowc[i] = gi < job.ho ? job.out_rows[2 * gi] : 0.0f;
     rows[i] = gi < job.ho ? job.out_rows[2 * gi + 1] : 0.0f;
   }
-  for (int d = tid; d < job.ws; d += kThreads) cosd[d] = job.cos_d[d];
+  for (int d = tid; d < job.ws; d += kHThreads) cosd[d] = job.cos_d[d];
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base_sh)),
@@ -229,13 +239,23 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   const int j1 = min(job.hs, j0 + j_per);
   const int wo_ph = job.wo;            // polyphase row length = ws / s = wo
   const int ksteps_row = (job.kpad + kKStep - 1) / kKStep;
+  const long long total_steps =
+      (j1 > j0 ? (long long)(j1 - j0) : 0LL) * job.s * ksteps_row;
   const uint32_t idesc = idesc_bf16(kM, job.n_mma);
+  const int gi_row = tid >> 2;           // weight row 0..127
+  const int kk0 = (tid & 3) * 16;        // 16 consecutive k per thread
+  const bool row_ok = i0 + gi_row < job.ho;
+  const float cp = rowc[gi_row], sp = rows[gi_row];
+  const int out_i = i0 + warp * 32 + lane;   // TMEM lane owned in a drain (warps 0-3)
+  bool first_drain = true;
 
   long long step = 0;
   bool ok = true;
+  bool fresh = true;  // the next MMA of each channel overwrites the accumulator
   for (int j = j0; j < j1 && ok; ++j) {
     const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
     const float om = job.src_rows[3 * j + 2];
+    const float ccq = cp * cq, ssq = sp * sq;
     for (int ph = 0; ph < job.s && ok; ++ph) {
       for (int kc = 0; kc < ksteps_row && ok; ++kc, ++step) {
         const int stage = (int)(step & 1);
@@ -257,9 +277,9 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
         // (2) stage the polyphase row (x residue folded in) on a row start:
         // buf[t] = plane[j][(s * (t + xph) + ph) mod ws].
         if (kc == 0) {
-          for (int e = tid; e < 6 * rlen; e += kThreads) {
+          for (int e = tid; e < 6 * rlen; e += kHThreads) {
             int p = e / rlen, t = e - p * rlen;
-            long long src = ((long long)job.s * (t + xph) + ph) % job.ws;
+            unsigned src = ((unsigned)job.s * (unsigned)(t + xph) + (unsigned)ph) % (unsigned)job.ws;
             slot_base[e] = job.planes[((size_t)p * job.hs + j) * job.ws + src];
           }
         }
@@ -267,40 +287,33 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
         // element (i, k) at (i/8)*1024 + (k/8)*128 + (i%8)*16 + (k%8)*2.
         unsigned char* a_hi = a_base + stage * 2 * Smem::kA;
         unsigned char* a_lo = a_hi + Smem::kA;
-        {
-          const int i = tid >> 1;           // 0..127
-          const int kk0 = (tid & 1) * 32;   // 32 consecutive k per thread
-          const float cp = rowc[i], sp = rows[i];
-          const bool row_ok = i0 + i < job.ho;
-          const float ccq = cp * cq, ssq = sp * sq;
 #pragma unroll
-          for (int g = 0; g < 4; ++g) {
-            uint32_t hw[4], lw[4];
+        for (int g = 0; g < 2; ++g) {
+          uint32_t hw[4], lw[4];
 #pragma unroll
-            for (int e = 0; e < 8; e += 2) {
-              float wv[2];
+          for (int e = 0; e < 8; e += 2) {
+            float wv[2];
 #pragma unroll
-              for (int u = 0; u < 2; ++u) {
-                int kl = kc * kKStep + kk0 + 8 * g + e + u;   // polyphase column
-                float w = 0.0f;
-                if (row_ok && kl < wo_ph) {
-                  int d = job.s * kl + ph;                    // y - s*x
-                  float c = fmaf(ccq, cosd[d], ssq);
-                  w = weight_of(c, job.a2, job.kind) * om;
-                }
-                wv[u] = w;
+            for (int u = 0; u < 2; ++u) {
+              int kl = kc * kKStep + kk0 + 8 * g + e + u;   // polyphase column
+              float w = 0.0f;
+              if (row_ok && kl < wo_ph) {
+                int d = job.s * kl + ph;                    // y - s*x
+                float c = fmaf(ccq, cosd[d], ssq);
+                w = weight_of(c, job.a2, job.kind) * om;
               }
-              __nv_bfloat162 h2 = __floats2bfloat162_rn(wv[0], wv[1]);
-              float2 hf = __bfloat1622float2(h2);
-              __nv_bfloat162 l2 = __floats2bfloat162_rn(wv[0] - hf.x, wv[1] - hf.y);
-              hw[e / 2] = *reinterpret_cast<uint32_t*>(&h2);
-              lw[e / 2] = *reinterpret_cast<uint32_t*>(&l2);
+              wv[u] = w;
             }
-            const int kk = kk0 + 8 * g;
-            const int off = (i >> 3) * 1024 + (kk >> 3) * 128 + (i & 7) * 16;
-            *reinterpret_cast<uint4*>(a_hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-            *reinterpret_cast<uint4*>(a_lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(wv[0], wv[1]);
+            float2 hf = __bfloat1622float2(h2);
+            __nv_bfloat162 l2 = __floats2bfloat162_rn(wv[0] - hf.x, wv[1] - hf.y);
+            hw[e / 2] = *reinterpret_cast<uint32_t*>(&h2);
+            lw[e / 2] = *reinterpret_cast<uint32_t*>(&l2);
           }
+          const int kk = kk0 + 8 * g;
+          const int off = (gi_row >> 3) * 1024 + (kk >> 3) * 128 + (gi_row & 7) * 16;
+          *reinterpret_cast<uint4*>(a_hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+          *reinterpret_cast<uint4*>(a_lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
         }
         fence_async_smem();
         tc_fence_before();
@@ -313,7 +326,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
           for (int q = 0; q < kmax / 16; ++q) {
             const uint64_t da_hi = smem_desc(ah + q * 256, 128, 1024);
             const uint64_t da_lo = smem_desc(al + q * 256, 128, 1024);
-            const uint32_t first = (j == j0 && ph == 0 && kc == 0 && q == 0) ? 0u : 1u;
+            const uint32_t first = (fresh && q == 0) ? 0u : 1u;
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
               const uint32_t bh = smem_u32(slot_base + (size_t)(2 * ch) * rlen) +
@@ -330,10 +343,43 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
           }
           mma_commit(&mbar[stage]);
         }
+        fresh = false;
+        // (5) drain the accumulators every kDrain steps and after the last.
+        if ((step + 1) % kDrain == 0 || step + 1 == total_steps) {
+          if (!mbar_wait(&mbar[stage], (uint32_t)((step >> 1) & 1))) {
+            if (tid == 0) abort_flag = 1;
+          }
+          tc_fence_after();
+          __syncthreads();
+          if (!abort_flag && warp < 4) {
+            for (int ch = 0; ch < 3; ++ch) {
+              for (int c0 = 0; c0 < job.n_mma; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) +
+                              (uint32_t)(ch * job.n_mma + c0), v);
+                if (out_i < job.ho) {
+#pragma unroll
+                  for (int u = 0; u < 16; ++u) {
+                    int x = xph + 8 * (c0 + u);
+                    if (x < job.wo) {
+                      float* pp =
+                          &job.partial[(((size_t)split * 3 + ch) * job.wo + x) * job.ho + out_i];
+                      *pp = first_drain ? v[u] : *pp + v[u];
+                    }
+                  }
+                }
+              }
+            }
+          }
+          first_drain = false;
+          fresh = true;
+          tc_fence_before();
+          __syncthreads();
+        }
       }
     }
   }
-  // Drain: the last commits of both stages.
+  // Make sure no MMA is in flight before TMEM is released.
   const long long nsteps = step;
   bool drained = true;
   for (long long s2 = nsteps - 2; s2 < nsteps; ++s2) {
@@ -342,37 +388,259 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   }
   tc_fence_after();
   __syncthreads();
-  if (!ok || !drained) {
+  if (!ok || !drained || abort_flag) {
     if (tid == 0) atomicExch(job.error, 1);
-  } else if (nsteps > 0 && warp < 4) {
-    // Epilogue: warp w reads TMEM lanes 32w..32w+31 (output rows).
-    const int i = i0 + warp * 32 + lane;
-    for (int ch = 0; ch < 3; ++ch) {
-      for (int c0 = 0; c0 < job.n_mma; c0 += 16) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(ch * job.n_mma + c0), v);
-        if (i < job.ho) {
-#pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            int x = xph + 8 * (c0 + u);
-            if (x < job.wo)
-              job.partial[(((size_t)split * job.ho + i) * 3 + ch) * job.wo + x] = v[u];
-          }
-        }
-      }
-    }
   } else if (nsteps == 0 && warp < 4) {
-    const int i = i0 + warp * 32 + lane;
-    if (i < job.ho)
+    if (out_i < job.ho)
       for (int ch = 0; ch < 3; ++ch)
         for (int x = xph; x < job.wo; x += 8)
-          job.partial[(((size_t)split * job.ho + i) * 3 + ch) * job.wo + x] = 0.0f;
+          job.partial[(((size_t)split * 3 + ch) * job.wo + x) * job.ho + out_i] = 0.0f;
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"((uint32_t)job.tmem_cols));
+}
+
+// Direct contraction for narrow outputs: M = 128 output texels (flattened),
+// N = 16 (the six hi/lo radiance planes, zero-padded), K = source texels.
+// Weights have no shift reuse here (each (output, source) pair is generated
+// once), so the CUDA cores bound it; it replaces the polyphase Hankel form
+// when a source row would split into many tiny polyphase rows.  Same
+// pipeline and bounded waits as contract_kernel; weight sums accumulate per
+// output texel in FP64.  Grid: (ceil(ho*wo/128), ksplit).
+__global__ void __launch_bounds__(kThreads, 2) contract_direct_kernel(const Job job) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t mbar[2];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ float dirx[kM], diry[kM], dirz[kM];
+  __shared__ double wsum_sh[kThreads];
+  __shared__ int abort_flag;
+  constexpr int kB = 16 * kKStep * 2;  // one bf16 B tile (2 KB)
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long o0 = (long long)blockIdx.x * kM;
+  const long long nout = (long long)job.ho * job.wo;
+  const int split = blockIdx.y;
+  unsigned char* a_base = smem;                         // [2 stages][hi, lo] 16 KB each
+  unsigned char* b_base = smem + 4 * (16 * 1024);       // [2 stages] 2 KB each
+  float* ccol = reinterpret_cast<float*>(b_base + 2 * kB);  // [ws][2]
+
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int i = tid; i < kM; i += kThreads) {
+    long long o = o0 + i;
+    float x = 0.0f, y = 0.0f, z = 0.0f;
+    if (o < nout) {
+      int oi = (int)(o / job.wo), ox = (int)(o % job.wo);
+      float cp = job.out_rows[2 * oi], sp = job.out_rows[2 * oi + 1];
+      x = cp * job.out_cols[2 * ox];
+      y = sp;
+      z = cp * job.out_cols[2 * ox + 1];
+    }
+    dirx[i] = x;
+    diry[i] = y;
+    dirz[i] = z;
+  }
+  for (int d = tid; d < 2 * job.ws; d += kThreads) ccol[d] = job.src_cols[d];
+  // rows 6..15 of both B tiles stay zero
+  for (int e = tid; e < 2 * kB / 16; e += kThreads)
+    reinterpret_cast<uint4*>(b_base)[e] = make_uint4(0, 0, 0, 0);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_sh)),
+                 "r"((uint32_t)job.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+  const int j_per = (job.hs + job.ksplit - 1) / job.ksplit;
+  const int j0 = split * j_per;
+  const int j1 = min(job.hs, j0 + j_per);
+  const int chunks = job.ws / kKStep;
+  const long long total_steps = (j1 > j0 ? (long long)(j1 - j0) : 0LL) * chunks;
+  const uint32_t idesc = idesc_bf16(kM, 16);
+  const int oi = tid >> 1, kk0 = (tid & 1) * 32;
+  const float nx = dirx[oi], ny = diry[oi], nz = dirz[oi];
+  double acc6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // drained sums (warps 0-3)
+  bool fresh = true;
+  double wacc = 0.0;
+
+  long long step = 0;
+  bool ok = true;
+  for (int j = j0; j < j1 && ok; ++j) {
+    const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
+    const float om = job.src_rows[3 * j + 2];
+    const float sny = sq * ny;
+    for (int ch = 0; ch < chunks && ok; ++ch, ++step) {
+      const int stage = (int)(step & 1);
+      if (step >= 2) {
+        if (!mbar_wait(&mbar[stage], (uint32_t)(((step - 2) >> 1) & 1))) {
+          if (tid == 0) abort_flag = 1;
+        }
+      }
+      __syncthreads();
+      if (abort_flag) {
+        ok = false;
+        break;
+      }
+      const int y0 = ch * kKStep;
+      unsigned char* bt = b_base + stage * kB;
+      if (tid < 48) {  // 6 planes x 8 chunks of 8 bf16
+        int p = tid >> 3, c8 = tid & 7;
+        const uint4* src = reinterpret_cast<const uint4*>(
+            job.planes + ((size_t)p * job.hs + j) * job.ws + y0 + 8 * c8);
+        *reinterpret_cast<uint4*>(bt + c8 * 128 + p * 16) = __ldg(src);
+      }
+      unsigned char* a_hi = a_base + stage * 2 * Smem::kA;
+      unsigned char* a_lo = a_hi + Smem::kA;
+      float wsum_step = 0.0f;
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        uint32_t hw[4], lw[4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          float wv[2];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            int y = y0 + kk0 + 8 * g + e + u;
+            float c = fmaf(cq, fmaf(nx, ccol[2 * y], nz * ccol[2 * y + 1]), sny);
+            float w = (o0 + oi < nout) ? weight_of(c, job.a2, job.kind) * om : 0.0f;
+            wv[u] = w;
+            wsum_step += w;
+          }
+          __nv_bfloat162 h2 = __floats2bfloat162_rn(wv[0], wv[1]);
+          float2 hf = __bfloat1622float2(h2);
+          __nv_bfloat162 l2 = __floats2bfloat162_rn(wv[0] - hf.x, wv[1] - hf.y);
+          hw[e / 2] = *reinterpret_cast<uint32_t*>(&h2);
+          lw[e / 2] = *reinterpret_cast<uint32_t*>(&l2);
+        }
+        const int kk = kk0 + 8 * g;
+        const int off = (oi >> 3) * 1024 + (kk >> 3) * 128 + (oi & 7) * 16;
+        *reinterpret_cast<uint4*>(a_hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *reinterpret_cast<uint4*>(a_lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+      }
+      wacc += (double)wsum_step;
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bb = smem_u32(bt);
+        for (int q = 0; q < kKStep / 16; ++q) {
+          const uint64_t da_hi = smem_desc(ah + q * 256, 128, 1024);
+          const uint64_t da_lo = smem_desc(al + q * 256, 128, 1024);
+          const uint64_t db = smem_desc(bb + q * 256, 128, 1024);
+          mma_bf16(tmem, da_hi, db, idesc, (fresh && q == 0) ? 0u : 1u);
+          mma_bf16(tmem, da_lo, db, idesc, 1u);
+        }
+        mma_commit(&mbar[stage]);
+      }
+      fresh = false;
+      // Drain the accumulator into FP64 registers every kDrain steps.
+      if ((step + 1) % kDrain == 0 || step + 1 == total_steps) {
+        if (!mbar_wait(&mbar[stage], (uint32_t)((step >> 1) & 1))) {
+          if (tid == 0) abort_flag = 1;
+        }
+        tc_fence_after();
+        __syncthreads();
+        if (!abort_flag && warp < 4) {
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), v);
+#pragma unroll
+          for (int u = 0; u < 6; ++u) acc6[u] += (double)v[u];
+        }
+        fresh = true;
+        tc_fence_before();
+        __syncthreads();
+      }
+    }
+  }
+  const long long nsteps = step;
+  bool drained = true;
+  for (long long s2 = nsteps - 2; s2 < nsteps; ++s2) {
+    if (s2 < 0) continue;
+    if (!mbar_wait(&mbar[s2 & 1], (uint32_t)((s2 >> 1) & 1))) drained = false;
+  }
+  wsum_sh[tid] = wacc;
+  tc_fence_after();
+  __syncthreads();
+  if (!ok || !drained || abort_flag) {
+    if (tid == 0) atomicExch(job.error, 1);
+  } else if (warp < 4) {
+    const int i = warp * 32 + lane;
+    const long long o = o0 + i;
+    if (o < nout) {
+      float* pp = job.partial + ((size_t)split * nout + o) * 3;
+      pp[0] = (float)(acc6[0] + acc6[1]);
+      pp[1] = (float)(acc6[2] + acc6[3]);
+      pp[2] = (float)(acc6[4] + acc6[5]);
+      job.wsum_part[(size_t)split * nout + o] = wsum_sh[2 * i] + wsum_sh[2 * i + 1];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"((uint32_t)job.tmem_cols));
+}
+
+__global__ void finish_direct_kernel(const Job job, float4* __restrict__ out, long long pitch) {
+  long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nout = (long long)job.ho * job.wo;
+  if (o >= nout) return;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, w = 0.0;
+  for (int k = 0; k < job.ksplit; ++k) {
+    const float* p = job.partial + ((size_t)k * nout + o) * 3;
+    s0 += p[0];
+    s1 += p[1];
+    s2 += p[2];
+    w += job.wsum_part[(size_t)k * nout + o];
+  }
+  double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / w);
+  int x = (int)(o % job.wo), i = (int)(o / job.wo);
+  out[(long long)i * pitch + x] =
+      make_float4((float)(s0 * norm), (float)(s1 * norm), (float)(s2 * norm), 1.0f);
+}
+
+// Direction tables in FP64, stored as FP32: cos of the column offsets
+// (2 pi (d + 0.5) / ws), source rows (cos q, sin q, solid angle), output
+// rows (cos p, sin p at texel corners), and for the direct kernel the source
+// and output column yaws (cos, sin).
+__global__ void tables_kernel(int ws, int hs, int ho, int wo, float* __restrict__ cosd,
+                              float* __restrict__ srows, float* __restrict__ orows,
+                              float* __restrict__ scols, float* __restrict__ ocols) {
+  const double pi = 3.14159265358979323846;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < ws) {
+    cosd[t] = (float)cos(2.0 * pi * (t + 0.5) / ws);
+    double yaw = pi * (2.0 * (t + 0.5) / ws - 1.0);
+    scols[2 * t] = (float)cos(yaw);
+    scols[2 * t + 1] = (float)sin(yaw);
+  }
+  if (t < wo) {
+    double yaw = pi * (2.0 * t / wo - 1.0);
+    ocols[2 * t] = (float)cos(yaw);
+    ocols[2 * t + 1] = (float)sin(yaw);
+  }
+  if (t < hs) {
+    double q = pi * ((t + 0.5) / hs - 0.5);
+    double q0 = pi * ((double)t / hs - 0.5), q1 = pi * ((double)(t + 1) / hs - 0.5);
+    srows[3 * t] = (float)cos(q);
+    srows[3 * t + 1] = (float)sin(q);
+    srows[3 * t + 2] = (float)((2.0 * pi / ws) * (sin(q1) - sin(q0)));
+  }
+  if (t < ho) {
+    double p = pi * ((double)t / ho - 0.5);
+    orows[2 * t] = (float)cos(p);
+    orows[2 * t + 1] = (float)sin(p);
+  }
 }
 
 // RGBA32F source level -> 6 bf16 planes (R hi, R lo, G hi, G lo, B hi, B lo).
@@ -429,7 +697,7 @@ __global__ void finish_kernel(const Job job, const double* __restrict__ wsum,
   double s[3] = {0.0, 0.0, 0.0};
   for (int k = 0; k < job.ksplit; ++k)
     for (int ch = 0; ch < 3; ++ch)
-      s[ch] += (double)job.partial[(((size_t)k * job.ho + i) * 3 + ch) * job.wo + x];
+      s[ch] += (double)job.partial[(((size_t)k * 3 + ch) * job.wo + x) * job.ho + i];
   double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / wsum[i]);
   out[(long long)i * pitch + x] =
       make_float4((float)(s[0] * norm), (float)(s[1] * norm), (float)(s[2] * norm), 1.0f);
@@ -456,10 +724,8 @@ int planned_level(int w, int ow, float roughness, bool irradiance) {
   int target;
   if (irradiance)
     target = 2048;
-  else if (roughness <= 0.40f)
-    target = 1024;
   else if (roughness <= 0.55f)
-    target = 512;
+    target = 1024;
   else if (roughness >= 0.85f && roughness <= 0.90f)
     target = 512;
   else
@@ -481,7 +747,7 @@ struct TcPlan {
   std::vector<Job> jobs;
   std::vector<int> job_level;      // index into levels
   std::vector<LevelPlanes> levels;
-  std::vector<size_t> cosd_off, rows_off, orows_off, partial_off, wsum_off;
+  std::vector<size_t> cosd_off, rows_off, orows_off, scols_off, ocols_off, partial_off, wsum_off;
   size_t total = 0;
 };
 
@@ -519,8 +785,29 @@ void add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind,
   J.kpad = ((ow + 15) / 16) * 16;
   J.tmem_cols = 32;
   while (J.tmem_cols < 3 * J.n_mma) J.tmem_cols <<= 1;
-  int ctas = ((oh + kM - 1) / kM) * 8;
-  int ks = 152 / ctas;  // one wave of CTAs
+  // Pipeline steps of each form (K = 64 per step): the Hankel form pays for
+  // every polyphase row of every source row in each of 8 x residues; the
+  // direct form pays for every source texel in each 128-texel output tile.
+  const double itiles = (oh + kM - 1) / kM;
+  const double hankel_steps = itiles * 8 * J.hs * (double)J.s * ((J.kpad + kKStep - 1) / kKStep);
+  const double otiles = ((double)oh * ow + kM - 1) / kM;
+  const double direct_steps = otiles * J.hs * ((double)J.ws / kKStep);
+  J.direct = (J.ws % kKStep == 0) && 1100.0 * direct_steps < 2500.0 * hankel_steps;
+  int ctas;
+  if (J.direct) {
+    J.tmem_cols = 32;
+    ctas = (int)otiles;
+  } else {
+    ctas = (int)itiles * 8;
+  }
+  // Split the source rows so the CTAs fill whole waves of the 152 SMs.
+  int g = 152, b = ctas;
+  while (b) {
+    int t = g % b;
+    g = b;
+    b = t;
+  }
+  int ks = 152 / g;
   if (ks > J.hs) ks = J.hs;
   if (ks < 1) ks = 1;
   J.ksplit = ks;
@@ -532,10 +819,14 @@ void add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind,
   off = al256(off + (size_t)J.hs * 12);
   P.orows_off.push_back(off);
   off = al256(off + (size_t)oh * 8);
+  P.scols_off.push_back(off);
+  off = al256(off + (size_t)J.ws * 8);
+  P.ocols_off.push_back(off);
+  off = al256(off + (size_t)ow * 8);
   P.partial_off.push_back(off);
   off = al256(off + (size_t)ks * oh * 3 * ow * 4);
   P.wsum_off.push_back(off);
-  off = al256(off + (size_t)oh * 8);
+  off = al256(off + (J.direct ? (size_t)ks * oh * ow * 8 : (size_t)oh * 8));
 }
 
 int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int* levels,
@@ -548,6 +839,8 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
       P.cosd_off.push_back(0);
       P.rows_off.push_back(0);
       P.orows_off.push_back(0);
+      P.scols_off.push_back(0);
+      P.ocols_off.push_back(0);
       P.partial_off.push_back(0);
       P.wsum_off.push_back(0);
       continue;
@@ -575,6 +868,7 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
 }
 
 size_t smem_bytes(const Job& J) {
+  if (J.direct) return (size_t)4 * Smem::kA + 2 * (16 * kKStep * 2) + (size_t)J.ws * 8;
   int rlen = Smem::row_len(J.n_mma, J.kpad);
   return (size_t)Smem::kAStages * 2 * Smem::kA + (size_t)Smem::kRowSlots * 6 * rlen * 2 +
          (size_t)J.ws * 4;
@@ -638,50 +932,45 @@ extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
     split_kernel<<<(nt + 255) / 256, 256, 0, s>>>(
         src, nt, reinterpret_cast<__nv_bfloat16*>(base + L.offset));
   }
-  std::vector<float> host;
   for (size_t k = 0; k < P.jobs.size(); ++k) {
     if (P.job_level[k] < 0) continue;
     Job& J = P.jobs[k];
     const LevelPlanes& L = P.levels[P.job_level[k]];
     J.planes = reinterpret_cast<const __nv_bfloat16*>(base + L.offset);
-    std::vector<float> cosd(J.ws), rowsv((size_t)J.hs * 3), orows((size_t)J.ho * 2);
-    for (int d = 0; d < J.ws; ++d) cosd[d] = (float)cos(2.0 * M_PI * (d + 0.5) / J.ws);
-    for (int j = 0; j < J.hs; ++j) {
-      double q = M_PI * ((j + 0.5) / J.hs - 0.5);
-      double q0 = M_PI * ((double)j / J.hs - 0.5), q1 = M_PI * ((double)(j + 1) / J.hs - 0.5);
-      rowsv[3 * j] = (float)cos(q);
-      rowsv[3 * j + 1] = (float)sin(q);
-      rowsv[3 * j + 2] = (float)((2.0 * M_PI / J.ws) * (sin(q1) - sin(q0)));
-    }
-    for (int i = 0; i < J.ho; ++i) {
-      double p = M_PI * ((double)i / J.ho - 0.5);
-      orows[2 * i] = (float)cos(p);
-      orows[2 * i + 1] = (float)sin(p);
-    }
-    // Synchronous copies: the tables are small and the host vectors die here.
-    e = cudaMemcpyAsync(base + P.cosd_off[k], cosd.data(), cosd.size() * 4,
-                        cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(base + P.rows_off[k], rowsv.data(), rowsv.size() * 4,
-                          cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(base + P.orows_off[k], orows.data(), orows.size() * 4,
-                          cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return cuda_status(e, "tc tables");
-    J.cos_d = reinterpret_cast<const float*>(base + P.cosd_off[k]);
-    J.src_rows = reinterpret_cast<const float*>(base + P.rows_off[k]);
-    J.out_rows = reinterpret_cast<const float*>(base + P.orows_off[k]);
+    float* cosd = reinterpret_cast<float*>(base + P.cosd_off[k]);
+    float* srows = reinterpret_cast<float*>(base + P.rows_off[k]);
+    float* orows = reinterpret_cast<float*>(base + P.orows_off[k]);
+    float* scols = reinterpret_cast<float*>(base + P.scols_off[k]);
+    float* ocols = reinterpret_cast<float*>(base + P.ocols_off[k]);
+    int nmax = J.ws > J.hs ? J.ws : J.hs;
+    if (J.ho > nmax) nmax = J.ho;
+    if (J.wo > nmax) nmax = J.wo;
+    tables_kernel<<<(nmax + 255) / 256, 256, 0, s>>>(J.ws, J.hs, J.ho, J.wo, cosd, srows, orows,
+                                                     scols, ocols);
+    J.cos_d = cosd;
+    J.src_rows = srows;
+    J.out_rows = orows;
+    J.src_cols = scols;
+    J.out_cols = ocols;
     J.partial = reinterpret_cast<float*>(base + P.partial_off[k]);
     J.error = reinterpret_cast<int*>(base);
-    size_t smem = smem_bytes(J);
-    e = cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
-    dim3 grid((J.ho + kM - 1) / kM, 8, J.ksplit);
-    contract_kernel<<<grid, kThreads, smem, s>>>(J);
     double* wsum = reinterpret_cast<double*>(base + P.wsum_off[k]);
-    if (J.kind == 0) weight_sum_kernel<<<J.ho, 256, 0, s>>>(J, wsum);
+    size_t smem = smem_bytes(J);
+    if (J.direct) {
+      J.wsum_part = wsum;
+      e = cudaFuncSetAttribute(contract_direct_kernel,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
+      dim3 grid((unsigned)(((long long)J.ho * J.wo + kM - 1) / kM), J.ksplit);
+      contract_direct_kernel<<<grid, kThreads, smem, s>>>(J);
+    } else {
+      e = cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
+      dim3 grid((J.ho + kM - 1) / kM, 8, J.ksplit);
+      contract_kernel<<<grid, kHThreads, smem, s>>>(J);
+      if (J.kind == 0) weight_sum_kernel<<<J.ho, 256, 0, s>>>(J, wsum);
+    }
     float4* out;
     long long pitch;
     if ((int)k < n) {
@@ -692,7 +981,10 @@ extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
       pitch = (long long)(irr_pitch / 16);
     }
     long long nt = (long long)J.wo * J.ho;
-    finish_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(J, wsum, out, pitch);
+    if (J.direct)
+      finish_direct_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(J, out, pitch);
+    else
+      finish_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(J, wsum, out, pitch);
   }
   // Roughness-0 mips are a delta (no contraction): the plain path's exact
   // texel-corner sample.

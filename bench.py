@@ -373,6 +373,164 @@ def run_ours(args):
     return 0
 
 
+def tc_algorithmic_flops(levels, irr_level):
+    """2 * outputs * sources * 4 per contraction (RGB + weight, counted once)."""
+    total = 0
+    for (w, h), lv in zip(mip_sizes(), levels):
+        if lv >= 0:
+            total += 2 * w * h * max(ENV_W >> lv, 1) * max(ENV_H >> lv, 1) * 4
+    total += 2 * IRR_W * IRR_H * max(ENV_W >> irr_level, 1) * max(ENV_H >> irr_level, 1) * 4
+    return total
+
+
+def error_table(env, outs_by_path, irr_by_path, per_mip=12, seed=7):
+    """Max/mean relative error of each path against the FP64 quadrature over
+    level 0 (oracle O2) on sampled texels of every mip with roughness > 0 and
+    of the irradiance."""
+    import oracle
+    rng = np.random.default_rng(seed)
+    res = {k: {} for k in outs_by_path}
+    for m, ((w, h), r) in enumerate(zip(mip_sizes(), roughness())):
+        if r == 0.0:
+            continue
+        n = min(per_mip, w * h)
+        idx = rng.choice(w * h, size=n, replace=False)
+        xy = np.stack([idx % w, idx // w], 1).astype(np.int32)
+        ref = oracle.quad_prefilter(env, w, h, r, xy)[:, :3]
+        for k, outs in outs_by_path.items():
+            got = outs[m][xy[:, 1], xy[:, 0], :3]
+            e = np.abs(got - ref) / np.abs(ref)
+            res[k][f"mip{m}"] = [float(e.max()), float(e.mean())]
+    idx = rng.choice(IRR_W * IRR_H, size=per_mip, replace=False)
+    xy = np.stack([idx % IRR_W, idx // IRR_W], 1).astype(np.int32)
+    ref = oracle.quad_irradiance(env, IRR_W, IRR_H, xy)[:, :3]
+    for k, irr in irr_by_path.items():
+        got = irr[xy[:, 1], xy[:, 0], :3]
+        e = np.abs(got - ref) / np.abs(ref)
+        res[k]["irradiance"] = [float(e.max()), float(e.mean())]
+    for k in res:
+        res[k]["max"] = max(v[0] for v in res[k].values())
+    return res
+
+
+def run_tc(args):
+    """Precision configuration: 4096x2048 map with suns up to 1e6; mips 1-8 and
+    the irradiance as tensor-core contractions (roughness-0 mip 0 via the plain
+    kernel), plus chain and LUT; compared with the plain path on the same map."""
+    import torch
+    from althea_gb300 import ibl, synth
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    env = synth.make_env(ENV_W, ENV_H, seed=rank, sun_max=args.sun_max)
+    env_d = torch.from_numpy(env).to(dev)
+    chain = torch.empty((ibl.chain_texels(ENV_W, ENV_H), 4), dtype=torch.float32, device=dev)
+    mips = [torch.empty((h, w, 4), dtype=torch.float32, device=dev) for w, h in mip_sizes()]
+    irr = torch.empty((IRR_H, IRR_W, 4), dtype=torch.float32, device=dev)
+    lut = torch.empty((LUT_N, LUT_N, 2), dtype=torch.float32, device=dev)
+    rough = roughness()
+    levels, irr_level = ibl.tc_plan(ENV_W, ENV_H, mip_sizes(), rough, IRR_W)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ibl.build_env_chain_into(env_d, chain, stream)
+    ws = ibl.bake_tc(chain, ENV_W, ENV_H, mips, rough, irradiance=irr, stream=stream)
+
+    def step(ev):
+        ev[0].record(stream)
+        ibl.build_env_chain_into(env_d, chain, stream)
+        ev[1].record(stream)
+        ibl.bake_tc(chain, ENV_W, ENV_H, mips, rough, irradiance=irr, workspace=ws,
+                    stream=stream, check=False)
+        ev[2].record(stream)
+        ibl.brdf_lut(LUT_N, LUT_SAMPLES, ibl.LUT_ASSET, out=lut, stream=stream)
+        ev[3].record(stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step([torch.cuda.Event(enable_timing=True) for _ in range(4)])
+    stream.synchronize()
+    evs = []
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                flush.fill_(1)
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+                step(ev)
+                evs.append(ev)
+        torch.cuda.synchronize()
+    ibl._check(ibl.load().althea_ibl_tc_error(ws.data_ptr(), stream.cuda_stream))
+    step_ms = float(np.mean([e[0].elapsed_time(e[3]) for e in evs]))
+    tc_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+    # e2e: pinned host env in, every output out, through the public calls
+    host_env = torch.from_numpy(env).pin_memory()
+    h_outs = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in mips + [irr, lut]]
+
+    def e2e_step():
+        env_d.copy_(host_env, non_blocking=True)
+        step([torch.cuda.Event(enable_timing=True) for _ in range(4)])
+        for hdst, dsrc in zip(h_outs, mips + [irr, lut]):
+            hdst.copy_(dsrc, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        e2e_step()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        b.record(stream)
+    stream.synchronize()
+    e2e_ms = a.elapsed_time(b) / args.steps
+    tc_outs = [t.cpu().numpy() for t in mips]
+    tc_irr = irr.cpu().numpy()
+    # the plain path on the same map (Hammersley, N = 1024) for the error table
+    p_mips = [torch.empty_like(t) for t in mips]
+    p_irr = torch.empty_like(irr)
+    with torch.cuda.stream(stream):
+        pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pa.record(stream)
+        ibl.prefilter(chain, ENV_W, ENV_H, p_mips, rough, SAMPLES, ibl.GEN_HAMMERSLEY, stream)
+        ibl.irradiance(chain, ENV_W, ENV_H, p_irr, None, stream)
+        pb.record(stream)
+    stream.synchronize()
+    plain_ms = pa.elapsed_time(pb)
+    errs = error_table(env, {"tensor": tc_outs, "plain": [t.cpu().numpy() for t in p_mips]},
+                       {"tensor": tc_irr, "plain": p_irr.cpu().numpy()})
+    peaks = {}
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        peaks = json.load(open(p))
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    flops = tc_algorithmic_flops(levels, irr_level)
+    achieved = flops / (tc_ms / 1e3) / 1e12
+    h2d = host_env.numel() * 4
+    d2h = sum(t.numel() * 4 for t in h_outs)
+    line = {"metric": METRIC, "value": 1e3 / step_ms, "unit": "probes/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 hi/lo (fp32 accumulate, fp64 normalisation)",
+            "data": f"synthetic (sky x log-normal noise + 8 suns <= {args.sun_max:g})",
+            "config": {"workload": "precision: 4096x2048 env, 9-mip GGX chain from 2048x1024 "
+                                   "(roughness m/8), 128x64 irradiance, 512x512 LUT; mips 1-8 "
+                                   "and irradiance as tcgen05 contractions, mip 0 plain",
+                       "path": "tensor", "source_levels": levels, "irradiance_level": irr_level,
+                       "stage_ms": {"contraction": tc_ms},
+                       "plain_same_map_ms_prefilter_irradiance": plain_ms,
+                       "max_rel_err_vs_fp64": {"tensor": errs["tensor"]["max"],
+                                               "plain_N1024": errs["plain"]["max"]},
+                       "errors_per_mip_max_mean": errs,
+                       "l2": "flushed (256 MB write) between timed steps"},
+            "e2e": {"value": 1e3 / e2e_ms, "unit": "probes/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                         "kernel": "contract_kernel (all contractions of one bake)",
+                         "algorithmic_flops_per_bake": flops},
+            "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def batch_specs(n, seed=0):
     """256-probe batch configuration: widths uniform over {256, 512, 1024,
     2048} (2:1 maps), log2(W)-3 mips from W/2, 32x16 irradiance."""
@@ -502,6 +660,9 @@ def main():
                     help="probe: one 4096x2048 bake per step (default); batch: many probes; "
                          "serve: Poisson request stream against the server")
     ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--path", default="plain", choices=["plain", "tc"],
+                    help="probe workload: plain estimator or tensor-core precision path")
+    ap.add_argument("--sun-max", type=float, default=1e6, help="precision path sun radiance")
     ap.add_argument("--rates", type=float, nargs="+", default=[50, 200, 500, 1000, 2000])
     ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--seconds", type=float, default=4.0, help="per-rate cap on arrival time")
@@ -517,6 +678,8 @@ def main():
         return run_batch(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.path == "tc":
+        return run_tc(args)
     return run_ours(args)
 
 
