@@ -312,6 +312,16 @@ double althea_ibl_server_now(void);   /* the steady clock used in completions */
 /* Waits for everything in flight, then releases all device memory. */
 int althea_ibl_server_destroy(althea_ibl_server* s);
 
+/* ---- Radiance .hdr (RGBE) files: the bake cache format ---------------------
+ * Replaces Utilities::loadHdri / saveHdri (Src/Utilities.cpp:216-255, stb) as
+ * used by the bake cache (Src/ImageBasedLighting.cpp:58-102,429-446,483-568).
+ * Host memory, RGBA32F with alpha 1, row 0 = first scanline.  read allocates
+ * *rgba_out (free it with althea_ibl_hdr_free); write run-length encodes
+ * scanlines 8..32767 wide. */
+int althea_ibl_hdr_read(const char* path, float** rgba_out, int* width, int* height);
+void althea_ibl_hdr_free(float* rgba);
+int althea_ibl_hdr_write(const char* path, const float* rgba, int width, int height);
+
 const char* althea_ibl_last_error(void);
 int althea_ibl_abi_version(void);
 

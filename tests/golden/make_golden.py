@@ -12,6 +12,8 @@ reference next to it; the fixtures themselves travel, the reference does not).
   with a from-spec PNG reader, red/green channels subsampled every 5th texel.
 * ``prefiltered_hdr_headers.npz`` -- width/height/format of the reference's
   shipped Content/PrecomputedMaps/*/Prefiltered{2..5}.hdr (RGBE).
+* ``ref_LuxuryRoom_Prefiltered5.hdr`` -- one of those files, copied as is
+  (25 KB), for the run-length RGBE reader.
 
 Usage: python tests/golden/make_golden.py
 """
@@ -152,8 +154,16 @@ def hdr_fixture():
                         fmt=np.array([r[4] for r in rows]), magic=np.array([r[5] for r in rows]))
 
 
+def hdr_file_fixture():
+    """One shipped reference output (128x64, run-length RGBE) for the reader."""
+    import shutil
+    src = os.path.join(REF, "Content", "PrecomputedMaps", "LuxuryRoom", "Prefiltered5.hdr")
+    shutil.copyfile(src, os.path.join(HERE, "ref_LuxuryRoom_Prefiltered5.hdr"))
+
+
 if __name__ == "__main__":
     ref_shader_fixture()
     lut_fixture()
     hdr_fixture()
+    hdr_file_fixture()
     print("fixtures written to", HERE)
