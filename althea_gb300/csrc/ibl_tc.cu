@@ -12,27 +12,45 @@
 // table so the result stays within 1e-3 of the same sum over level 0.
 //
 // Structure.  On an equirect map the weight of output texel (i, x) for source
-// texel (j, y) depends only on (i, j, d = y - s*x) with s = W_src / W_out:
-// c = cos p_i cos q_j cos(2 pi (d + 0.5) / W_src) + sin p_i sin q_j.  Splitting
-// the source row into s polyphase rows L_{j,ph}[t] = L_j[s t + ph] gives
-//   out[i, x] = sum_{j, ph, k} w_ij(s k + ph) * L_{j,ph}[x + k]
-// -- a GEMM with M = 128 output rows i (TMEM lanes), N = output columns and
-// K = (j, ph, k).  A CTA owns the columns x = x_ph + 8 n of one residue x_ph;
-// then B[n, k] = L_{j,ph}[x_ph + 8 n + k] is a Hankel matrix whose rows start
-// 16 bytes apart, which the K-major no-swizzle UMMA layout expresses directly
-// (core-matrix row pitch 16 B, LBO = 16 B along K, SBO = 128 B along N), so
-// the radiance operand is read straight from a staged row buffer.  The weight
-// operand A[i, k] is generated on the CUDA cores into shared memory.
+// texel (j, y) depends only on (i, j, d = y - s*x), s = W_src / W_out, through
+// c = cos p_i cos q_j cos(2 pi (d + 0.5) / W_src) + sin p_i sin q_j.  Pick a
+// phase count g and a column step m with 8 g = s m (g = 1, m = 8/s for s <= 8;
+// g = s/8, m = 1 for s >= 8) and split each source row into g phase rows
+// P_ph[u] = L_j[g u + ph] (length krow = ws / g).  For the output columns
+// x = x0 + m (n0 + n):
+//   out[i, x] = sum_{j, ph, k} A[i, (j, ph, k)] * B[(j, ph, k), n],
+//   A = w_ij(g ((k - (s/g) x0) mod krow) + ph),  B[k, n] = P_ph[(8 n + k + 8 n0) mod krow],
+// a GEMM with M = 128 output rows (TMEM lanes), N = up to 128 columns n and
+// K = (j, ph, k).  B is a Hankel matrix (rows 8 elements = 16 bytes apart),
+// which the K-major no-swizzle UMMA layout expresses directly (LBO = 16 B,
+// SBO = 128 B): the radiance operand is read straight from a staged row.
+// The column residue x0 shifts the weights, not the row, so every staged row
+// is the phase row rotated by a multiple of 16 bytes: TMA bulk copies.
+//
+// Kernel (warp-specialised, one CTA per SM, 736 threads):
+//   warps 0-15  weight producers: generate A (hi and lo BF16) for one K = 32
+//               stage and write it straight into TMEM with tcgen05.st (four
+//               stages in flight), so no shared-memory bandwidth goes to A;
+//   warps 16-21 one thread each issues the MMAs of one colour channel and one
+//               half of the columns (A from TMEM, B from shared memory; one
+//               channel per thread when N < 32).  A single issuing thread
+//               cannot keep the tensor core busy: on sm_103a one thread issues
+//               a tcgen05.mma about every 64 cycles, while an N = 64 MMA
+//               executes in 32;
+//   warp 22     one thread stages the Hankel radiance rows with TMA bulk
+//               copies (up to four slots in flight).
+// Each CTA owns at most kMaxK = 8192 of K (the source rows are split over the
+// grid to guarantee it), so each accumulator is one tensor-core FP32
+// accumulation chain of bounded length; the producer warps move it to the
+// partial sums at the end.  All hand-offs are mbarriers; every wait is bounded by the
+// global timer and an abort flag, after which the kernel records an error,
+// waits (bounded) for its own MMAs and copies, frees its TMEM and returns.
 //
 // Precision.  Radiance and weights are each split x = hi + lo (hi = bf16(x),
 // lo = bf16(x - hi)); three MMAs per channel (hi*hi + hi*lo + lo*hi) give
-// products to ~2^-17 relative; sums of positive terms accumulate in FP32
-// TMEM.  BF16 shares FP32's exponent range, so 1e6-bright suns need no
-// per-tile scaling.  The weight sum is taken in FP64 per output row (it does
-// not depend on x).
-//
-// Safety.  Every mbarrier wait is bounded; on timeout the kernel records an
-// error flag, waits (bounded) for its own MMAs, frees its TMEM and returns.
+// products to ~2^-17 relative.  BF16 shares FP32's exponent range, so
+// 1e6-bright suns need no scaling.  The weight sum of each output row is
+// taken in FP64 (FP32 within one source phase row) by the producers.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -48,15 +66,24 @@
 namespace ibl {
 namespace tc {
 
-constexpr int kM = 128;          // output rows per CTA (TMEM lanes)
-constexpr int kKStep = 64;       // K per pipeline step (4 MMA instructions)
-constexpr int kThreads = 256;   // direct kernel
-constexpr int kHThreads = 512;  // Hankel kernel
-constexpr int kDrain = 128;     // MMA steps per TMEM accumulation chain
-
-
-constexpr long long kSpinLimit = 1LL << 26;
+constexpr int kM = 128;           // output rows per CTA (TMEM lanes)
+constexpr int kKS = 32;           // K per pipeline stage (two K = 16 MMAs)
+constexpr int kStages = 4;        // A stages in TMEM
+constexpr int kNBMax = 128;       // MMA N (columns) per CTA
+constexpr int kACol = 3 * kNBMax; // first A stage column (accumulators before it)
+constexpr int kTmemCols = 512;
+constexpr int kProducerWarps = 16;  // four per TMEM lane quarter, 8 K each per stage
+constexpr int kMmaWarp0 = 16;       // MMA issuers: (colour channel, column half)
+constexpr int kMmaWarps = 6;
+constexpr int kLoaderWarp = 22;
+constexpr int kThreads = 32 * (kLoaderWarp + 1);
+static_assert(kMmaWarp0 == kProducerWarps && kLoaderWarp == kMmaWarp0 + kMmaWarps, "warp roles");
+static_assert(kACol + kStages * kKS <= kTmemCols, "TMEM columns");
+constexpr int kMaxSlots = 4;      // staged radiance rows in flight
+constexpr int kMaxK = 8192;       // K per CTA: one TMEM accumulation chain
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr float kPiF = 3.14159265358979f;
+constexpr int kSmemLimit = 232448;  // opt-in shared memory per block
 
 // ---- PTX wrappers -------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -65,6 +92,27 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Global -> shared bulk copy (16-byte aligned addresses, size a multiple of
+// 16), completion counted on the mbarrier's transaction count.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
@@ -78,11 +126,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait; returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long i = 0; i < kSpinLimit; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: false when the abort flag is up or after kWaitNs (which
+// raises the flag so every other role stops too).
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    for (int i = 0; i < 64; ++i)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+    if (global_ns() - t0 > kWaitNs) {
+      *abort = 1;
+      return false;
+    }
+  }
 }
 
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
@@ -105,12 +168,13 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
          ((uint32_t)(m >> 4) << 24);    // M / 16
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t accumulate) {
+// D (TMEM) += A (TMEM) * B (shared memory).
+__device__ __forceinline__ void mma_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t b,
+                                       uint32_t idesc, uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "r"(tmem_a), "l"(b), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -130,6 +194,16 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, const uint32_t* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr),
+               "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3])
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
   asm volatile(
@@ -146,86 +220,89 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 
 // ---- job description --------------------------------------------------------------
 struct Job {
-  const __nv_bfloat16* planes;  // 6 planes [ch*2 + hl][H_s][W_s] of the source level
-  int ws, hs;                   // source level size
-  int wo, ho;                   // output size
-  int s;                        // ws / wo (power of two >= 1)
-  int kind;                     // 0 = GGX prefilter, 1 = irradiance
-  float a2;                     // roughness^2
-  int n_mma;                    // N of the MMA (multiple of 16, >= ceil(wo/8))
-  int kpad;                     // polyphase row length padded to a multiple of 16
-  int ksplit;                   // source rows are split over this many CTAs
-  int tmem_cols;                // power of two >= 3 * n_mma (channel c at column c * n_mma)
-  int direct;                   // 1: direct kernel (M = output texels, N = radiance planes)
-  const float* cos_d;           // [ws]  cos(2 pi (d + 0.5) / ws)
-  const float* src_rows;        // [hs][3]  cos q, sin q, Omega
-  const float* out_rows;        // [ho][2]  cos p, sin p
-  const float* src_cols;        // [ws][2]  cos, sin of source column yaw (direct kernel)
-  const float* out_cols;        // [wo][2]  cos, sin of output column yaw (direct kernel)
-  float* partial;               // [ksplit][ho][3][wo]
-  double* wsum_part;            // [ksplit][ho*wo] weight sums (direct kernel)
-  int* error;                   // set on a bounded-wait timeout
+  const __nv_bfloat16* src;  // 6 planes (R hi, R lo, G hi, G lo, B hi, B lo) as
+                             // [plane][hs][g][krow] (g = 1: the level itself)
+  int ws, hs;                // source level size
+  int wo, ho;                // output size
+  int s, g, m;               // s = ws / wo; 8 g = s m
+  int krow, kpad;            // phase row length ws / g, padded to a multiple of kKS
+  int nres, nb, nblk;        // columns per residue x0, MMA N, column blocks per residue
+  int rlen;                  // staged row length (bf16 elements, multiple of 8)
+  int nslots;                // staged rows in flight (2..kMaxSlots)
+  int nsplit;                // MMA issuers per channel (column halves): 2 when nb % 32 == 0
+  int kind;                  // 0 = GGX prefilter, 1 = irradiance
+  float a2;                  // roughness^2
+  int ksplit;                // source rows are split over this many CTAs
+  const float* cos_d;        // [ws]  cos(2 pi (d + 0.5) / ws)
+  const float* src_rows;     // [hs][3]  cos q, sin q, Omega
+  const float* out_rows;     // [ho][2]  cos p, sin p
+  float* partial;            // [ksplit][3][wo][ho]
+  double* wsum_part;         // [ksplit][ho]  (kind 0)
+  int* error;                // set when a bounded wait gave up
 };
 
-// Weight for cos-angle c (see the file comment).
-__device__ __forceinline__ float weight_of(float c, float a2, int kind) {
-  if (!(c > 0.0f)) return 0.0f;
-  if (kind == 1) return c;
-  float nh2 = 0.5f * (1.0f + c);
-  float den = fmaf(nh2, a2 - 1.0f, 1.0f);
-  return __fdividef(a2, kPiF * den * den) * c;
+struct SmemPlan {
+  size_t slots, cosd, total;
+};
+
+__host__ __device__ inline SmemPlan smem_plan(const Job& J) {
+  SmemPlan p;
+  p.slots = 0;
+  p.cosd = p.slots + (size_t)J.nslots * 6 * J.rlen * 2;
+  p.total = p.cosd + (size_t)J.g * J.kpad * 4;
+  return p;
 }
 
-// Shared-memory plan of the contraction kernel (bytes).
-struct Smem {
-  static constexpr int kA = kM * kKStep * 2;            // one bf16 A tile (16 KB)
-  static constexpr int kAStages = 2;
-  static constexpr int kRowSlots = 2;
-  __host__ __device__ static int row_len(int n_mma, int kpad) {
-    return ((8 * n_mma + kpad + 7) / 8) * 8;            // bf16 elements per staged row
-  }
-};
-
-// The contraction kernel (Hankel form).  Grid: (ceil(ho/128), 8 x residues,
-// ksplit); 512 threads generate weights, thread 0 issues the MMAs.  Every
-// kDrain steps the TMEM accumulators are drained into the CTA's FP32 partial
-// sums (IEEE round-to-nearest adds) and restarted, which keeps the tensor
-// core's accumulation chains short.
-__global__ void __launch_bounds__(kHThreads, 1) contract_kernel(const Job job) {
+// The contraction kernel.  Grid: (ceil(ho/128), m * nblk, ksplit); each CTA
+// sums at most kMaxK of K in one TMEM accumulation chain per channel.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t mbar[2];
+  __shared__ uint64_t a_full[kStages], a_empty[kStages];
+  __shared__ uint64_t slot_full[kMaxSlots], slot_empty[kMaxSlots];
+  __shared__ uint64_t done_bar;
   __shared__ uint32_t tmem_base_sh;
-  __shared__ float rowc[kM], rows[kM];
-  __shared__ int abort_flag;
+  __shared__ int abort_sh;
+  __shared__ double wsum_sh[kProducerWarps / 4][kM];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int i0 = blockIdx.x * kM;
-  const int xph = blockIdx.y;
+  const int x0 = blockIdx.y / job.nblk;
+  const int n0 = (blockIdx.y - x0 * job.nblk) * job.nb;
   const int split = blockIdx.z;
-  const int rlen = Smem::row_len(job.n_mma, job.kpad);
-  // layout: A stages [2][hi,lo] | row slots [2][6 planes][rlen] | cos_d[ws]
-  unsigned char* a_base = smem;
-  __nv_bfloat16* rows_base =
-      reinterpret_cast<__nv_bfloat16*>(smem + Smem::kAStages * 2 * Smem::kA);
-  float* cosd = reinterpret_cast<float*>(
-      smem + Smem::kAStages * 2 * Smem::kA + Smem::kRowSlots * 6 * rlen * 2);
+  const SmemPlan sp = smem_plan(job);
+  __nv_bfloat16* slots = reinterpret_cast<__nv_bfloat16*>(smem + sp.slots);
+  float* cosd_sm = reinterpret_cast<float*>(smem + sp.cosd);
+  volatile int* abort_flag = &abort_sh;
 
   if (tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
-    abort_flag = 0;
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&a_full[s], kProducerWarps);
+      mbar_init(&a_empty[s], 3 * job.nsplit);
+    }
+    for (int s = 0; s < kMaxSlots; ++s) {
+      mbar_init(&slot_full[s], 1);
+      mbar_init(&slot_empty[s], 3 * job.nsplit);
+    }
+    mbar_init(&done_bar, 3 * job.nsplit);
+    abort_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int i = tid; i < kM; i += kHThreads) {
-    int gi = i0 + i;
-    rowc[i] = gi < job.ho ? job.out_rows[2 * gi] : 0.0f;
-    rows[i] = gi < job.ho ? job.out_rows[2 * gi + 1] : 0.0f;
+  // cos of the column offsets in phase order, shifted by this CTA's column
+  // residue: cosd_sm[ph][k] = cos_d[g ((k - (s/g) x0) mod krow) + ph]
+  {
+    const int sh = (job.s / job.g) * x0 % job.krow;
+    for (int e = tid; e < job.g * job.kpad; e += kThreads) {
+      int ph = e / job.kpad, k = e - ph * job.kpad;
+      int kk = k - sh;
+      if (kk < 0) kk += job.krow;
+      cosd_sm[e] = k < job.krow ? job.cos_d[job.g * kk + ph] : 0.0f;
+    }
   }
-  for (int d = tid; d < job.ws; d += kHThreads) cosd[d] = job.cos_d[d];
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base_sh)),
-                 "r"((uint32_t)job.tmem_cols));
+                 "r"((uint32_t)kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -233,402 +310,253 @@ __global__ void __launch_bounds__(kHThreads, 1) contract_kernel(const Job job) {
   tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
 
-  // Source rows of this split.
   const int j_per = (job.hs + job.ksplit - 1) / job.ksplit;
   const int j0 = split * j_per;
   const int j1 = min(job.hs, j0 + j_per);
-  const int wo_ph = job.wo;            // polyphase row length = ws / s = wo
-  const int ksteps_row = (job.kpad + kKStep - 1) / kKStep;
-  const long long total_steps =
-      (j1 > j0 ? (long long)(j1 - j0) : 0LL) * job.s * ksteps_row;
-  const uint32_t idesc = idesc_bf16(kM, job.n_mma);
-  const int gi_row = tid >> 2;           // weight row 0..127
-  const int kk0 = (tid & 3) * 16;        // 16 consecutive k per thread
-  const bool row_ok = i0 + gi_row < job.ho;
-  const float cp = rowc[gi_row], sp = rows[gi_row];
-  const int out_i = i0 + warp * 32 + lane;   // TMEM lane owned in a drain (warps 0-3)
-  bool first_drain = true;
+  const int nrows = j1 > j0 ? j1 - j0 : 0;
+  const int kchunks = job.kpad / kKS;
+  const long long total = (long long)nrows * job.g * kchunks;
+  const bool want_wsum = KIND == 0 && blockIdx.y == 0;
 
-  long long step = 0;
-  bool ok = true;
-  bool fresh = true;  // the next MMA of each channel overwrites the accumulator
-  for (int j = j0; j < j1 && ok; ++j) {
-    const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
-    const float om = job.src_rows[3 * j + 2];
-    const float ccq = cp * cq, ssq = sp * sq;
-    for (int ph = 0; ph < job.s && ok; ++ph) {
-      for (int kc = 0; kc < ksteps_row && ok; ++kc, ++step) {
-        const int stage = (int)(step & 1);
-        // (1) the MMAs of step - 2 read this stage's A tile and (on a row
-        // start) this slot's row buffers: wait for them.
-        if (step >= 2) {
-          if (!mbar_wait(&mbar[stage], (uint32_t)(((step - 2) >> 1) & 1))) {
-            if (tid == 0) abort_flag = 1;
+  if (warp < kProducerWarps) {
+    // ---- weight producers: rows 32q + lane, K sub-range [8h, 8h + 8) of each stage
+    const int q = warp & 3, h = warp >> 2;
+    const int row = 32 * q + lane, gi = i0 + row;
+    const bool live = i0 + 32 * q < job.ho;
+    float cp = 0.0f, sp_ = 0.0f;
+    if (gi < job.ho) {
+      cp = job.out_rows[2 * gi];
+      sp_ = job.out_rows[2 * gi + 1];
+    }
+    const float a2 = job.a2;
+    const float alpha = 0.5f * (1.0f + a2), beta = 0.5f * (a2 - 1.0f), ka = a2 / kPiF;
+    const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    double wacc = 0.0;
+    long long gidx = 0;
+    int pending = -1;  // stage whose stores are issued but not yet published
+    bool ok = true;
+    for (int j = j0; j < j1 && ok; ++j) {
+      const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
+      const float om = job.src_rows[3 * j + 2];
+      const float ccq = cp * cq, ssq = sp_ * sq;
+      const float k1 = KIND == 0 ? ka * om : om;
+      for (int ph = 0; ph < job.g && ok; ++ph) {
+        const float* cdrow = cosd_sm + ph * job.kpad;
+        float rowsum = 0.0f;
+        for (int kc = 0; kc < kchunks; ++kc, ++gidx) {
+          const int st = (int)(gidx & (kStages - 1));
+          const long long use = gidx / kStages;
+          uint32_t hw[4], lw[4];
+          if (live) {
+            const int kb = kc * kKS + 8 * h;
+            float w[8];
+#pragma unroll
+            for (int e = 0; e < 8; e += 4) {
+              const float4 cd = *reinterpret_cast<const float4*>(cdrow + kb + e);
+              const float cs[4] = {cd.x, cd.y, cd.z, cd.w};
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                const float c = fmaf(ccq, cs[u], ssq);
+                float v;
+                if (KIND == 0) {
+                  const float den = fmaf(c, beta, alpha);
+                  v = __fdividef(k1 * c, den * den);
+                } else {
+                  v = k1 * c;
+                }
+                w[e + u] = fmaxf(v, 0.0f);
+              }
+            }
+            if (kb + 8 > job.krow) {
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                if (kb + u >= job.krow) w[u] = 0.0f;
+            }
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const __nv_bfloat162 h2 = __floats2bfloat162_rn(w[2 * e], w[2 * e + 1]);
+              const float2 hf = __bfloat1622float2(h2);
+              const __nv_bfloat162 l2 =
+                  __floats2bfloat162_rn(w[2 * e] - hf.x, w[2 * e + 1] - hf.y);
+              hw[e] = *reinterpret_cast<const uint32_t*>(&h2);
+              lw[e] = *reinterpret_cast<const uint32_t*>(&l2);
+            }
+            if (want_wsum) {
+#pragma unroll
+              for (int u = 0; u < 8; ++u) rowsum += w[u];
+            }
+          }
+          // Software pipeline: the previous stage's TMEM stores landed while
+          // this stage's weights were computed; publish that stage now.
+          if (pending >= 0) {
+            if (live) tmem_wait_st();
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&a_full[pending]);
+            pending = -1;
+          }
+          if (use >= 1 && !wait_bar(&a_empty[st], (uint32_t)((use - 1) & 1), abort_flag)) {
+            ok = false;
+            break;
+          }
+          if (live) {
+            const uint32_t col = (uint32_t)(kACol + st * kKS + 4 * h);
+            tmem_st4(lane_base + col, hw);
+            tmem_st4(lane_base + col + 16, lw);
+          }
+          pending = st;
+        }
+        wacc += (double)rowsum;
+      }
+    }
+    if (live) tmem_wait_st();
+    if (pending >= 0) {
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&a_full[pending]);
+    }
+    wsum_sh[h][row] = wacc;
+  } else if (warp < kMmaWarp0 + kMmaWarps) {
+    // ---- MMA issuers: one thread per (colour channel, column half) --------------
+    const int u = warp - kMmaWarp0;
+    const int ch = u / job.nsplit, hf = u - ch * job.nsplit;
+    if (lane == 0 && total > 0 && u < 3 * job.nsplit) {
+      const int nm = job.nb / job.nsplit;
+      const uint32_t idesc = idesc_bf16(kM, nm);
+      // B descriptors differ only in the start-address field (16-byte units;
+      // every staged address stays below 2^18 bytes, so no carry out of it).
+      const uint64_t bdesc0 = smem_desc(smem_u32(slots), 16, 128);
+      const uint32_t r8 = (uint32_t)(job.rlen >> 3);
+      const uint32_t d = tmem + (uint32_t)(ch * job.nb + hf * nm);
+      // this issuer's hi plane rows within a slot, in 16-byte units
+      const uint32_t plane16 = 2u * (uint32_t)ch * r8 + (uint32_t)(hf * nm);
+      const uint32_t slot16 = 6u * r8;
+      uint32_t gidx = 0, row_id = 0;
+      bool ok = true;
+      for (int j = j0; j < j1 && ok; ++j) {
+        for (int ph = 0; ph < job.g && ok; ++ph, ++row_id) {
+          const uint32_t slot = row_id % (uint32_t)job.nslots;
+          if (!wait_bar(&slot_full[slot], (row_id / (uint32_t)job.nslots) & 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          uint64_t dbh = bdesc0 + (uint64_t)(slot * slot16 + plane16);
+          for (int kc = 0; kc < kchunks; ++kc, ++gidx, dbh += kKS * 2 / 16) {
+            const uint32_t st = gidx & (kStages - 1);
+            if (!wait_bar(&a_full[st], (gidx / kStages) & 1u, abort_flag)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t a_hi = tmem + (uint32_t)kACol + st * kKS;
+            const uint32_t acc0 = gidx != 0;
+            mma_ts(d, a_hi, dbh, idesc, acc0);
+            mma_ts(d, a_hi, dbh + r8, idesc, 1u);
+            mma_ts(d, a_hi + 16, dbh, idesc, 1u);
+            mma_ts(d, a_hi + 8, dbh + 2, idesc, 1u);
+            mma_ts(d, a_hi + 8, dbh + 2 + r8, idesc, 1u);
+            mma_ts(d, a_hi + 24, dbh + 2, idesc, 1u);
+            mma_commit(&a_empty[st]);
+            if (kc == kchunks - 1) mma_commit(&slot_empty[slot]);
           }
         }
-        __syncthreads();
-        if (abort_flag) {
+      }
+      // every MMA issued by all issuers has completed before the accumulators
+      // are read and TMEM is released
+      mma_commit(&done_bar);
+      const unsigned long long t0 = global_ns();
+      while (!mbar_try_wait(&done_bar, 0u))
+        if (global_ns() - t0 > kWaitNs) {
+          *abort_flag = 1;
+          break;
+        }
+    }
+  } else if (lane == 0) {
+    // ---- Hankel row loader: slot[p][t] = P_ph[(t + 8 n0) mod krow], t < rlen ----
+    const int u0 = (8 * n0) % job.krow;
+    long long row_id = 0;
+    bool ok = true;
+    for (int j = j0; j < j1 && ok; ++j) {
+      for (int ph = 0; ph < job.g && ok; ++ph, ++row_id) {
+        const int slot = (int)(row_id % job.nslots);
+        const long long use = row_id / job.nslots;
+        if (use >= 1 &&
+            !wait_bar(&slot_empty[slot], (uint32_t)((use - 1) & 1), abort_flag)) {
           ok = false;
           break;
         }
-        const long long row_id = (long long)(j - j0) * job.s + ph;
-        const int slot = (int)(row_id & 1);
-        __nv_bfloat16* slot_base = rows_base + (size_t)slot * 6 * rlen;
-        // (2) stage the polyphase row (x residue folded in) on a row start:
-        // buf[t] = plane[j][(s * (t + xph) + ph) mod ws].
-        if (kc == 0) {
-          for (int e = tid; e < 6 * rlen; e += kHThreads) {
-            int p = e / rlen, t = e - p * rlen;
-            unsigned src = ((unsigned)job.s * (unsigned)(t + xph) + (unsigned)ph) % (unsigned)job.ws;
-            slot_base[e] = job.planes[((size_t)p * job.hs + j) * job.ws + src];
+        __nv_bfloat16* dst = slots + (size_t)slot * 6 * job.rlen;
+        mbar_expect_tx(&slot_full[slot], (uint32_t)(6 * job.rlen * 2));
+        for (int p = 0; p < 6; ++p) {
+          const __nv_bfloat16* srcrow =
+              job.src + (((size_t)p * job.hs + j) * job.g + ph) * job.krow;
+          int t = 0, u = u0;
+          while (t < job.rlen) {
+            const int len = min(job.krow - u, job.rlen - t);
+            bulk_g2s(dst + (size_t)p * job.rlen + t, srcrow + u, (uint32_t)(len * 2),
+                     &slot_full[slot]);
+            t += len;
+            u = 0;
           }
-        }
-        // (3) weights of this step into A[stage] (hi, lo), K-major no-swizzle:
-        // element (i, k) at (i/8)*1024 + (k/8)*128 + (i%8)*16 + (k%8)*2.
-        unsigned char* a_hi = a_base + stage * 2 * Smem::kA;
-        unsigned char* a_lo = a_hi + Smem::kA;
-#pragma unroll
-        for (int g = 0; g < 2; ++g) {
-          uint32_t hw[4], lw[4];
-#pragma unroll
-          for (int e = 0; e < 8; e += 2) {
-            float wv[2];
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-              int kl = kc * kKStep + kk0 + 8 * g + e + u;   // polyphase column
-              float w = 0.0f;
-              if (row_ok && kl < wo_ph) {
-                int d = job.s * kl + ph;                    // y - s*x
-                float c = fmaf(ccq, cosd[d], ssq);
-                w = weight_of(c, job.a2, job.kind) * om;
-              }
-              wv[u] = w;
-            }
-            __nv_bfloat162 h2 = __floats2bfloat162_rn(wv[0], wv[1]);
-            float2 hf = __bfloat1622float2(h2);
-            __nv_bfloat162 l2 = __floats2bfloat162_rn(wv[0] - hf.x, wv[1] - hf.y);
-            hw[e / 2] = *reinterpret_cast<uint32_t*>(&h2);
-            lw[e / 2] = *reinterpret_cast<uint32_t*>(&l2);
-          }
-          const int kk = kk0 + 8 * g;
-          const int off = (gi_row >> 3) * 1024 + (kk >> 3) * 128 + (gi_row & 7) * 16;
-          *reinterpret_cast<uint4*>(a_hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-          *reinterpret_cast<uint4*>(a_lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-        }
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        // (4) one thread issues the MMAs of this step and commits.
-        if (tid == 0) {
-          tc_fence_after();
-          const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
-          const int kmax = min(kKStep, job.kpad - kc * kKStep);
-          for (int q = 0; q < kmax / 16; ++q) {
-            const uint64_t da_hi = smem_desc(ah + q * 256, 128, 1024);
-            const uint64_t da_lo = smem_desc(al + q * 256, 128, 1024);
-            const uint32_t first = (fresh && q == 0) ? 0u : 1u;
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-              const uint32_t bh = smem_u32(slot_base + (size_t)(2 * ch) * rlen) +
-                                  2u * (uint32_t)(kc * kKStep + q * 16);
-              const uint32_t bl = smem_u32(slot_base + (size_t)(2 * ch + 1) * rlen) +
-                                  2u * (uint32_t)(kc * kKStep + q * 16);
-              const uint64_t db_hi = smem_desc(bh, 16, 128);
-              const uint64_t db_lo = smem_desc(bl, 16, 128);
-              const uint32_t d = tmem + (uint32_t)(ch * job.n_mma);
-              mma_bf16(d, da_hi, db_hi, idesc, first);
-              mma_bf16(d, da_hi, db_lo, idesc, 1u);
-              mma_bf16(d, da_lo, db_hi, idesc, 1u);
-            }
-          }
-          mma_commit(&mbar[stage]);
-        }
-        fresh = false;
-        // (5) drain the accumulators every kDrain steps and after the last.
-        if ((step + 1) % kDrain == 0 || step + 1 == total_steps) {
-          if (!mbar_wait(&mbar[stage], (uint32_t)((step >> 1) & 1))) {
-            if (tid == 0) abort_flag = 1;
-          }
-          tc_fence_after();
-          __syncthreads();
-          if (!abort_flag && warp < 4) {
-            for (int ch = 0; ch < 3; ++ch) {
-              for (int c0 = 0; c0 < job.n_mma; c0 += 16) {
-                float v[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) +
-                              (uint32_t)(ch * job.n_mma + c0), v);
-                if (out_i < job.ho) {
-#pragma unroll
-                  for (int u = 0; u < 16; ++u) {
-                    int x = xph + 8 * (c0 + u);
-                    if (x < job.wo) {
-                      float* pp =
-                          &job.partial[(((size_t)split * 3 + ch) * job.wo + x) * job.ho + out_i];
-                      *pp = first_drain ? v[u] : *pp + v[u];
-                    }
-                  }
-                }
-              }
-            }
-          }
-          first_drain = false;
-          fresh = true;
-          tc_fence_before();
-          __syncthreads();
         }
       }
     }
+    // After an abort, copies may still be in flight: they land before the CTA
+    // exits (in a normal run the MMA threads have already seen every fill).
+    for (long long r = row_id > job.nslots ? row_id - job.nslots : 0; r < row_id; ++r) {
+      const unsigned long long t0 = global_ns();
+      while (!mbar_try_wait(&slot_full[r % job.nslots], (uint32_t)((r / job.nslots) & 1)))
+        if (global_ns() - t0 > kWaitNs) break;
+    }
   }
-  // Make sure no MMA is in flight before TMEM is released.
-  const long long nsteps = step;
-  bool drained = true;
-  for (long long s2 = nsteps - 2; s2 < nsteps; ++s2) {
-    if (s2 < 0) continue;
-    if (!mbar_wait(&mbar[s2 & 1], (uint32_t)((s2 >> 1) & 1))) drained = false;
-  }
-  tc_fence_after();
+
+  tc_fence_before();
   __syncthreads();
-  if (!ok || !drained || abort_flag) {
+  tc_fence_after();
+  const bool failed = abort_sh != 0;
+  if (failed) {
     if (tid == 0) atomicExch(job.error, 1);
-  } else if (nsteps == 0 && warp < 4) {
-    if (out_i < job.ho)
-      for (int ch = 0; ch < 3; ++ch)
-        for (int x = xph; x < job.wo; x += 8)
-          job.partial[(((size_t)split * 3 + ch) * job.wo + x) * job.ho + out_i] = 0.0f;
+  } else {
+    const int q = warp & 3;
+    if (warp < kProducerWarps && i0 + 32 * q < job.ho) {
+      // accumulators -> partial sums (lane = output row, column = (channel, n));
+      // the four warps of a lane quarter take every fourth 16-column chunk
+      const int gi = i0 + 32 * q + lane;
+      for (int c0 = 16 * (warp >> 2); c0 < 3 * job.nb; c0 += 16 * (kProducerWarps / 4)) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int col = c0 + u, ch = col / job.nb, n = col - ch * job.nb;
+          const int x = x0 + job.m * (n0 + n);
+          if (gi < job.ho && n0 + n < job.nres && x < job.wo)
+            job.partial[(((size_t)split * 3 + ch) * job.wo + x) * job.ho + gi] =
+                total > 0 ? v[u] : 0.0f;
+        }
+      }
+    }
+    if (want_wsum && tid < kM && i0 + tid < job.ho) {
+      double ws = 0.0;
+      for (int hh = 0; hh < kProducerWarps / 4; ++hh) ws += wsum_sh[hh][tid];
+      job.wsum_part[(size_t)split * job.ho + i0 + tid] = ws;
+    }
   }
   tc_fence_before();
   __syncthreads();
+  tc_fence_after();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"((uint32_t)job.tmem_cols));
-}
-
-// Direct contraction for narrow outputs: M = 128 output texels (flattened),
-// N = 16 (the six hi/lo radiance planes, zero-padded), K = source texels.
-// Weights have no shift reuse here (each (output, source) pair is generated
-// once), so the CUDA cores bound it; it replaces the polyphase Hankel form
-// when a source row would split into many tiny polyphase rows.  Same
-// pipeline and bounded waits as contract_kernel; weight sums accumulate per
-// output texel in FP64.  Grid: (ceil(ho*wo/128), ksplit).
-__global__ void __launch_bounds__(kThreads, 2) contract_direct_kernel(const Job job) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t mbar[2];
-  __shared__ uint32_t tmem_base_sh;
-  __shared__ float dirx[kM], diry[kM], dirz[kM];
-  __shared__ double wsum_sh[kThreads];
-  __shared__ int abort_flag;
-  constexpr int kB = 16 * kKStep * 2;  // one bf16 B tile (2 KB)
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const long long o0 = (long long)blockIdx.x * kM;
-  const long long nout = (long long)job.ho * job.wo;
-  const int split = blockIdx.y;
-  unsigned char* a_base = smem;                         // [2 stages][hi, lo] 16 KB each
-  unsigned char* b_base = smem + 4 * (16 * 1024);       // [2 stages] 2 KB each
-  float* ccol = reinterpret_cast<float*>(b_base + 2 * kB);  // [ws][2]
-
-  if (tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
-    abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  for (int i = tid; i < kM; i += kThreads) {
-    long long o = o0 + i;
-    float x = 0.0f, y = 0.0f, z = 0.0f;
-    if (o < nout) {
-      int oi = (int)(o / job.wo), ox = (int)(o % job.wo);
-      float cp = job.out_rows[2 * oi], sp = job.out_rows[2 * oi + 1];
-      x = cp * job.out_cols[2 * ox];
-      y = sp;
-      z = cp * job.out_cols[2 * ox + 1];
-    }
-    dirx[i] = x;
-    diry[i] = y;
-    dirz[i] = z;
-  }
-  for (int d = tid; d < 2 * job.ws; d += kThreads) ccol[d] = job.src_cols[d];
-  // rows 6..15 of both B tiles stay zero
-  for (int e = tid; e < 2 * kB / 16; e += kThreads)
-    reinterpret_cast<uint4*>(b_base)[e] = make_uint4(0, 0, 0, 0);
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(&tmem_base_sh)),
-                 "r"((uint32_t)job.tmem_cols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = tmem_base_sh;
-  const int j_per = (job.hs + job.ksplit - 1) / job.ksplit;
-  const int j0 = split * j_per;
-  const int j1 = min(job.hs, j0 + j_per);
-  const int chunks = job.ws / kKStep;
-  const long long total_steps = (j1 > j0 ? (long long)(j1 - j0) : 0LL) * chunks;
-  const uint32_t idesc = idesc_bf16(kM, 16);
-  const int oi = tid >> 1, kk0 = (tid & 1) * 32;
-  const float nx = dirx[oi], ny = diry[oi], nz = dirz[oi];
-  double acc6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // drained sums (warps 0-3)
-  bool fresh = true;
-  double wacc = 0.0;
-
-  long long step = 0;
-  bool ok = true;
-  for (int j = j0; j < j1 && ok; ++j) {
-    const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
-    const float om = job.src_rows[3 * j + 2];
-    const float sny = sq * ny;
-    for (int ch = 0; ch < chunks && ok; ++ch, ++step) {
-      const int stage = (int)(step & 1);
-      if (step >= 2) {
-        if (!mbar_wait(&mbar[stage], (uint32_t)(((step - 2) >> 1) & 1))) {
-          if (tid == 0) abort_flag = 1;
-        }
-      }
-      __syncthreads();
-      if (abort_flag) {
-        ok = false;
-        break;
-      }
-      const int y0 = ch * kKStep;
-      unsigned char* bt = b_base + stage * kB;
-      if (tid < 48) {  // 6 planes x 8 chunks of 8 bf16
-        int p = tid >> 3, c8 = tid & 7;
-        const uint4* src = reinterpret_cast<const uint4*>(
-            job.planes + ((size_t)p * job.hs + j) * job.ws + y0 + 8 * c8);
-        *reinterpret_cast<uint4*>(bt + c8 * 128 + p * 16) = __ldg(src);
-      }
-      unsigned char* a_hi = a_base + stage * 2 * Smem::kA;
-      unsigned char* a_lo = a_hi + Smem::kA;
-      float wsum_step = 0.0f;
-#pragma unroll
-      for (int g = 0; g < 4; ++g) {
-        uint32_t hw[4], lw[4];
-#pragma unroll
-        for (int e = 0; e < 8; e += 2) {
-          float wv[2];
-#pragma unroll
-          for (int u = 0; u < 2; ++u) {
-            int y = y0 + kk0 + 8 * g + e + u;
-            float c = fmaf(cq, fmaf(nx, ccol[2 * y], nz * ccol[2 * y + 1]), sny);
-            float w = (o0 + oi < nout) ? weight_of(c, job.a2, job.kind) * om : 0.0f;
-            wv[u] = w;
-            wsum_step += w;
-          }
-          __nv_bfloat162 h2 = __floats2bfloat162_rn(wv[0], wv[1]);
-          float2 hf = __bfloat1622float2(h2);
-          __nv_bfloat162 l2 = __floats2bfloat162_rn(wv[0] - hf.x, wv[1] - hf.y);
-          hw[e / 2] = *reinterpret_cast<uint32_t*>(&h2);
-          lw[e / 2] = *reinterpret_cast<uint32_t*>(&l2);
-        }
-        const int kk = kk0 + 8 * g;
-        const int off = (oi >> 3) * 1024 + (kk >> 3) * 128 + (oi & 7) * 16;
-        *reinterpret_cast<uint4*>(a_hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-        *reinterpret_cast<uint4*>(a_lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-      }
-      wacc += (double)wsum_step;
-      fence_async_smem();
-      tc_fence_before();
-      __syncthreads();
-      if (tid == 0) {
-        tc_fence_after();
-        const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bb = smem_u32(bt);
-        for (int q = 0; q < kKStep / 16; ++q) {
-          const uint64_t da_hi = smem_desc(ah + q * 256, 128, 1024);
-          const uint64_t da_lo = smem_desc(al + q * 256, 128, 1024);
-          const uint64_t db = smem_desc(bb + q * 256, 128, 1024);
-          mma_bf16(tmem, da_hi, db, idesc, (fresh && q == 0) ? 0u : 1u);
-          mma_bf16(tmem, da_lo, db, idesc, 1u);
-        }
-        mma_commit(&mbar[stage]);
-      }
-      fresh = false;
-      // Drain the accumulator into FP64 registers every kDrain steps.
-      if ((step + 1) % kDrain == 0 || step + 1 == total_steps) {
-        if (!mbar_wait(&mbar[stage], (uint32_t)((step >> 1) & 1))) {
-          if (tid == 0) abort_flag = 1;
-        }
-        tc_fence_after();
-        __syncthreads();
-        if (!abort_flag && warp < 4) {
-          float v[16];
-          tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), v);
-#pragma unroll
-          for (int u = 0; u < 6; ++u) acc6[u] += (double)v[u];
-        }
-        fresh = true;
-        tc_fence_before();
-        __syncthreads();
-      }
-    }
-  }
-  const long long nsteps = step;
-  bool drained = true;
-  for (long long s2 = nsteps - 2; s2 < nsteps; ++s2) {
-    if (s2 < 0) continue;
-    if (!mbar_wait(&mbar[s2 & 1], (uint32_t)((s2 >> 1) & 1))) drained = false;
-  }
-  wsum_sh[tid] = wacc;
-  tc_fence_after();
-  __syncthreads();
-  if (!ok || !drained || abort_flag) {
-    if (tid == 0) atomicExch(job.error, 1);
-  } else if (warp < 4) {
-    const int i = warp * 32 + lane;
-    const long long o = o0 + i;
-    if (o < nout) {
-      float* pp = job.partial + ((size_t)split * nout + o) * 3;
-      pp[0] = (float)(acc6[0] + acc6[1]);
-      pp[1] = (float)(acc6[2] + acc6[3]);
-      pp[2] = (float)(acc6[4] + acc6[5]);
-      job.wsum_part[(size_t)split * nout + o] = wsum_sh[2 * i] + wsum_sh[2 * i + 1];
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"((uint32_t)job.tmem_cols));
-}
-
-__global__ void finish_direct_kernel(const Job job, float4* __restrict__ out, long long pitch) {
-  long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long nout = (long long)job.ho * job.wo;
-  if (o >= nout) return;
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0, w = 0.0;
-  for (int k = 0; k < job.ksplit; ++k) {
-    const float* p = job.partial + ((size_t)k * nout + o) * 3;
-    s0 += p[0];
-    s1 += p[1];
-    s2 += p[2];
-    w += job.wsum_part[(size_t)k * nout + o];
-  }
-  double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / w);
-  int x = (int)(o % job.wo), i = (int)(o / job.wo);
-  out[(long long)i * pitch + x] =
-      make_float4((float)(s0 * norm), (float)(s1 * norm), (float)(s2 * norm), 1.0f);
+                 "r"((uint32_t)kTmemCols));
 }
 
 // Direction tables in FP64, stored as FP32: cos of the column offsets
-// (2 pi (d + 0.5) / ws), source rows (cos q, sin q, solid angle), output
-// rows (cos p, sin p at texel corners), and for the direct kernel the source
-// and output column yaws (cos, sin).
-__global__ void tables_kernel(int ws, int hs, int ho, int wo, float* __restrict__ cosd,
-                              float* __restrict__ srows, float* __restrict__ orows,
-                              float* __restrict__ scols, float* __restrict__ ocols) {
+// (2 pi (d + 0.5) / ws), source rows (cos q, sin q, solid angle) and output
+// rows (cos p, sin p at texel corners).
+__global__ void tables_kernel(int ws, int hs, int ho, float* __restrict__ cosd,
+                              float* __restrict__ srows, float* __restrict__ orows) {
   const double pi = 3.14159265358979323846;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < ws) {
-    cosd[t] = (float)cos(2.0 * pi * (t + 0.5) / ws);
-    double yaw = pi * (2.0 * (t + 0.5) / ws - 1.0);
-    scols[2 * t] = (float)cos(yaw);
-    scols[2 * t + 1] = (float)sin(yaw);
-  }
-  if (t < wo) {
-    double yaw = pi * (2.0 * t / wo - 1.0);
-    ocols[2 * t] = (float)cos(yaw);
-    ocols[2 * t + 1] = (float)sin(yaw);
-  }
+  if (t < ws) cosd[t] = (float)cos(2.0 * pi * (t + 0.5) / ws);
   if (t < hs) {
     double q = pi * ((t + 0.5) / hs - 0.5);
     double q0 = pi * ((double)t / hs - 0.5), q1 = pi * ((double)(t + 1) / hs - 0.5);
@@ -643,64 +571,66 @@ __global__ void tables_kernel(int ws, int hs, int ho, int wo, float* __restrict_
   }
 }
 
-// RGBA32F source level -> 6 bf16 planes (R hi, R lo, G hi, G lo, B hi, B lo).
-__global__ void split_kernel(const float4* __restrict__ src, int n,
-                             __nv_bfloat16* __restrict__ planes) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  float4 v = src[t];
-  float c[3] = {v.x, v.y, v.z};
+// One RGBA32F source row -> 6 bf16 planes (R hi, R lo, G hi, G lo, B hi, B lo) in
+// phase order: out[plane][j][ph][u] = split(src[j][g u + ph]).  Block per
+// source row; the row is split into shared memory, then written out
+// contiguously.  Dynamic shared memory: 6 * ws bf16.
+__global__ void rows_kernel(const float4* __restrict__ src, int ws, int hs, int g,
+                           __nv_bfloat16* __restrict__ out) {
+  extern __shared__ __nv_bfloat16 row_sm[];
+  const int j = blockIdx.x;
+  for (int x = threadIdx.x; x < ws; x += blockDim.x) {
+    const float4 v = src[(size_t)j * ws + x];
+    const float c[3] = {v.x, v.y, v.z};
 #pragma unroll
-  for (int ch = 0; ch < 3; ++ch) {
-    __nv_bfloat16 h = __float2bfloat16_rn(c[ch]);
-    __nv_bfloat16 l = __float2bfloat16_rn(c[ch] - __bfloat162float(h));
-    planes[(size_t)(2 * ch) * n + t] = h;
-    planes[(size_t)(2 * ch + 1) * n + t] = l;
-  }
-}
-
-// FP64 weight sum per output row: sum_j sum_d w_ij(d) (FP32 terms, each
-// source row summed in FP32 by a warp, rows accumulated in FP64).
-__global__ void weight_sum_kernel(const Job job, double* __restrict__ wsum) {
-  const int i = blockIdx.x;
-  const float cp = job.out_rows[2 * i], sp = job.out_rows[2 * i + 1];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  __shared__ double part[32];
-  double acc = 0.0;
-  for (int j = warp; j < job.hs; j += nw) {
-    const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
-    const float om = job.src_rows[3 * j + 2];
-    const float ccq = cp * cq, ssq = sp * sq;
-    float s = 0.0f;
-    for (int d = lane; d < job.ws; d += 32) {
-      float c = fmaf(ccq, job.cos_d[d], ssq);
-      s += weight_of(c, job.a2, job.kind) * om;
+    for (int ch = 0; ch < 3; ++ch) {
+      const __nv_bfloat16 h = __float2bfloat16_rn(c[ch]);
+      row_sm[(2 * ch) * ws + x] = h;
+      row_sm[(2 * ch + 1) * ws + x] = __float2bfloat16_rn(c[ch] - __bfloat162float(h));
     }
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) acc += (double)s;
   }
-  if (lane == 0) part[warp] = acc;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < nw; ++w) t += part[w];
-    wsum[i] = t;
+  const int krow = ws / g;
+  for (int e = threadIdx.x; e < 6 * ws; e += blockDim.x) {
+    const int p = e / ws, t = e - p * ws;
+    const int ph = t / krow, u = t - ph * krow;
+    out[((size_t)p * hs + j) * ws + t] = row_sm[p * ws + g * u + ph];
   }
 }
 
-// Sum the K splits in order, normalise, write RGBA32F.
-__global__ void finish_kernel(const Job job, const double* __restrict__ wsum,
-                              float4* __restrict__ out, long long pitch) {
-  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= (long long)job.wo * job.ho) return;
-  int x = (int)(g % job.wo), i = (int)(g / job.wo);
-  double s[3] = {0.0, 0.0, 0.0};
-  for (int k = 0; k < job.ksplit; ++k)
-    for (int ch = 0; ch < 3; ++ch)
-      s[ch] += (double)job.partial[(((size_t)k * 3 + ch) * job.wo + x) * job.ho + i];
-  double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / wsum[i]);
-  out[(long long)i * pitch + x] =
-      make_float4((float)(s[0] * norm), (float)(s[1] * norm), (float)(s[2] * norm), 1.0f);
+// Sum the K splits (FP64, fixed order), normalise, write RGBA32F.  Block per
+// (32 output rows, one column); warp w sums the splits k = w mod 8 with the
+// lanes on consecutive rows (the partial layout), then warp 0 combines.
+__global__ void __launch_bounds__(256) finish_kernel(const Job job, float4* __restrict__ out,
+                                                     long long pitch) {
+  __shared__ double red[8][4][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane, x = blockIdx.y;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, sw = 0.0;
+  if (i < job.ho) {
+    for (int k = w; k < job.ksplit; k += 8) {
+      const float* p = job.partial + (((size_t)k * 3) * job.wo + x) * job.ho + i;
+      const size_t plane = (size_t)job.wo * job.ho;
+      s0 += (double)p[0];
+      s1 += (double)p[plane];
+      s2 += (double)p[2 * plane];
+      if (job.kind == 0) sw += job.wsum_part[(size_t)k * job.ho + i];
+    }
+  }
+  red[w][0][lane] = s0;
+  red[w][1][lane] = s1;
+  red[w][2][lane] = s2;
+  red[w][3][lane] = sw;
+  __syncthreads();
+  if (w == 0 && i < job.ho) {
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int ww = 0; ww < 8; ++ww)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) t[c] += red[ww][c][lane];
+    const double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / t[3]);
+    out[(long long)i * pitch + x] =
+        make_float4((float)(t[0] * norm), (float)(t[1] * norm), (float)(t[2] * norm), 1.0f);
+  }
 }
 
 }  // namespace tc
@@ -739,25 +669,31 @@ int planned_level(int w, int ow, float roughness, bool irradiance) {
 }
 
 struct LevelPlanes {
-  int level, ws, hs;
-  size_t offset;  // byte offset of the 6 planes in the workspace
+  int level, g, ws, hs;
+  size_t offset;  // byte offset of the 6 planes (phase order for g) in the workspace
+};
+
+struct JobPlan {
+  Job J;
+  int level = -1;  // index into TcPlan::levels; -1 = roughness 0 (plain path)
+  size_t cosd_off = 0, rows_off = 0, orows_off = 0, partial_off = 0,
+         wsum_off = 0;
 };
 
 struct TcPlan {
-  std::vector<Job> jobs;
-  std::vector<int> job_level;      // index into levels
+  std::vector<JobPlan> jobs;
   std::vector<LevelPlanes> levels;
-  std::vector<size_t> cosd_off, rows_off, orows_off, scols_off, ocols_off, partial_off, wsum_off;
   size_t total = 0;
 };
 
 size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-int level_index(TcPlan& P, int w, int h, int level, size_t& off) {
+int level_index(TcPlan& P, int w, int h, int level, int g, size_t& off) {
   for (size_t k = 0; k < P.levels.size(); ++k)
-    if (P.levels[k].level == level) return (int)k;
+    if (P.levels[k].level == level && P.levels[k].g == g) return (int)k;
   LevelPlanes L;
   L.level = level;
+  L.g = g;
   L.ws = level_dim(w, level);
   L.hs = level_dim(h, level);
   L.offset = off;
@@ -767,66 +703,80 @@ int level_index(TcPlan& P, int w, int h, int level, size_t& off) {
 }
 
 // Adds a contraction job (mip or irradiance) to the plan.
-void add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, int level,
-             size_t& off) {
-  Job J;
+int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, int level,
+            size_t& off) {
+  JobPlan jp;
+  Job& J = jp.J;
   memset(&J, 0, sizeof(J));
-  int li = level_index(P, w, h, level, off);
-  J.ws = P.levels[li].ws;
-  J.hs = P.levels[li].hs;
+  J.ws = level_dim(w, level);
+  J.hs = level_dim(h, level);
   J.wo = ow;
   J.ho = oh;
   J.s = J.ws / ow;
+  if (8 % J.s == 0) {
+    J.g = 1;
+    J.m = 8 / J.s;
+  } else if (J.s % 8 == 0) {
+    J.g = J.s / 8;
+    J.m = 1;
+  } else {
+    J.g = J.s;
+    J.m = 8;
+  }
+  const int li = level_index(P, w, h, level, J.g, off);
+  J.krow = J.ws / J.g;
+  J.kpad = ((J.krow + kKS - 1) / kKS) * kKS;
+  J.nres = (ow + J.m - 1) / J.m;
+  J.nb = ((J.nres + 15) / 16) * 16;
+  if (J.nb > kNBMax) J.nb = kNBMax;
+  J.nblk = (J.nres + J.nb - 1) / J.nb;
+  J.nsplit = 1;  // two issuers per channel (N/2 each) measured slower
+  J.rlen = ((8 * J.nb + J.kpad + 7) / 8) * 8;
   J.kind = kind;
   J.a2 = roughness * roughness;
-  int neff = (ow + 7) / 8;
-  J.n_mma = ((neff + 15) / 16) * 16;
-  if (J.n_mma < 16) J.n_mma = 16;
-  J.kpad = ((ow + 15) / 16) * 16;
-  J.tmem_cols = 32;
-  while (J.tmem_cols < 3 * J.n_mma) J.tmem_cols <<= 1;
-  // Pipeline steps of each form (K = 64 per step): the Hankel form pays for
-  // every polyphase row of every source row in each of 8 x residues; the
-  // direct form pays for every source texel in each 128-texel output tile.
-  const double itiles = (oh + kM - 1) / kM;
-  const double hankel_steps = itiles * 8 * J.hs * (double)J.s * ((J.kpad + kKStep - 1) / kKStep);
-  const double otiles = ((double)oh * ow + kM - 1) / kM;
-  const double direct_steps = otiles * J.hs * ((double)J.ws / kKStep);
-  J.direct = (J.ws % kKStep == 0) && 1100.0 * direct_steps < 2500.0 * hankel_steps;
-  int ctas;
-  if (J.direct) {
-    J.tmem_cols = 32;
-    ctas = (int)otiles;
-  } else {
-    ctas = (int)itiles * 8;
-  }
-  // Split the source rows so the CTAs fill whole waves of the 152 SMs.
-  int g = 152, b = ctas;
-  while (b) {
-    int t = g % b;
-    g = b;
-    b = t;
-  }
-  int ks = 152 / g;
+  // Staged rows are rotations of a phase row by multiples of 8 elements, copied
+  // by TMA in 16-byte units.
+  if (J.krow % 8 != 0)
+    return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
+                     "tensor path: a %dx%d output against a %d-wide level has phase rows of "
+                     "%d texels (needs a multiple of 8)",
+                     ow, oh, J.ws, J.krow);
+  for (J.nslots = kMaxSlots; J.nslots > 2; --J.nslots)
+    if (smem_plan(J).total + 4096 <= (size_t)kSmemLimit) break;
+  if (smem_plan(J).total + 4096 > (size_t)kSmemLimit)
+    return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
+                     "tensor path: a %dx%d output against a %d-wide level needs too much "
+                     "shared memory",
+                     ow, oh, J.ws);
+  // Split the source rows so that no CTA sums more than kMaxK of K (one
+  // source row at least: a phase row longer than kMaxK is one chain), then
+  // round the grid up towards whole waves of the 152 SMs.
+  const int ctas = ((oh + kM - 1) / kM) * J.m * J.nblk;
+  int rows_max = kMaxK / (J.g * J.kpad);
+  if (rows_max < 1) rows_max = 1;
+  int ks = (J.hs + rows_max - 1) / rows_max;
+  for (int t = ks; t <= J.hs && t <= 2 * ks; ++t)
+    if ((long long)ctas * t % 152 == 0) {
+      ks = t;
+      break;
+    }
+  if ((long long)ctas * ks < 152) ks = (152 + ctas - 1) / ctas;
   if (ks > J.hs) ks = J.hs;
   if (ks < 1) ks = 1;
   J.ksplit = ks;
-  P.jobs.push_back(J);
-  P.job_level.push_back(li);
-  P.cosd_off.push_back(off);
+  jp.level = li;
+  jp.cosd_off = off;
   off = al256(off + (size_t)J.ws * 4);
-  P.rows_off.push_back(off);
+  jp.rows_off = off;
   off = al256(off + (size_t)J.hs * 12);
-  P.orows_off.push_back(off);
+  jp.orows_off = off;
   off = al256(off + (size_t)oh * 8);
-  P.scols_off.push_back(off);
-  off = al256(off + (size_t)J.ws * 8);
-  P.ocols_off.push_back(off);
-  off = al256(off + (size_t)ow * 8);
-  P.partial_off.push_back(off);
-  off = al256(off + (size_t)ks * oh * 3 * ow * 4);
-  P.wsum_off.push_back(off);
-  off = al256(off + (J.direct ? (size_t)ks * oh * ow * 8 : (size_t)oh * 8));
+  jp.partial_off = off;
+  off = al256(off + (size_t)ks * 3 * ow * oh * 4);
+  jp.wsum_off = off;
+  off = al256(off + (size_t)ks * oh * 8);
+  P.jobs.push_back(jp);
+  return ALTHEA_IBL_OK;
 }
 
 int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int* levels,
@@ -834,44 +784,31 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
   size_t off = 256;  // error flag first
   for (int m = 0; m < n; ++m) {
     if (mips[m].roughness == 0.0f) {  // a delta: handled by the plain path
-      P.jobs.push_back(Job{});
-      P.job_level.push_back(-1);
-      P.cosd_off.push_back(0);
-      P.rows_off.push_back(0);
-      P.orows_off.push_back(0);
-      P.scols_off.push_back(0);
-      P.ocols_off.push_back(0);
-      P.partial_off.push_back(0);
-      P.wsum_off.push_back(0);
+      P.jobs.push_back(JobPlan{});
       continue;
     }
     int lv = levels && levels[m] >= 0 ? levels[m]
                                       : planned_level(w, mips[m].width, mips[m].roughness, false);
     int ws = level_dim(w, lv);
-    if (ws < mips[m].width || ws % mips[m].width != 0 || mips[m].width > 1024 ||
+    if (ws < mips[m].width || ws % mips[m].width != 0 || mips[m].width > 4096 ||
         mips[m].height > 65536)
       return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
                        "tensor path: mip %d (%dx%d) cannot contract against level %d", m,
                        mips[m].width, mips[m].height, lv);
-    add_job(P, w, h, mips[m].width, mips[m].height, mips[m].roughness, 0, lv, off);
+    int st = add_job(P, w, h, mips[m].width, mips[m].height, mips[m].roughness, 0, lv, off);
+    if (st) return st;
   }
   if (irr_w > 0) {
     int lv = irr_level >= 0 ? irr_level : planned_level(w, irr_w, 1.0f, true);
     int ws = level_dim(w, lv);
-    if (ws < irr_w || ws % irr_w != 0 || irr_w > 1024)
+    if (ws < irr_w || ws % irr_w != 0 || irr_w > 4096)
       return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "tensor path: irradiance %dx%d vs level %d",
                        irr_w, irr_h, lv);
-    add_job(P, w, h, irr_w, irr_h, 1.0f, 1, lv, off);
+    int st = add_job(P, w, h, irr_w, irr_h, 1.0f, 1, lv, off);
+    if (st) return st;
   }
   P.total = off;
   return ALTHEA_IBL_OK;
-}
-
-size_t smem_bytes(const Job& J) {
-  if (J.direct) return (size_t)4 * Smem::kA + 2 * (16 * kKStep * 2) + (size_t)J.ws * 8;
-  int rlen = Smem::row_len(J.n_mma, J.kpad);
-  return (size_t)Smem::kAStages * 2 * Smem::kA + (size_t)Smem::kRowSlots * 6 * rlen * 2 +
-         (size_t)J.ws * 4;
 }
 
 }  // namespace
@@ -923,53 +860,51 @@ extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
   char* base = static_cast<char*>(ws);
   cudaError_t e = cudaMemsetAsync(base, 0, 256, s);
   if (e != cudaSuccess) return cuda_status(e, "tc error flag");
-  // Host tables (FP64 -> FP32), uploaded once per call.
   ChainTable tab;
   make_table(w, h, &tab);
   for (auto& L : P.levels) {
-    int nt = L.ws * L.hs;
     const float4* src = reinterpret_cast<const float4*>(chain) + tab.off[L.level];
-    split_kernel<<<(nt + 255) / 256, 256, 0, s>>>(
-        src, nt, reinterpret_cast<__nv_bfloat16*>(base + L.offset));
+    const int sm = 6 * L.ws * 2;
+    if (sm > 48 * 1024) {
+      e = cudaFuncSetAttribute(rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      if (e != cudaSuccess) return cuda_status(e, "tc rows smem attribute");
+    }
+    rows_kernel<<<L.hs, 256, sm, s>>>(src, L.ws, L.hs, L.g,
+                                      reinterpret_cast<__nv_bfloat16*>(base + L.offset));
   }
   for (size_t k = 0; k < P.jobs.size(); ++k) {
-    if (P.job_level[k] < 0) continue;
-    Job& J = P.jobs[k];
-    const LevelPlanes& L = P.levels[P.job_level[k]];
-    J.planes = reinterpret_cast<const __nv_bfloat16*>(base + L.offset);
-    float* cosd = reinterpret_cast<float*>(base + P.cosd_off[k]);
-    float* srows = reinterpret_cast<float*>(base + P.rows_off[k]);
-    float* orows = reinterpret_cast<float*>(base + P.orows_off[k]);
-    float* scols = reinterpret_cast<float*>(base + P.scols_off[k]);
-    float* ocols = reinterpret_cast<float*>(base + P.ocols_off[k]);
+    JobPlan& jp = P.jobs[k];
+    if (jp.level < 0) continue;
+    Job& J = jp.J;
+    const LevelPlanes& L = P.levels[jp.level];
+    J.src = reinterpret_cast<const __nv_bfloat16*>(base + L.offset);
+    float* cosd = reinterpret_cast<float*>(base + jp.cosd_off);
+    float* srows = reinterpret_cast<float*>(base + jp.rows_off);
+    float* orows = reinterpret_cast<float*>(base + jp.orows_off);
     int nmax = J.ws > J.hs ? J.ws : J.hs;
     if (J.ho > nmax) nmax = J.ho;
-    if (J.wo > nmax) nmax = J.wo;
-    tables_kernel<<<(nmax + 255) / 256, 256, 0, s>>>(J.ws, J.hs, J.ho, J.wo, cosd, srows, orows,
-                                                     scols, ocols);
+    // FP64 transcendentals: few per thread, spread over many SMs
+    tables_kernel<<<(nmax + 31) / 32, 32, 0, s>>>(J.ws, J.hs, J.ho, cosd, srows, orows);
     J.cos_d = cosd;
     J.src_rows = srows;
     J.out_rows = orows;
-    J.src_cols = scols;
-    J.out_cols = ocols;
-    J.partial = reinterpret_cast<float*>(base + P.partial_off[k]);
+    J.partial = reinterpret_cast<float*>(base + jp.partial_off);
+    J.wsum_part = reinterpret_cast<double*>(base + jp.wsum_off);
     J.error = reinterpret_cast<int*>(base);
-    double* wsum = reinterpret_cast<double*>(base + P.wsum_off[k]);
-    size_t smem = smem_bytes(J);
-    if (J.direct) {
-      J.wsum_part = wsum;
-      e = cudaFuncSetAttribute(contract_direct_kernel,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // At least 120 KB so no two CTAs share an SM (each allocates all of TMEM).
+    int smem = (int)smem_plan(J).total;
+    if (smem < 120 * 1024) smem = 120 * 1024;
+    dim3 grid((J.ho + kM - 1) / kM, J.m * J.nblk, J.ksplit);
+    if (J.kind == 0) {
+      e = cudaFuncSetAttribute(contract_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               smem);
       if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
-      dim3 grid((unsigned)(((long long)J.ho * J.wo + kM - 1) / kM), J.ksplit);
-      contract_direct_kernel<<<grid, kThreads, smem, s>>>(J);
+      contract_kernel<0><<<grid, kThreads, smem, s>>>(J);
     } else {
-      e = cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem);
+      e = cudaFuncSetAttribute(contract_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               smem);
       if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
-      dim3 grid((J.ho + kM - 1) / kM, 8, J.ksplit);
-      contract_kernel<<<grid, kHThreads, smem, s>>>(J);
-      if (J.kind == 0) weight_sum_kernel<<<J.ho, 256, 0, s>>>(J, wsum);
+      contract_kernel<1><<<grid, kThreads, smem, s>>>(J);
     }
     float4* out;
     long long pitch;
@@ -980,16 +915,12 @@ extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
       out = reinterpret_cast<float4*>(irr_out);
       pitch = (long long)(irr_pitch / 16);
     }
-    long long nt = (long long)J.wo * J.ho;
-    if (J.direct)
-      finish_direct_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(J, out, pitch);
-    else
-      finish_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(J, wsum, out, pitch);
+    finish_kernel<<<dim3((J.ho + 31) / 32, J.wo), 256, 0, s>>>(J, out, pitch);
   }
   // Roughness-0 mips are a delta (no contraction): the plain path's exact
   // texel-corner sample.
   for (int m = 0; m < n; ++m) {
-    if (P.job_level[m] >= 0) continue;
+    if (P.jobs[m].level >= 0) continue;
     st = launch_prefilter(chain, w, h, &mips[m], 1, 1024, ALTHEA_IBL_GEN_HAMMERSLEY, s);
     if (st) return st;
   }

@@ -20,19 +20,29 @@ def _rel(got, ref):
     return np.abs(got - ref) / np.abs(ref)
 
 
-def test_contraction_matches_fp64_quadrature_at_same_source_level():
-    w, h = 512, 256
-    env = synth.make_env(w, h, seed=8, sun_max=1e6)
+# (env w, h, mip sizes, roughness, source levels, irradiance size, irradiance level).
+# The source/output width ratios s cover every decomposition of the kernel:
+# s = 1, 2, 4 (column residues), s = 8, s = 16, 32 (phase rows), s = 3 (both),
+# output heights above one 128-row tile (ragged), and tiny outputs.
+SAME_LEVEL_CASES = [
+    (512, 256, [(128, 64), (64, 32), (16, 8), (256, 128)], [0.25, 0.5, 1.0, 0.125],
+     [1, 1, 2, 1], (32, 16), 2),
+    (384, 192, [(128, 64), (24, 12), (12, 6), (96, 48), (384, 192), (4, 2)],
+     [0.3, 0.6, 0.9, 0.2, 0.15, 1.0], [0, 0, 0, 1, 0, 1], (24, 12), 0),
+]
+
+
+@pytest.mark.parametrize("case", range(len(SAME_LEVEL_CASES)))
+def test_contraction_matches_fp64_quadrature_at_same_source_level(case):
+    w, h, sizes, rough, levels, (iw, ih), ilv = SAME_LEVEL_CASES[case]
+    env = synth.make_env(w, h, seed=8 + case, sun_max=1e6)
     chain = oracle.build_chain(env)
     chain_d = torch.from_numpy(chain).cuda()
-    sizes = [(128, 64), (64, 32), (16, 8), (256, 128)]
-    rough = [0.25, 0.5, 1.0, 0.125]
-    levels = [1, 1, 2, 1]
     outs = [torch.empty((mh, mw, 4), dtype=torch.float32, device="cuda") for mw, mh in sizes]
-    irr = torch.empty((16, 32, 4), dtype=torch.float32, device="cuda")
-    ibl.bake_tc(chain_d, w, h, outs, rough, irradiance=irr, levels=levels, irradiance_level=2)
+    irr = torch.empty((ih, iw, 4), dtype=torch.float32, device="cuda")
+    ibl.bake_tc(chain_d, w, h, outs, rough, irradiance=irr, levels=levels, irradiance_level=ilv)
     torch.cuda.synchronize()
-    rng = np.random.default_rng(0)
+    rng = np.random.default_rng(case)
     for (mw, mh), r, lv, o in zip(sizes, rough, levels, outs):
         src = oracle.chain_level(chain, w, h, lv)
         n = min(mw * mh, 256)
@@ -41,10 +51,10 @@ def test_contraction_matches_fp64_quadrature_at_same_source_level():
         ref = oracle.quad_prefilter(src, mw, mh, r, xy)[:, :3]
         got = o.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
         assert _rel(got, ref).max() <= 1e-4, (mw, r, _rel(got, ref).max())
-    src = oracle.chain_level(chain, w, h, 2)
-    ys, xs = np.mgrid[0:16, 0:32]
+    src = oracle.chain_level(chain, w, h, ilv)
+    ys, xs = np.mgrid[0:ih, 0:iw]
     xy = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
-    ref = oracle.quad_irradiance(src, 32, 16, xy)[:, :3]
+    ref = oracle.quad_irradiance(src, iw, ih, xy)[:, :3]
     got = irr.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
     assert _rel(got, ref).max() <= 1e-4, _rel(got, ref).max()
 
