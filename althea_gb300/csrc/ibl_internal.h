@@ -33,6 +33,9 @@ int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_targ
                      int mip_count, int samples, int generator, cudaStream_t st);
 int launch_irradiance(const float* chain, int w, int h, float* out, int ow, int oh,
                       size_t pitch_bytes, void* ws, cudaStream_t st);
+// Roughness-0 mip as the single reflected sample (no Monte Carlo accumulation).
+int launch_delta_mip(const float* chain, int w, int h, const althea_ibl_mip_target* mip,
+                     cudaStream_t st);
 int launch_brdf_lut(float* out, int n, size_t pitch_bytes, int samples, int orientation,
                     cudaStream_t st);
 

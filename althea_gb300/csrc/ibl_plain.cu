@@ -121,6 +121,45 @@ __global__ void __launch_bounds__(kPfTileX* kPfTileY) prefilter_kernel(const Pre
                       p.generator, tabulated ? h_local : nullptr);
 }
 
+// The value a delta lobe (roughness 0) converges to: the one reflected sample
+// that every kept sample of PreFilterEnvMap.comp:147-167 repeats (H = N, first
+// Hammersley point), without repeating its accumulation.  The precision path
+// uses it for roughness-0 mips (its quadrature of a delta).
+__global__ void __launch_bounds__(256) delta_mip_kernel(const float4* __restrict__ chain, int w,
+                                                        int h, float4* __restrict__ out,
+                                                        long long pitch, int ow, int oh) {
+  __shared__ ChainTable tab;
+  if (threadIdx.x == 0) make_table(w, h, &tab);
+  __syncthreads();
+  const int x = blockIdx.x * 32 + (int)(threadIdx.x & 31);
+  const int y = blockIdx.y * 8 + (int)(threadIdx.x >> 5);
+  if (x >= ow || y >= oh) return;
+  Float3 n = texel_dir(x, y, ow, oh);
+  Float3 t, b;
+  local_frame(n, t, b);
+  Float3 hv = to_world(t, b, n, sample_ggx(0.0f, 0.0f, 0.0f));
+  float vdh = (n.x * hv.x + n.y * hv.y) + n.z * hv.z;
+  float k = 2.0f * vdh;
+  Float3 l = normalize3(f3(k * hv.x - n.x, k * hv.y - n.y, k * hv.z - n.z));
+  float ndotl = glsl_max((n.x * l.x + n.y * l.y) + n.z * l.z, 0.0f);
+  float4 o = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+  if (ndotl > 0.0f) {
+    Float3 c = sample_env(chain, tab, l, 0.0f);
+    o = make_float4(c.x, c.y, c.z, 1.0f);
+  }
+  out[(long long)y * pitch + x] = o;
+}
+
+int launch_delta_mip(const float* chain, int w, int h, const althea_ibl_mip_target* mip,
+                     cudaStream_t st) {
+  dim3 grid((mip->width + 31) / 32, (mip->height + 7) / 8);
+  delta_mip_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const float4*>(chain), w, h,
+                                         reinterpret_cast<float4*>(mip->out_dev),
+                                         (long long)(mip->pitch_bytes / sizeof(float4)),
+                                         mip->width, mip->height);
+  return cuda_status(cudaGetLastError(), "delta mip launch");
+}
+
 int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
                      int mip_count, int samples, int generator, cudaStream_t st) {
   PrefilterParams p;
@@ -271,13 +310,79 @@ __global__ void __launch_bounds__(256) brdf_lut_kernel(float2* __restrict__ out,
   out[(long long)j * pitch + i] = make_float2(sum_a / (float)samples, sum_b / (float)samples);
 }
 
+// The same estimator with the half-vector samples of a row (they depend on the
+// roughness only, not on N.V) tabulated once in shared memory: every texel
+// evaluates the identical IEEE operations in the identical order, so the
+// result is bit-identical to brdf_lut_kernel.  Block per (row, 256 columns);
+// dynamic shared memory: samples * 8 bytes.
+constexpr int kLutTableMax = 8192;
+
+__global__ void __launch_bounds__(256) brdf_lut_row_kernel(float2* __restrict__ out, int n,
+                                                           long long pitch, int samples,
+                                                           int orientation) {
+  extern __shared__ float2 hsamp[];  // (hx, hz) per sample
+  const int j = blockIdx.y;
+  float tj = ((float)j + 0.5f) / (float)n;
+  float rough = orientation == ALTHEA_IBL_LUT_ASSET ? 1.0f - tj : tj;
+  float alpha = rough * rough;
+  float a2 = alpha * alpha;
+  float k = alpha / 2.0f;
+  for (int s = threadIdx.x; s < samples; s += blockDim.x) {
+    float xi_x, xi_y;
+    hammersley(s, samples, xi_x, xi_y);
+    float phi = 2.0f * kPi * xi_x;
+    float cos_t = sqrtf((1.0f - xi_y) / (1.0f + (a2 - 1.0f) * xi_y));
+    float sin_t = sqrtf(1.0f - cos_t * cos_t);
+    hsamp[s] = make_float2(sin_t * agb_cos(phi), cos_t);
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float nov = ((float)i + 0.5f) / (float)n;
+  float vx = sqrtf(1.0f - nov * nov), vz = nov;
+  float sum_a = 0.0f, sum_b = 0.0f;
+#pragma unroll 4
+  for (int s = 0; s < samples; ++s) {
+    const float2 hv = hsamp[s];
+    float hx = hv.x, hz = hv.y;
+    float vdh = vx * hx + vz * hz;
+    float lz = 2.0f * vdh * hz - vz;
+    float nol = lz > 0.0f ? (lz < 1.0f ? lz : 1.0f) : 0.0f;
+    float noh = hz > 0.0f ? (hz < 1.0f ? hz : 1.0f) : 0.0f;
+    float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
+    if (nol > 0.0f) {
+      float g1l = nol / (nol * (1.0f - k) + k);
+      float g1v = nov / (nov * (1.0f - k) + k);
+      float g_vis = g1l * g1v * voh / (noh * nov);
+      float tt = 1.0f - voh;
+      float t2 = tt * tt;
+      float fc = t2 * t2 * tt;
+      sum_a += (1.0f - fc) * g_vis;
+      sum_b += fc * g_vis;
+    }
+  }
+  out[(long long)j * pitch + i] = make_float2(sum_a / (float)samples, sum_b / (float)samples);
+}
+
 int launch_brdf_lut(float* out, int n, size_t pitch_bytes, int samples, int orientation,
                     cudaStream_t st) {
-  dim3 grid((n + 31) / 32, (n + 7) / 8);
-  brdf_lut_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<float2*>(out), n,
-                                        (long long)(pitch_bytes / sizeof(float2)), samples,
-                                        orientation);
-  return cuda_status(cudaGetLastError(), "brdf_lut_kernel launch");
+  const long long pitch = (long long)(pitch_bytes / sizeof(float2));
+  if (samples <= kLutTableMax) {
+    const int sm = samples * (int)sizeof(float2);
+    if (sm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(brdf_lut_row_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      if (e != cudaSuccess) return cuda_status(e, "brdf lut smem attribute");
+    }
+    dim3 grid((n + 255) / 256, n);
+    brdf_lut_row_kernel<<<grid, 256, sm, st>>>(reinterpret_cast<float2*>(out), n, pitch, samples,
+                                               orientation);
+  } else {
+    dim3 grid((n + 31) / 32, (n + 7) / 8);
+    brdf_lut_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<float2*>(out), n, pitch, samples,
+                                          orientation);
+  }
+  return cuda_status(cudaGetLastError(), "brdf lut launch");
 }
 
 // ---------------------------------------------------------------------------

@@ -56,6 +56,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -82,6 +83,7 @@ static_assert(kACol + kStages * kKS <= kTmemCols, "TMEM columns");
 constexpr int kMaxSlots = 4;      // staged radiance rows in flight
 constexpr int kMaxK = 8192;       // K per CTA: one TMEM accumulation chain
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+constexpr uint32_t kSleepNs = 200000;  // longest hardware suspension per try (0.2 ms)
 constexpr float kPiF = 3.14159265358979f;
 constexpr int kSmemLimit = 232448;  // opt-in shared memory per block
 
@@ -126,6 +128,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait that lets the hardware suspend the thread until the phase
+// completes or `ns` nanoseconds pass, so waiting warps do not take issue
+// slots from the working ones.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -138,8 +154,7 @@ __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, volatil
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (;;) {
-    for (int i = 0; i < 64; ++i)
-      if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_sleep(bar, parity, kSleepNs)) return true;
     if (*abort) return false;
     if (global_ns() - t0 > kWaitNs) {
       *abort = 1;
@@ -168,13 +183,36 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
          ((uint32_t)(m >> 4) << 24);    // M / 16
 }
 
-// D (TMEM) += A (TMEM) * B (shared memory).
-__device__ __forceinline__ void mma_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t b,
-                                       uint32_t idesc, uint32_t accumulate) {
+// One K = 32 stage of one channel, hi/lo split, then a commit to `bar`:
+//   D += Ahi*Bhi + Ahi*Blo + Alo*Bhi  for K = 0..15 and 16..31
+// A: TMEM columns a (hi, K 0..15 at +0, 16..31 at +8; lo at +16 / +24);
+// B: descriptors bh/bl (hi/lo plane) and bh2/bl2 (the same 16 K further).
+// One asm block so the six MMAs leave the issuing thread back to back: any
+// instruction between two tcgen05.mma adds to the per-MMA issue time.
+__device__ __forceinline__ void mma_stage_ts(uint32_t d, uint32_t a, uint64_t bh, uint64_t bl,
+                                             uint64_t bh2, uint64_t bl2, uint32_t idesc,
+                                             uint32_t accumulate, uint64_t* bar) {
   asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "r"(tmem_a), "l"(b), "r"(idesc), "r"(accumulate));
+      "{\n .reg .pred p, t;\n .reg .b32 a8, a16, a24;\n"
+      " setp.ne.b32 p, %7, 0;\n setp.eq.b32 t, %7, %7;\n"
+      " add.u32 a8, %1, 8;\n add.u32 a16, %1, 16;\n add.u32 a24, %1, 24;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %6, p;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %3, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a16], %2, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a8], %4, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a8], %5, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a24], %4, %6, t;\n"
+      " tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%8];\n}\n" ::"r"(d),
+      "r"(a), "l"(bh), "l"(bl), "l"(bh2), "l"(bl2), "r"(idesc), "r"(accumulate),
+      "r"((uint32_t)__cvta_generic_to_shared(bar))
+      : "memory");
+}
+
+// Hardware reciprocal approximation (one MUFU operation, ~1 ulp).
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -275,9 +313,12 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   float* cosd_sm = reinterpret_cast<float*>(smem + sp.cosd);
   volatile int* abort_flag = &abort_sh;
 
+  // Producer warps only for lane quarters that hold output rows (four per
+  // quarter); the others have nothing to generate and stay out of the loop.
+  const int live_quarters = min(4, (job.ho - i0 + 31) / 32);
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&a_full[s], kProducerWarps);
+      mbar_init(&a_full[s], 4 * live_quarters);
       mbar_init(&a_empty[s], 3 * job.nsplit);
     }
     for (int s = 0; s < kMaxSlots; ++s) {
@@ -322,7 +363,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     // ---- weight producers: rows 32q + lane, K sub-range [8h, 8h + 8) of each stage
     const int q = warp & 3, h = warp >> 2;
     const int row = 32 * q + lane, gi = i0 + row;
-    const bool live = i0 + 32 * q < job.ho;
+    const bool live = q < live_quarters;
     float cp = 0.0f, sp_ = 0.0f;
     if (gi < job.ho) {
       cp = job.out_rows[2 * gi];
@@ -330,61 +371,74 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     }
     const float a2 = job.a2;
     const float alpha = 0.5f * (1.0f + a2), beta = 0.5f * (a2 - 1.0f), ka = a2 / kPiF;
+    const float2 alpha2 = make_float2(alpha, alpha), beta2 = make_float2(beta, beta);
+    const float2 minus1 = make_float2(-1.0f, -1.0f);
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
     double wacc = 0.0;
     long long gidx = 0;
     int pending = -1;  // stage whose stores are issued but not yet published
     bool ok = true;
-    for (int j = j0; j < j1 && ok; ++j) {
+    for (int j = j0; live && j < j1 && ok; ++j) {
       const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
       const float om = job.src_rows[3 * j + 2];
       const float ccq = cp * cq, ssq = sp_ * sq;
       const float k1 = KIND == 0 ? ka * om : om;
+      const float2 ccq2 = make_float2(ccq, ccq), ssq2 = make_float2(ssq, ssq);
+      const float2 k12 = make_float2(k1, k1);
       for (int ph = 0; ph < job.g && ok; ++ph) {
         const float* cdrow = cosd_sm + ph * job.kpad;
-        float rowsum = 0.0f;
+        float2 rowsum2 = make_float2(0.0f, 0.0f);
         for (int kc = 0; kc < kchunks; ++kc, ++gidx) {
           const int st = (int)(gidx & (kStages - 1));
           const long long use = gidx / kStages;
           uint32_t hw[4], lw[4];
           if (live) {
             const int kb = kc * kKS + 8 * h;
-            float w[8];
+            // four pairs of weights with packed FP32x2 arithmetic
+            float2 w[4];
 #pragma unroll
-            for (int e = 0; e < 8; e += 4) {
-              const float4 cd = *reinterpret_cast<const float4*>(cdrow + kb + e);
-              const float cs[4] = {cd.x, cd.y, cd.z, cd.w};
-#pragma unroll
-              for (int u = 0; u < 4; ++u) {
-                const float c = fmaf(ccq, cs[u], ssq);
-                float v;
-                if (KIND == 0) {
-                  const float den = fmaf(c, beta, alpha);
-                  v = __fdividef(k1 * c, den * den);
-                } else {
-                  v = k1 * c;
-                }
-                w[e + u] = fmaxf(v, 0.0f);
+            for (int e = 0; e < 2; ++e) {
+              const float4 cd = *reinterpret_cast<const float4*>(cdrow + kb + 4 * e);
+              const float2 c01 = __ffma2_rn(ccq2, make_float2(cd.x, cd.y), ssq2);
+              const float2 c23 = __ffma2_rn(ccq2, make_float2(cd.z, cd.w), ssq2);
+              if (KIND == 0) {
+                const float2 d01 = __ffma2_rn(c01, beta2, alpha2);
+                const float2 d23 = __ffma2_rn(c23, beta2, alpha2);
+                const float2 q01 = __fmul2_rn(d01, d01), q23 = __fmul2_rn(d23, d23);
+                const float2 r01 = make_float2(rcp_approx(q01.x), rcp_approx(q01.y));
+                const float2 r23 = make_float2(rcp_approx(q23.x), rcp_approx(q23.y));
+                w[2 * e] = __fmul2_rn(__fmul2_rn(k12, c01), r01);
+                w[2 * e + 1] = __fmul2_rn(__fmul2_rn(k12, c23), r23);
+              } else {
+                w[2 * e] = __fmul2_rn(k12, c01);
+                w[2 * e + 1] = __fmul2_rn(k12, c23);
               }
+            }
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              w[e].x = fmaxf(w[e].x, 0.0f);
+              w[e].y = fmaxf(w[e].y, 0.0f);
             }
             if (kb + 8 > job.krow) {
 #pragma unroll
               for (int u = 0; u < 8; ++u)
-                if (kb + u >= job.krow) w[u] = 0.0f;
+                if (kb + u >= job.krow) {
+                  if (u & 1)
+                    w[u >> 1].y = 0.0f;
+                  else
+                    w[u >> 1].x = 0.0f;
+                }
             }
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-              const __nv_bfloat162 h2 = __floats2bfloat162_rn(w[2 * e], w[2 * e + 1]);
-              const float2 hf = __bfloat1622float2(h2);
-              const __nv_bfloat162 l2 =
-                  __floats2bfloat162_rn(w[2 * e] - hf.x, w[2 * e + 1] - hf.y);
+              const __nv_bfloat162 h2 = __floats2bfloat162_rn(w[e].x, w[e].y);
+              const float2 lo = __ffma2_rn(__bfloat1622float2(h2), minus1, w[e]);
+              const __nv_bfloat162 l2 = __floats2bfloat162_rn(lo.x, lo.y);
               hw[e] = *reinterpret_cast<const uint32_t*>(&h2);
               lw[e] = *reinterpret_cast<const uint32_t*>(&l2);
             }
-            if (want_wsum) {
-#pragma unroll
-              for (int u = 0; u < 8; ++u) rowsum += w[u];
-            }
+            if (want_wsum)
+              rowsum2 = __fadd2_rn(__fadd2_rn(rowsum2, w[0]), __fadd2_rn(__fadd2_rn(w[1], w[2]), w[3]));
           }
           // Software pipeline: the previous stage's TMEM stores landed while
           // this stage's weights were computed; publish that stage now.
@@ -406,7 +460,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
           }
           pending = st;
         }
-        wacc += (double)rowsum;
+        wacc += (double)(rowsum2.x + rowsum2.y);
       }
     }
     if (live) tmem_wait_st();
@@ -449,14 +503,8 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
             }
             tc_fence_after();
             const uint32_t a_hi = tmem + (uint32_t)kACol + st * kKS;
-            const uint32_t acc0 = gidx != 0;
-            mma_ts(d, a_hi, dbh, idesc, acc0);
-            mma_ts(d, a_hi, dbh + r8, idesc, 1u);
-            mma_ts(d, a_hi + 16, dbh, idesc, 1u);
-            mma_ts(d, a_hi + 8, dbh + 2, idesc, 1u);
-            mma_ts(d, a_hi + 8, dbh + 2 + r8, idesc, 1u);
-            mma_ts(d, a_hi + 24, dbh + 2, idesc, 1u);
-            mma_commit(&a_empty[st]);
+            mma_stage_ts(d, a_hi, dbh, dbh + r8, dbh + 2, dbh + 2 + r8, idesc, gidx != 0,
+                         &a_empty[st]);
             if (kc == kchunks - 1) mma_commit(&slot_empty[slot]);
           }
         }
@@ -551,23 +599,33 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
 
 // Direction tables in FP64, stored as FP32: cos of the column offsets
 // (2 pi (d + 0.5) / ws), source rows (cos q, sin q, solid angle) and output
-// rows (cos p, sin p at texel corners).
-__global__ void tables_kernel(int ws, int hs, int ho, float* __restrict__ cosd,
-                              float* __restrict__ srows, float* __restrict__ orows) {
+// rows (cos p, sin p at texel corners).  One launch for every job of a bake:
+// blockIdx.y selects the job.
+constexpr int kMaxTcJobs = ALTHEA_IBL_MAX_MIPS + 1;
+struct TableArgs {
+  int ws[kMaxTcJobs], hs[kMaxTcJobs], ho[kMaxTcJobs];
+  float* cosd[kMaxTcJobs];
+  float* srows[kMaxTcJobs];
+  float* orows[kMaxTcJobs];
+};
+
+__global__ void tables_kernel(const TableArgs a) {
   const double pi = 3.14159265358979323846;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < ws) cosd[t] = (float)cos(2.0 * pi * (t + 0.5) / ws);
+  const int jb = blockIdx.y;
+  const int ws = a.ws[jb], hs = a.hs[jb], ho = a.ho[jb];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < ws) a.cosd[jb][t] = (float)cos(2.0 * pi * (t + 0.5) / ws);
   if (t < hs) {
     double q = pi * ((t + 0.5) / hs - 0.5);
     double q0 = pi * ((double)t / hs - 0.5), q1 = pi * ((double)(t + 1) / hs - 0.5);
-    srows[3 * t] = (float)cos(q);
-    srows[3 * t + 1] = (float)sin(q);
-    srows[3 * t + 2] = (float)((2.0 * pi / ws) * (sin(q1) - sin(q0)));
+    a.srows[jb][3 * t] = (float)cos(q);
+    a.srows[jb][3 * t + 1] = (float)sin(q);
+    a.srows[jb][3 * t + 2] = (float)((2.0 * pi / ws) * (sin(q1) - sin(q0)));
   }
   if (t < ho) {
     double p = pi * ((double)t / ho - 0.5);
-    orows[2 * t] = (float)cos(p);
-    orows[2 * t + 1] = (float)sin(p);
+    a.orows[jb][2 * t] = (float)cos(p);
+    a.orows[jb][2 * t + 1] = (float)sin(p);
   }
 }
 
@@ -598,38 +656,46 @@ __global__ void rows_kernel(const float4* __restrict__ src, int ws, int hs, int 
   }
 }
 
-// Sum the K splits (FP64, fixed order), normalise, write RGBA32F.  Block per
-// (32 output rows, one column); warp w sums the splits k = w mod 8 with the
-// lanes on consecutive rows (the partial layout), then warp 0 combines.
+// Sum the K splits (FP32, fixed order), normalise by the FP64 weight sum,
+// write RGBA32F.  Block per (32 output rows, one column); warp w sums the
+// splits k = w mod 8 with the lanes on consecutive rows (the partial layout),
+// then warp 0 combines the eight in order.  FP64 is used only for the weight
+// sums and the final normalisation.
 __global__ void __launch_bounds__(256) finish_kernel(const Job job, float4* __restrict__ out,
                                                      long long pitch) {
-  __shared__ double red[8][4][32];
+  __shared__ float red[8][3][32];
+  __shared__ double redw[8][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int i = blockIdx.x * 32 + lane, x = blockIdx.y;
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0, sw = 0.0;
+  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+  double sw = 0.0;
   if (i < job.ho) {
+    const size_t plane = (size_t)job.wo * job.ho;
     for (int k = w; k < job.ksplit; k += 8) {
       const float* p = job.partial + (((size_t)k * 3) * job.wo + x) * job.ho + i;
-      const size_t plane = (size_t)job.wo * job.ho;
-      s0 += (double)p[0];
-      s1 += (double)p[plane];
-      s2 += (double)p[2 * plane];
+      s0 += p[0];
+      s1 += p[plane];
+      s2 += p[2 * plane];
       if (job.kind == 0) sw += job.wsum_part[(size_t)k * job.ho + i];
     }
   }
   red[w][0][lane] = s0;
   red[w][1][lane] = s1;
   red[w][2][lane] = s2;
-  red[w][3][lane] = sw;
+  redw[w][lane] = sw;
   __syncthreads();
   if (w == 0 && i < job.ho) {
-    double t[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int ww = 0; ww < 8; ++ww)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) t[c] += red[ww][c][lane];
-    const double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / t[3]);
+    float t0 = 0.0f, t1 = 0.0f, t2 = 0.0f;
+    double tw = 0.0;
+    for (int ww = 0; ww < 8; ++ww) {
+      t0 += red[ww][0][lane];
+      t1 += red[ww][1][lane];
+      t2 += red[ww][2][lane];
+      tw += redw[ww][lane];
+    }
+    const double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / tw);
     out[(long long)i * pitch + x] =
-        make_float4((float)(t[0] * norm), (float)(t[1] * norm), (float)(t[2] * norm), 1.0f);
+        make_float4((float)(t0 * norm), (float)(t1 * norm), (float)(t2 * norm), 1.0f);
   }
 }
 
@@ -872,22 +938,36 @@ extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
     rows_kernel<<<L.hs, 256, sm, s>>>(src, L.ws, L.hs, L.g,
                                       reinterpret_cast<__nv_bfloat16*>(base + L.offset));
   }
+  // Direction tables of every job, one launch (FP64 transcendentals spread
+  // over many SMs).
+  {
+    TableArgs ta;
+    memset(&ta, 0, sizeof(ta));
+    int nt = 0, nmax = 1;
+    for (size_t k = 0; k < P.jobs.size(); ++k) {
+      JobPlan& jp = P.jobs[k];
+      if (jp.level < 0) continue;
+      Job& J = jp.J;
+      J.cos_d = reinterpret_cast<float*>(base + jp.cosd_off);
+      J.src_rows = reinterpret_cast<float*>(base + jp.rows_off);
+      J.out_rows = reinterpret_cast<float*>(base + jp.orows_off);
+      ta.ws[nt] = J.ws;
+      ta.hs[nt] = J.hs;
+      ta.ho[nt] = J.ho;
+      ta.cosd[nt] = const_cast<float*>(J.cos_d);
+      ta.srows[nt] = const_cast<float*>(J.src_rows);
+      ta.orows[nt] = const_cast<float*>(J.out_rows);
+      nmax = std::max(nmax, std::max(J.ws, std::max(J.hs, J.ho)));
+      ++nt;
+    }
+    if (nt > 0) tables_kernel<<<dim3((nmax + 31) / 32, nt), 32, 0, s>>>(ta);
+  }
   for (size_t k = 0; k < P.jobs.size(); ++k) {
     JobPlan& jp = P.jobs[k];
     if (jp.level < 0) continue;
     Job& J = jp.J;
     const LevelPlanes& L = P.levels[jp.level];
     J.src = reinterpret_cast<const __nv_bfloat16*>(base + L.offset);
-    float* cosd = reinterpret_cast<float*>(base + jp.cosd_off);
-    float* srows = reinterpret_cast<float*>(base + jp.rows_off);
-    float* orows = reinterpret_cast<float*>(base + jp.orows_off);
-    int nmax = J.ws > J.hs ? J.ws : J.hs;
-    if (J.ho > nmax) nmax = J.ho;
-    // FP64 transcendentals: few per thread, spread over many SMs
-    tables_kernel<<<(nmax + 31) / 32, 32, 0, s>>>(J.ws, J.hs, J.ho, cosd, srows, orows);
-    J.cos_d = cosd;
-    J.src_rows = srows;
-    J.out_rows = orows;
     J.partial = reinterpret_cast<float*>(base + jp.partial_off);
     J.wsum_part = reinterpret_cast<double*>(base + jp.wsum_off);
     J.error = reinterpret_cast<int*>(base);
@@ -917,11 +997,10 @@ extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
     }
     finish_kernel<<<dim3((J.ho + 31) / 32, J.wo), 256, 0, s>>>(J, out, pitch);
   }
-  // Roughness-0 mips are a delta (no contraction): the plain path's exact
-  // texel-corner sample.
+  // Roughness-0 mips are a delta (no contraction): the reflected sample itself.
   for (int m = 0; m < n; ++m) {
     if (P.jobs[m].level >= 0) continue;
-    st = launch_prefilter(chain, w, h, &mips[m], 1, 1024, ALTHEA_IBL_GEN_HAMMERSLEY, s);
+    st = launch_delta_mip(chain, w, h, &mips[m], s);
     if (st) return st;
   }
   return cuda_status(cudaGetLastError(), "tensor path launch");

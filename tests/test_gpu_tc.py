@@ -79,9 +79,10 @@ def test_plan_meets_1e3_against_level0_quadrature():
         ref = oracle.quad_prefilter(lvl0, mw, mh, r, xy)[:, :3]
         got = o.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
         assert _rel(got, ref).max() <= 1e-3, (mw, r, _rel(got, ref).max())
-    # roughness 0 takes the plain path (a delta)
+    # roughness 0 is a delta: the reflected sample itself, which the reference
+    # estimator reaches after summing 1024 identical samples in FP32
     ref0 = oracle.prefilter(chain, w, h, 512, 256, 0.0, 1024, oracle.GEN_HAMMERSLEY)
-    assert np.array_equal(outs[0].cpu().numpy(), ref0)
+    assert _rel(outs[0].cpu().numpy()[..., :3], ref0[..., :3]).max() <= 1e-4
     idx = rng.choice(64 * 32, size=48, replace=False)
     xy = np.stack([idx % 64, idx // 64], 1).astype(np.int32)
     ref = oracle.quad_irradiance(lvl0, 64, 32, xy)[:, :3]
