@@ -1,28 +1,31 @@
 #!/usr/bin/env python
-"""Benchmark: IBL probe bakes per second on one GB300 (plain path).
+"""Benchmark: IBL probe bakes per second on one GB300.
 
-Workload (one "step" = one probe bake): a 4096x2048 RGBA32F equirect map
-(seeded synthetic: sky gradient x log-normal noise + 8 suns up to 1e4) ->
-env mip chain (13 levels) + 128x64 irradiance + 9-mip GGX chain from
-2048x1024 (roughness m/8) with N = 1024 reference-hash samples per texel +
-512x512 RG32F split-sum LUT (1024 Hammersley samples), all FP32.
+Default (``--path tc``), the metric's configuration: a 4096x2048 RGBA32F
+equirect map (seeded synthetic: sky gradient x log-normal noise + 8 suns up to
+1e6) -> env mip chain (13 levels) + 9-mip GGX chain from 2048x1024 (roughness
+m/8) + 128x64 irradiance + 512x512 RG32F split-sum LUT.  Mips 1-8 and the
+irradiance are split-precision (BF16 hi/lo) tcgen05 contractions within 1e-3
+of the FP64 quadrature; the plain path (the reference estimator, N = 1024
+Hammersley) is timed on the same map in the same run.
 
-* value   : probes/s with the env level 0 resident in HBM (chain build +
-            prefilter + irradiance + LUT timed with CUDA events; L2 flushed
-            by a 256 MB write between steps, outside the events).
-* e2e     : probes/s through the public context API with host buffers:
-            pinned H2D upload of level 0, bake, D2H of every output.
-* roofline: the prefilter kernel (dominant), algorithmic gathered bytes
-            (128 B per trilinear sample, 64 B per roughness-0 texel, 16 B per
-            output texel) / its event-timed duration vs measured HBM peak.
-* cpu_baseline: the reference shaders compiled as C++ (oracle/_ref) -- or
-            the C restatement when that library is absent -- on every host
-            core, over a bounded sample of texels per mip, extrapolated to a
-            whole probe.
+* value   : probes/s with the env level 0 resident in HBM (chain + bake + LUT
+            timed with CUDA events; L2 flushed by a 256 MB write between steps,
+            outside the events).
+* e2e     : the same step with the env uploaded from pinned host memory and
+            every output read back, through the public calls.
+* roofline: the contraction kernels against the measured BF16 tensor peak
+            (split-precision flops: 2 x 9 per (output, source) texel pair).
+* cpu_baseline: the reference shaders compiled as C++ (oracle/_ref) -- or the
+            C restatement when that library is absent -- on every host core,
+            over a bounded sample of texels per mip, extrapolated to a probe.
 
-``--impl reference`` times only that CPU implementation (rank 0).
-Multi-GPU: one process per GPU, each bakes its own probe (independent
-units, no collective) -> weak scaling; value = all probes / max rank time.
+``--path plain``: the plain production configuration (suns up to 1e4, the
+reference estimator bit-for-bit) with its HBM roofline.  ``--impl reference``
+times only the reference's CPU implementation (rank 0).  ``--workload batch``
+and ``--workload serve`` run the batching and serving configurations.
+Multi-GPU: one process per GPU, each bakes its own probe (independent units,
+no collective) -> weak scaling; value = all probes / max rank time.
 """
 from __future__ import annotations
 
@@ -48,6 +51,9 @@ SAMPLES = 1024
 LUT_N, LUT_SAMPLES = 512, 1024
 WORKLOAD = ("4096x2048 RGBA32F env, 13-level chain, 128x64 irradiance, 9-mip GGX chain from "
             "2048x1024 (roughness m/8), N=1024 {gen} samples, 512x512 RG32F LUT, FP32")
+TC_WORKLOAD = ("precision: 4096x2048 RGBA32F env (suns <= 1e6), 9-mip GGX chain from 2048x1024 "
+               "(roughness m/8), 128x64 irradiance, 512x512 RG32F LUT; mips 1-8 and irradiance as "
+               "tcgen05 BF16 hi/lo contractions within 1e-3 of FP64")
 # Sample generator of the prefilter: 1 = Hammersley (the benchmark configurations'
 # choice), 0 = the reference shader's hash RNG.  Set from --generator.
 GENERATOR = 1
@@ -55,8 +61,9 @@ GENERATOR = 1
 
 def workload():
     return WORKLOAD.format(gen="Hammersley" if GENERATOR == 1 else "reference-hash")
-# DRAM bytes per prefilter launch from ncu (profiles/prefilter_c2_ncu.md); None until measured.
-NCU_PREFILTER_TRAFFIC = None
+# DRAM bytes (read + write) of one prefilter_kernel launch of the plain 4096x2048
+# workload, from the ncu capture summarised in profiles/ibl_bake_c2_4096x2048_ncu.md.
+NCU_PREFILTER_TRAFFIC = 156.4e6
 
 
 def mip_sizes():
@@ -195,7 +202,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     from althea_gb300 import synth
-    env = synth.make_env(ENV_W, ENV_H, seed=0, sun_max=1e4)
+    env = synth.make_env(ENV_W, ENV_H, seed=0, sun_max=args.sun_max if args.path == "tc" else 1e4)
     for _ in range(args.warmup):
         cpu_sample_probe_time(env, "reference", scale=8.0)
     times = []
@@ -210,8 +217,10 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload(), "path": "reference compute shaders compiled as C++ "
-                       "(CPU, all host threads), extrapolated from a bounded texel sample"},
+            "config": {"workload": TC_WORKLOAD if args.path == "tc" else workload(),
+                       "path": "reference compute shaders compiled as C++ (CPU, all host "
+                       "threads, N = 1024 samples per texel), extrapolated from a bounded "
+                       "texel sample"},
             "cpu_baseline": {"value": value, "unit": "probes/s", "cores": info[1],
                              "kind": info[0], "sample": info[2]},
             "e2e": {"value": value, "unit": "probes/s", "h2d_bytes_per_step": 0,
@@ -373,14 +382,39 @@ def run_ours(args):
     return 0
 
 
-def tc_algorithmic_flops(levels, irr_level):
-    """2 * outputs * sources * 4 per contraction (RGB + weight, counted once)."""
-    total = 0
-    for (w, h), lv in zip(mip_sizes(), levels):
-        if lv >= 0:
-            total += 2 * w * h * max(ENV_W >> lv, 1) * max(ENV_H >> lv, 1) * 4
-    total += 2 * IRR_W * IRR_H * max(ENV_W >> irr_level, 1) * max(ENV_H >> irr_level, 1) * 4
-    return total
+def tc_jobs(levels, irr_level):
+    """(output width, output height, source width, source height, phase count g)
+    of every contraction of one precision bake (the planner's decomposition:
+    g = 1 when 8 % s == 0, s / 8 when s % 8 == 0, else s; s = source / output width)."""
+    jobs = []
+    for (w, h), lv in list(zip(mip_sizes(), levels)) + [((IRR_W, IRR_H), irr_level)]:
+        if lv < 0:
+            continue
+        ws, hs = max(ENV_W >> lv, 1), max(ENV_H >> lv, 1)
+        s = ws // w
+        g = 1 if 8 % s == 0 else (s // 8 if s % 8 == 0 else s)
+        jobs.append((w, h, ws, hs, lv, g))
+    return jobs
+
+
+def tc_flops(levels, irr_level):
+    """Per bake: (split-precision flops, useful flops).  Every output texel is a
+    sum over every texel of its source level; the split-precision form spends
+    3 colour channels x 3 BF16 products (hi*hi, hi*lo, lo*hi) on each pair, the
+    weighted RGB sum itself 3 channels x 1 product (2 flops per product)."""
+    pairs = sum(w * h * ws * hs for w, h, ws, hs, _, _ in tc_jobs(levels, irr_level))
+    return 2 * 9 * pairs, 2 * 3 * pairs
+
+
+def tc_launches(levels, irr_level):
+    """Kernels of one precision probe step: chain blits, one split+phase pass per
+    (level, g), one tables pass, contraction + finish per job, one delta pass per
+    roughness-0 mip, the LUT."""
+    from althea_gb300 import ibl
+    jobs = tc_jobs(levels, irr_level)
+    groups = {(lv, g) for _, _, _, _, lv, g in jobs}
+    return ((ibl.chain_levels(ENV_W, ENV_H) - 1) + len(groups) + 1 + 2 * len(jobs) +
+            levels.count(-1) + 1)
 
 
 def error_table(env, outs_by_path, irr_by_path, per_mip=12, seed=7):
@@ -414,14 +448,27 @@ def error_table(env, outs_by_path, irr_by_path, per_mip=12, seed=7):
 
 
 def run_tc(args):
-    """Precision configuration: 4096x2048 map with suns up to 1e6; mips 1-8 and
-    the irradiance as tensor-core contractions (roughness-0 mip 0 via the plain
-    kernel), plus chain and LUT; compared with the plain path on the same map."""
+    """Precision configuration (the default): a 4096x2048 map with suns up to
+    1e6; mips 1-8 and the irradiance as split-precision tensor-core
+    contractions within 1e-3 of the FP64 quadrature, mip 0 (roughness 0) the
+    reflected sample, plus env chain and LUT.  The plain path is timed on the
+    same map in the same run (its error against FP64 is reported beside)."""
     import torch
+    from althea_gb300 import dist as adist
     from althea_gb300 import ibl, synth
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl", device_id=dev)
+        pg = tdist
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
     env = synth.make_env(ENV_W, ENV_H, seed=rank, sun_max=args.sun_max)
     env_d = torch.from_numpy(env).to(dev)
     chain = torch.empty((ibl.chain_texels(ENV_W, ENV_H), 4), dtype=torch.float32, device=dev)
@@ -445,22 +492,36 @@ def run_tc(args):
         ibl.brdf_lut(LUT_N, LUT_SAMPLES, ibl.LUT_ASSET, out=lut, stream=stream)
         ev[3].record(stream)
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            step([torch.cuda.Event(enable_timing=True) for _ in range(4)])
-    stream.synchronize()
-    evs = []
-    with ClockSampler(local) as clk:
+    def timed(step_fn, nev):
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                flush.fill_(1)
+                step_fn([torch.cuda.Event(enable_timing=True) for _ in range(nev)])
+        stream.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        evs = []
         with torch.cuda.stream(stream):
             for _ in range(args.steps):
-                flush.fill_(1)
-                ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-                step(ev)
+                flush.fill_(1)  # evict L2 between timed steps (outside the events)
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(nev)]
+                step_fn(ev)
                 evs.append(ev)
         torch.cuda.synchronize()
+        barrier()
+        return evs
+
+    with ClockSampler(local) as clk:
+        evs = timed(step, 4)
     ibl._check(ibl.load().althea_ibl_tc_error(ws.data_ptr(), stream.cuda_stream))
-    step_ms = float(np.mean([e[0].elapsed_time(e[3]) for e in evs]))
+    total_ms = adist.allreduce_max(float(np.sum([e[0].elapsed_time(e[3]) for e in evs])), dev)
+    value = args.steps * world / (total_ms / 1e3)
     tc_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+    chain_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+    lut_ms = float(np.mean([e[2].elapsed_time(e[3]) for e in evs]))
+    tc_outs = [t.cpu().numpy() for t in mips]
+    tc_irr = irr.cpu().numpy()
+
     # e2e: pinned host env in, every output out, through the public calls
     host_env = torch.from_numpy(env).pin_memory()
     h_outs = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in mips + [irr, lut]]
@@ -473,61 +534,84 @@ def run_tc(args):
 
     with torch.cuda.stream(stream):
         e2e_step()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream.synchronize()
+    barrier()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
         a.record(stream)
         for _ in range(args.steps):
             e2e_step()
         b.record(stream)
     stream.synchronize()
-    e2e_ms = a.elapsed_time(b) / args.steps
-    tc_outs = [t.cpu().numpy() for t in mips]
-    tc_irr = irr.cpu().numpy()
-    # the plain path on the same map (Hammersley, N = 1024) for the error table
+    barrier()
+    e2e_ms = adist.allreduce_max(a.elapsed_time(b), dev) / args.steps
+
+    # the plain path (reference estimator, N = 1024 Hammersley) on the same map
     p_mips = [torch.empty_like(t) for t in mips]
     p_irr = torch.empty_like(irr)
-    with torch.cuda.stream(stream):
-        pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        pa.record(stream)
+    p_ws = torch.empty(ibl.load().althea_ibl_irradiance_workspace_size(ENV_W, ENV_H, IRR_W, IRR_H),
+                       dtype=torch.uint8, device=dev)
+
+    def plain_step(ev):
+        ev[0].record(stream)
+        ibl.build_env_chain_into(env_d, chain, stream)
         ibl.prefilter(chain, ENV_W, ENV_H, p_mips, rough, SAMPLES, ibl.GEN_HAMMERSLEY, stream)
-        ibl.irradiance(chain, ENV_W, ENV_H, p_irr, None, stream)
-        pb.record(stream)
-    stream.synchronize()
-    plain_ms = pa.elapsed_time(pb)
+        ibl.irradiance(chain, ENV_W, ENV_H, p_irr, p_ws, stream)
+        ibl.brdf_lut(LUT_N, LUT_SAMPLES, ibl.LUT_ASSET, out=lut, stream=stream)
+        ev[1].record(stream)
+
+    pevs = timed(plain_step, 2)
+    plain_ms = adist.allreduce_max(float(np.sum([e[0].elapsed_time(e[1]) for e in pevs])),
+                                   dev) / args.steps
     errs = error_table(env, {"tensor": tc_outs, "plain": [t.cpu().numpy() for t in p_mips]},
                        {"tensor": tc_irr, "plain": p_irr.cpu().numpy()})
-    peaks = {}
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(p):
-        peaks = json.load(open(p))
-    peak = float(peaks.get("bf16_tflops", 1900.0))
-    flops = tc_algorithmic_flops(levels, irr_level)
-    achieved = flops / (tc_ms / 1e3) / 1e12
-    h2d = host_env.numel() * 4
-    d2h = sum(t.numel() * 4 for t in h_outs)
-    line = {"metric": METRIC, "value": 1e3 / step_ms, "unit": "probes/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16 hi/lo (fp32 accumulate, fp64 normalisation)",
-            "data": f"synthetic (sky x log-normal noise + 8 suns <= {args.sun_max:g})",
-            "config": {"workload": "precision: 4096x2048 env, 9-mip GGX chain from 2048x1024 "
-                                   "(roughness m/8), 128x64 irradiance, 512x512 LUT; mips 1-8 "
-                                   "and irradiance as tcgen05 contractions, mip 0 plain",
-                       "path": "tensor", "source_levels": levels, "irradiance_level": irr_level,
-                       "stage_ms": {"contraction": tc_ms},
-                       "plain_same_map_ms_prefilter_irradiance": plain_ms,
-                       "max_rel_err_vs_fp64": {"tensor": errs["tensor"]["max"],
-                                               "plain_N1024": errs["plain"]["max"]},
-                       "errors_per_mip_max_mean": errs,
-                       "l2": "flushed (256 MB write) between timed steps"},
-            "e2e": {"value": 1e3 / e2e_ms, "unit": "probes/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
-                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                         "kernel": "contract_kernel (all contractions of one bake)",
-                         "algorithmic_flops_per_bake": flops},
-            "clocks": clk.summary()}
     if rank == 0:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        peak = float(peaks.get("bf16_tflops", 1900.0))
+        peak_kind = "measured" if "bf16_tflops" in peaks else "fallback"
+        split_flops, useful_flops = tc_flops(levels, irr_level)
+        achieved = split_flops / (tc_ms / 1e3) / 1e12
+        h2d = host_env.numel() * 4
+        d2h = sum(t.numel() * 4 for t in h_outs)
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference",
+                                                                         scale=100.0)
+            cpu = {"value": 1.0 / per_probe, "unit": "probes/s", "cores": cores, "kind": kind,
+                   "sample": sample + f" ({spent:.1f} s of CPU work)"}
+        line = {"metric": METRIC, "value": value, "unit": "probes/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "bf16 hi/lo split (fp32 accumulate, fp64 weight normalisation)",
+                "data": f"synthetic (seeded sky x log-normal noise + 8 suns <= {args.sun_max:g})",
+                "config": {"workload": TC_WORKLOAD,
+                           "path": "tensor", "global_batch": world,
+                           "parallelism": f"replicas x{world}",
+                           "source_levels": levels, "irradiance_level": irr_level,
+                           "stage_ms": {"chain": chain_ms, "contraction": tc_ms, "lut": lut_ms},
+                           "plain_same_map": {"value": 1e3 / plain_ms, "unit": "probes/s",
+                                              "ms_per_step": plain_ms,
+                                              "max_rel_err_vs_fp64": errs["plain"]["max"]},
+                           "max_rel_err_vs_fp64": errs["tensor"]["max"],
+                           "errors_per_mip_max_mean": errs,
+                           "l2": "flushed (256 MB write) between timed steps"},
+                "e2e": {"value": world * 1e3 / e2e_ms, "unit": "probes/s",
+                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "gpu_launches": tc_launches(levels, irr_level) * args.steps,
+                "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                             "kernel": "contract_kernel (every contraction of one bake; the "
+                                       "timed stage also holds the split, tables, finish and "
+                                       "delta kernels)",
+                             "peak_source": peak_kind + " (bf16 burst)",
+                             "flops_per_bake": split_flops,
+                             "useful_flops_per_bake": useful_flops},
+                "clocks": clk.summary(),
+                "cpu_baseline": cpu}
         print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
     return 0
 
 
@@ -660,8 +744,9 @@ def main():
                     help="probe: one 4096x2048 bake per step (default); batch: many probes; "
                          "serve: Poisson request stream against the server")
     ap.add_argument("--batch", type=int, default=256)
-    ap.add_argument("--path", default="plain", choices=["plain", "tc"],
-                    help="probe workload: plain estimator or tensor-core precision path")
+    ap.add_argument("--path", default="tc", choices=["plain", "tc"],
+                    help="probe workload: tensor-core precision path (default, suns <= 1e6) "
+                         "or the plain estimator (suns <= 1e4)")
     ap.add_argument("--sun-max", type=float, default=1e6, help="precision path sun radiance")
     ap.add_argument("--rates", type=float, nargs="+", default=[50, 200, 500, 1000, 2000])
     ap.add_argument("--requests", type=int, default=10000)
