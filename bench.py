@@ -14,8 +14,9 @@ Hammersley) is timed on the same map in the same run.
             outside the events).
 * e2e     : the same step with the env uploaded from pinned host memory and
             every output read back, through the public calls.
-* roofline: the contraction kernels against the measured BF16 tensor peak
-            (split-precision flops: 2 x 9 per (output, source) texel pair).
+* roofline: the contraction stage against the measured BF16 tensor peak;
+            algorithmic flops 2 x 4 (RGBA, once) per (output, source) texel
+            pair; the executed split-precision flops (2 x 9 per pair) beside.
 * cpu_baseline: the reference shaders compiled as C++ (oracle/_ref) -- or the
             C restatement when that library is absent -- on every host core,
             over a bounded sample of texels per mip, extrapolated to a probe.
@@ -398,12 +399,13 @@ def tc_jobs(levels, irr_level):
 
 
 def tc_flops(levels, irr_level):
-    """Per bake: (split-precision flops, useful flops).  Every output texel is a
-    sum over every texel of its source level; the split-precision form spends
-    3 colour channels x 3 BF16 products (hi*hi, hi*lo, lo*hi) on each pair, the
-    weighted RGB sum itself 3 channels x 1 product (2 flops per product)."""
+    """Per bake: (algorithmic flops, executed split-precision flops).  Every
+    output texel is a sum over every texel of its source level (a pair).
+    Algorithmic: 2 flops x 4 channels (RGBA, counted once) per pair -- hi/lo
+    split terms, padding and weight generation not counted.  Executed: the
+    3 colour channels x 3 BF16 products (hi*hi, hi*lo, lo*hi) issued per pair."""
     pairs = sum(w * h * ws * hs for w, h, ws, hs, _, _ in tc_jobs(levels, irr_level))
-    return 2 * 9 * pairs, 2 * 3 * pairs
+    return 2 * 4 * pairs, 2 * 9 * pairs
 
 
 def tc_launches(levels, irr_level):
@@ -570,8 +572,9 @@ def run_tc(args):
             os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
         peak = float(peaks.get("bf16_tflops", 1900.0))
         peak_kind = "measured" if "bf16_tflops" in peaks else "fallback"
-        split_flops, useful_flops = tc_flops(levels, irr_level)
-        achieved = split_flops / (tc_ms / 1e3) / 1e12
+        alg_flops, split_flops = tc_flops(levels, irr_level)
+        achieved = alg_flops / (tc_ms / 1e3) / 1e12
+        executed = split_flops / (tc_ms / 1e3) / 1e12
         h2d = host_env.numel() * 4
         d2h = sum(t.numel() * 4 for t in h_outs)
         cpu = None
@@ -605,8 +608,10 @@ def run_tc(args):
                                        "timed stage also holds the split, tables, finish and "
                                        "delta kernels)",
                              "peak_source": peak_kind + " (bf16 burst)",
-                             "flops_per_bake": split_flops,
-                             "useful_flops_per_bake": useful_flops},
+                             "algorithmic_flops_per_bake": alg_flops,
+                             "executed_split_flops_per_bake": split_flops,
+                             "executed_tflops": executed, "executed_frac": executed / peak,
+                             "jobs": [list(j) for j in tc_jobs(levels, irr_level)]},
                 "clocks": clk.summary(),
                 "cpu_baseline": cpu}
         print(json.dumps(line))
