@@ -279,6 +279,23 @@ struct althea_ibl_batch {
   // graph
   cudaGraphExec_t exec = nullptr;
   cudaStream_t exec_stream = nullptr;
+  // precision path (ALTHEA_IBL_BATCH_PRECISION): one tensor-core bake per
+  // probe after the shared chain pass; probes of one shape share a workspace
+  // (every launch is stream-ordered, so the bakes never overlap)
+  bool precision = false;
+  int out_format = ALTHEA_IBL_FORMAT_RGBA32F;
+  struct TcProbe {
+    const float* chain;
+    int w, h;
+    std::vector<althea_ibl_mip_target> mips;
+    float* irr;
+    int irr_w, irr_h;
+    size_t irr_pitch;
+    int ws;  // index into tc_ws
+  };
+  std::vector<TcProbe> tc;
+  std::vector<void*> tc_ws;
+  std::vector<size_t> tc_ws_bytes;
 };
 
 namespace {
@@ -295,6 +312,7 @@ void free_batch(althea_ibl_batch* b) {
   cudaFree(b->d_irr_begins);
   cudaFree(b->d_irr_texel_begins);
   cudaFree(b->d_partial);
+  for (void* p : b->tc_ws) cudaFree(p);
   delete b;
 }
 
@@ -437,10 +455,25 @@ int launch_irradiance_batch(althea_ibl_batch* b, cudaStream_t st) {
   return cuda_status(cudaGetLastError(), "batch irradiance launch");
 }
 
+int launch_tc(althea_ibl_batch* b, cudaStream_t st) {
+  int r = ALTHEA_IBL_OK;
+  for (size_t i = 0; i < b->tc.size() && !r; ++i) {
+    const althea_ibl_batch::TcProbe& p = b->tc[i];
+    r = tc_bake(p.chain, p.w, p.h, p.mips.data(), (int)p.mips.size(), nullptr, p.irr, p.irr_w,
+                p.irr_h, p.irr_pitch, -1, b->tc_ws[p.ws], b->tc_ws_bytes[p.ws], b->out_format,
+                st);
+  }
+  return r;
+}
+
 int launch_all(althea_ibl_batch* b, cudaStream_t st) {
   int r = launch_chains(b, st);
-  if (!r) r = launch_prefilter_queue(b, st);
-  if (!r) r = launch_irradiance_batch(b, st);
+  if (b->precision) {
+    if (!r) r = launch_tc(b, st);
+  } else {
+    if (!r) r = launch_prefilter_queue(b, st);
+    if (!r) r = launch_irradiance_batch(b, st);
+  }
   if (!r && b->params.lut_dev && b->params.lut_size > 0)
     r = launch_brdf_lut(b->params.lut_dev, b->params.lut_size, b->params.lut_pitch_bytes,
                         b->params.lut_samples, b->params.lut_orientation, st);
@@ -519,7 +552,7 @@ int autotune(althea_ibl_batch* b, const althea_ibl_probe* probes, cudaStream_t s
   return r;
 }
 
-int check_probe(const althea_ibl_probe& p, int i) {
+int check_probe(const althea_ibl_probe& p, int i, size_t texel) {
   int r = check_env(p.env_width, p.env_height);
   if (r) return r;
   if (!p.chain_dev || ((uintptr_t)p.chain_dev) % 16 ||
@@ -528,7 +561,7 @@ int check_probe(const althea_ibl_probe& p, int i) {
   if (p.mip_count < 0 || p.mip_count > ALTHEA_IBL_MAX_MIPS)
     return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "probe %d: mip_count %d", i, p.mip_count);
   for (int m = 0; m < p.mip_count; ++m) {
-    r = check_image(p.mip_dev[m], p.mip_width[m], p.mip_height[m], p.mip_pitch_bytes[m], 16,
+    r = check_image(p.mip_dev[m], p.mip_width[m], p.mip_height[m], p.mip_pitch_bytes[m], texel,
                     "batch mip");
     if (r) return r;
     if (!(p.mip_roughness[m] >= 0.0f && p.mip_roughness[m] <= 1.0f))
@@ -539,7 +572,7 @@ int check_probe(const althea_ibl_probe& p, int i) {
                               p.irradiance_height);
     if (!r)
       r = check_image(p.irradiance_dev, p.irradiance_width, p.irradiance_height,
-                      p.irradiance_pitch_bytes, 16, "batch irradiance");
+                      p.irradiance_pitch_bytes, texel, "batch irradiance");
     if (r) return r;
   }
   return ALTHEA_IBL_OK;
@@ -566,14 +599,21 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
          params->lut_orientation != ALTHEA_IBL_LUT_CORRECTED))
       return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "lut samples/orientation");
   }
+  const bool precision = (params->flags & ALTHEA_IBL_BATCH_PRECISION) != 0;
+  const bool half = (params->flags & ALTHEA_IBL_BATCH_HALF) != 0;
+  if (half && !precision)
+    return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
+                     "RGBA16F batch outputs are produced by the precision path only");
   for (int i = 0; i < n; ++i) {
-    int r = check_probe(probes[i], i);
+    int r = check_probe(probes[i], i, half ? 8 : 16);
     if (r) return r;
   }
   althea_ibl_batch* b = new (std::nothrow) althea_ibl_batch();
   if (!b) return set_error(ALTHEA_IBL_ERR_OUT_OF_MEMORY, "host allocation");
   b->n = n;
   b->params = *params;
+  b->precision = precision;
+  b->out_format = half ? ALTHEA_IBL_FORMAT_RGBA16F : ALTHEA_IBL_FORMAT_RGBA32F;
   cudaGetDevice(&b->device);
   cudaStream_t st = (cudaStream_t)stream;
 
@@ -612,8 +652,57 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
       b->blit_level_blocks.push_back((int)blocks);
     }
   }
+  // ---- precision path: one planned tensor-core bake per probe --------------
+  if (precision) {
+    std::map<std::string, int> ws_of;
+    for (int i = 0; i < n; ++i) {
+      const althea_ibl_probe& p = probes[i];
+      althea_ibl_batch::TcProbe t;
+      t.chain = p.chain_dev;
+      t.w = p.env_width;
+      t.h = p.env_height;
+      std::ostringstream key;
+      key << p.env_width << 'x' << p.env_height;
+      for (int m = 0; m < p.mip_count; ++m) {
+        althea_ibl_mip_target mt;
+        mt.out_dev = p.mip_dev[m];
+        mt.pitch_bytes = p.mip_pitch_bytes[m];
+        mt.width = p.mip_width[m];
+        mt.height = p.mip_height[m];
+        mt.roughness = p.mip_roughness[m];
+        t.mips.push_back(mt);
+        key << ',' << mt.width << 'x' << mt.height << '@' << mt.roughness;
+      }
+      t.irr = p.irradiance_dev;
+      t.irr_w = p.irradiance_dev ? p.irradiance_width : 0;
+      t.irr_h = p.irradiance_dev ? p.irradiance_height : 0;
+      t.irr_pitch = p.irradiance_pitch_bytes;
+      key << '|' << t.irr_w << 'x' << t.irr_h;
+      auto it = ws_of.find(key.str());
+      if (it == ws_of.end()) {
+        const size_t bytes = tc_workspace_bytes(t.w, t.h, t.mips.data(), (int)t.mips.size(),
+                                                nullptr, t.irr_w, t.irr_h, -1);
+        if (bytes == 0) {
+          free_batch(b);
+          return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "probe %d: precision plan: %s", i,
+                           last_error());
+        }
+        void* ws = nullptr;
+        cudaError_t e = cudaMalloc(&ws, bytes);
+        if (e != cudaSuccess) {
+          free_batch(b);
+          return cuda_status(e, "precision workspace");
+        }
+        b->tc_ws.push_back(ws);
+        b->tc_ws_bytes.push_back(bytes);
+        it = ws_of.emplace(key.str(), (int)b->tc_ws.size() - 1).first;
+      }
+      t.ws = it->second;
+      b->tc.push_back(std::move(t));
+    }
+  }
   // ---- prefilter queue: full-sample jobs first, roughness 0 last ----------
-  for (int pass = 0; pass < 2; ++pass)
+  for (int pass = 0; pass < 2 && !precision; ++pass)
     for (int i = 0; i < n; ++i)
       for (int m = 0; m < probes[i].mip_count; ++m) {
         bool degenerate = probes[i].mip_roughness[m] == 0.0f;
@@ -679,7 +768,9 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
     }
   }
   int r = ALTHEA_IBL_OK;
-  if (have) {
+  if (precision) {
+    r = select_shape(b, 0);  // fixed tensor-core tiles: nothing to tune
+  } else if (have) {
     r = select_shape(b, cached.shape);
     if (!r) r = build_irradiance(b, probes, cached.irr_target);
     b->choice.irr_target = cached.irr_target;

@@ -33,9 +33,18 @@ int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_targ
                      int mip_count, int samples, int generator, cudaStream_t st);
 int launch_irradiance(const float* chain, int w, int h, float* out, int ow, int oh,
                       size_t pitch_bytes, void* ws, cudaStream_t st);
-// Roughness-0 mip as the single reflected sample (no Monte Carlo accumulation).
+// Roughness-0 mip as the single reflected sample (no Monte Carlo accumulation);
+// out_half: RGBA16F output (8-byte texels) instead of RGBA32F.
 int launch_delta_mip(const float* chain, int w, int h, const althea_ibl_mip_target* mip,
-                     cudaStream_t st);
+                     int out_half, cudaStream_t st);
+
+// Precision path (ibl_tc.cu): the bake behind althea_ibl_bake_tc_ex, and its
+// workspace size (0 when the plan is unsupported).
+int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
+            const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
+            int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream);
+size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n,
+                          const int* levels, int irr_w, int irr_h, int irr_level);
 int launch_brdf_lut(float* out, int n, size_t pitch_bytes, int samples, int orientation,
                     cudaStream_t st);
 

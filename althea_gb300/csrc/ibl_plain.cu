@@ -4,6 +4,7 @@
 // Compiled with -fmad=false (see ibl_device.cuh): outputs equal the CPU
 // restatement of the reference shaders bit for bit, except the irradiance sum,
 // which is split across threads (tree order instead of serial order; ~1e-7).
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -126,8 +127,9 @@ __global__ void __launch_bounds__(kPfTileX* kPfTileY) prefilter_kernel(const Pre
 // Hammersley point), without repeating its accumulation.  The precision path
 // uses it for roughness-0 mips (its quadrature of a delta).
 __global__ void __launch_bounds__(256) delta_mip_kernel(const float4* __restrict__ chain, int w,
-                                                        int h, float4* __restrict__ out,
-                                                        long long pitch, int ow, int oh) {
+                                                        int h, void* __restrict__ out,
+                                                        long long pitch, int ow, int oh,
+                                                        int out_half) {
   __shared__ ChainTable tab;
   if (threadIdx.x == 0) make_table(w, h, &tab);
   __syncthreads();
@@ -147,16 +149,24 @@ __global__ void __launch_bounds__(256) delta_mip_kernel(const float4* __restrict
     Float3 c = sample_env(chain, tab, l, 0.0f);
     o = make_float4(c.x, c.y, c.z, 1.0f);
   }
-  out[(long long)y * pitch + x] = o;
+  if (out_half) {
+    const __half2 rg = __floats2half2_rn(o.x, o.y), ba = __floats2half2_rn(o.z, o.w);
+    uint2 v;
+    v.x = *reinterpret_cast<const uint32_t*>(&rg);
+    v.y = *reinterpret_cast<const uint32_t*>(&ba);
+    reinterpret_cast<uint2*>(out)[(long long)y * pitch + x] = v;
+  } else {
+    reinterpret_cast<float4*>(out)[(long long)y * pitch + x] = o;
+  }
 }
 
 int launch_delta_mip(const float* chain, int w, int h, const althea_ibl_mip_target* mip,
-                     cudaStream_t st) {
+                     int out_half, cudaStream_t st) {
   dim3 grid((mip->width + 31) / 32, (mip->height + 7) / 8);
   delta_mip_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const float4*>(chain), w, h,
-                                         reinterpret_cast<float4*>(mip->out_dev),
-                                         (long long)(mip->pitch_bytes / sizeof(float4)),
-                                         mip->width, mip->height);
+                                         mip->out_dev,
+                                         (long long)(mip->pitch_bytes / (out_half ? 8 : 16)),
+                                         mip->width, mip->height, out_half);
   return cuda_status(cudaGetLastError(), "delta mip launch");
 }
 

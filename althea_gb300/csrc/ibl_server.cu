@@ -12,8 +12,9 @@
 // would synchronise the device); free blocks of other sizes are released only
 // when a new size class would otherwise exceed the budget.
 //
-// Host code only; the kernels are the single-probe ones (ibl_plain.cu), whose
-// results do not depend on what else runs on the device.
+// Host code only; the kernels are the single-probe ones (ibl_plain.cu, or
+// ibl_tc.cu when the server runs the precision path), whose results do not
+// depend on what else runs on the device.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -41,6 +42,19 @@ struct Layout {
   int mip_w[ALTHEA_IBL_MAX_MIPS], mip_h[ALTHEA_IBL_MAX_MIPS];
 };
 
+// Mip targets of a request (mips from W/2 x H/2, roughness m/(M-1)) inside a block.
+void mip_targets(const Layout& L, char* base, int mips, althea_ibl_mip_target* out) {
+  size_t off = L.mips_off;
+  for (int m = 0; m < mips; ++m) {
+    out[m].out_dev = base ? reinterpret_cast<float*>(base + off) : nullptr;
+    out[m].pitch_bytes = (size_t)L.mip_w[m] * 16;
+    out[m].width = L.mip_w[m];
+    out[m].height = L.mip_h[m];
+    out[m].roughness = mips > 1 ? (float)m / (float)(mips - 1) : 0.0f;
+    off += (size_t)L.mip_w[m] * L.mip_h[m] * 16;
+  }
+}
+
 struct Slot {
   cudaStream_t stream = nullptr;
   bool busy = false;
@@ -50,6 +64,7 @@ struct Slot {
   void* block = nullptr;
   size_t bytes = 0;
   int status = ALTHEA_IBL_OK;
+  int env_width = 0, env_height = 0, mip_count = 0;  // shape of the request in flight
 };
 
 struct Pending {
@@ -96,7 +111,19 @@ Layout layout_for(const althea_ibl_server* s, int w, int h, int mips) {
   L.irr_bytes = (size_t)s->cfg.irradiance_width * s->cfg.irradiance_height * 16;
   off = align256(off + L.irr_bytes);
   L.ws_off = off;
-  L.ws_bytes = ibl::irr_plan(w, h, s->cfg.irradiance_width, s->cfg.irradiance_height).workspace;
+  if (s->cfg.path == ALTHEA_IBL_PATH_PRECISION) {
+    althea_ibl_mip_target mt[ALTHEA_IBL_MAX_MIPS];
+    mip_targets(L, nullptr, mips, mt);
+    L.ws_bytes = ibl::tc_workspace_bytes(w, h, mt, mips, nullptr, s->cfg.irradiance_width,
+                                         s->cfg.irradiance_height, -1);
+    if (L.ws_bytes == 0) {  // unsupported shape: can never be admitted
+      L.total = (size_t)-1;
+      return L;
+    }
+  } else {
+    L.ws_bytes =
+        ibl::irr_plan(w, h, s->cfg.irradiance_width, s->cfg.irradiance_height).workspace;
+  }
   off = align256(off + L.ws_bytes);
   L.total = off;
   return L;
@@ -155,23 +182,25 @@ int start(althea_ibl_server* s, Slot* slot, const Pending& pend, const Layout& L
   if (e != cudaSuccess) status = ibl::cuda_status(e, "server env upload");
   if (!status) status = ibl::launch_build_chain(chain, r.env_width, r.env_height, chain, st);
   althea_ibl_mip_target mips[ALTHEA_IBL_MAX_MIPS];
-  size_t off = L.mips_off;
-  for (int m = 0; m < r.mip_count; ++m) {
-    mips[m].out_dev = reinterpret_cast<float*>(base + off);
-    mips[m].pitch_bytes = (size_t)L.mip_w[m] * 16;
-    mips[m].width = L.mip_w[m];
-    mips[m].height = L.mip_h[m];
-    mips[m].roughness = r.mip_count > 1 ? (float)m / (float)(r.mip_count - 1) : 0.0f;
-    off += (size_t)L.mip_w[m] * L.mip_h[m] * 16;
+  mip_targets(L, base, r.mip_count, mips);
+  if (s->cfg.path == ALTHEA_IBL_PATH_PRECISION) {
+    if (!status)
+      status = ibl::tc_bake(chain, r.env_width, r.env_height, mips, r.mip_count, nullptr,
+                            r.irradiance_host ? reinterpret_cast<float*>(base + L.irr_off)
+                                              : nullptr,
+                            s->cfg.irradiance_width, s->cfg.irradiance_height,
+                            (size_t)s->cfg.irradiance_width * 16, -1, base + L.ws_off,
+                            L.ws_bytes, ALTHEA_IBL_FORMAT_RGBA32F, st);
+  } else {
+    if (!status)
+      status = ibl::launch_prefilter(chain, r.env_width, r.env_height, mips, r.mip_count,
+                                     s->cfg.samples, s->cfg.generator, st);
+    if (!status && r.irradiance_host)
+      status = ibl::launch_irradiance(chain, r.env_width, r.env_height,
+                                      reinterpret_cast<float*>(base + L.irr_off),
+                                      s->cfg.irradiance_width, s->cfg.irradiance_height,
+                                      (size_t)s->cfg.irradiance_width * 16, base + L.ws_off, st);
   }
-  if (!status)
-    status = ibl::launch_prefilter(chain, r.env_width, r.env_height, mips, r.mip_count,
-                                   s->cfg.samples, s->cfg.generator, st);
-  if (!status && r.irradiance_host)
-    status = ibl::launch_irradiance(chain, r.env_width, r.env_height,
-                                    reinterpret_cast<float*>(base + L.irr_off),
-                                    s->cfg.irradiance_width, s->cfg.irradiance_height,
-                                    (size_t)s->cfg.irradiance_width * 16, base + L.ws_off, st);
   if (!status && r.mips_host && L.mips_bytes) {
     e = cudaMemcpyAsync(r.mips_host, base + L.mips_off, L.mips_bytes, cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) status = ibl::cuda_status(e, "server mips download");
@@ -222,6 +251,9 @@ void admit(althea_ibl_server* s) {
     free_slot->info.tag = head.req.tag;
     free_slot->info.submit_s = head.submit_s;
     free_slot->info.start_s = now_s();
+    free_slot->env_width = head.req.env_width;
+    free_slot->env_height = head.req.env_height;
+    free_slot->mip_count = head.req.mip_count;
     start(s, free_slot, head, L);
     s->queue.pop_front();
   }
@@ -233,6 +265,16 @@ void retire(althea_ibl_server* s) {
     althea_ibl_completion c = sl->info;
     c.done_s = sl->done_s;
     c.status = sl->status;
+    if (s->cfg.path == ALTHEA_IBL_PATH_PRECISION && c.status == ALTHEA_IBL_OK) {
+      // the precision kernels' bounded waits report through the workspace's
+      // first word; the slot's stream has finished, so this read is immediate
+      int flag = 0;
+      Layout L = layout_for(s, sl->env_width, sl->env_height, sl->mip_count);
+      if (cudaMemcpyAsync(&flag, static_cast<char*>(sl->block) + L.ws_off, sizeof(int),
+                          cudaMemcpyDeviceToHost, sl->stream) != cudaSuccess ||
+          cudaStreamSynchronize(sl->stream) != cudaSuccess || flag)
+        c.status = ALTHEA_IBL_ERR_CUDA;
+    }
     s->finished.push_back(c);
     pool_release(s, sl->block, sl->bytes);
     sl->block = nullptr;
@@ -264,7 +306,8 @@ extern "C" int althea_ibl_server_create(const althea_ibl_server_config* cfg,
   if (cfg->max_inflight < 1 || cfg->max_inflight > 256 || cfg->budget_bytes == 0 ||
       cfg->samples < 1 || cfg->samples > (1 << 24) ||
       (cfg->generator != ALTHEA_IBL_GEN_REF_HASH && cfg->generator != ALTHEA_IBL_GEN_HAMMERSLEY) ||
-      cfg->irradiance_width < 1 || cfg->irradiance_height < 1)
+      cfg->irradiance_width < 1 || cfg->irradiance_height < 1 ||
+      (cfg->path != ALTHEA_IBL_PATH_PLAIN && cfg->path != ALTHEA_IBL_PATH_PRECISION))
     return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "server config");
   althea_ibl_server* s = new (std::nothrow) althea_ibl_server();
   if (!s) return ibl::set_error(ALTHEA_IBL_ERR_OUT_OF_MEMORY, "host allocation");

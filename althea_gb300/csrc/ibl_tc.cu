@@ -52,6 +52,7 @@
 // 1e6-bright suns need no scaling.  The weight sum of each output row is
 // taken in FP64 (FP32 within one source phase row) by the producers.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -277,6 +278,7 @@ struct Job {
   float* partial;            // [ksplit][3][wo][ho]
   double* wsum_part;         // [ksplit][ho]  (kind 0)
   int* error;                // set when a bounded wait gave up
+  int out_half;              // 1: outputs are RGBA16F (8-byte texels), else RGBA32F
 };
 
 struct SmemPlan {
@@ -661,7 +663,7 @@ __global__ void rows_kernel(const float4* __restrict__ src, int ws, int hs, int 
 // splits k = w mod 8 with the lanes on consecutive rows (the partial layout),
 // then warp 0 combines the eight in order.  FP64 is used only for the weight
 // sums and the final normalisation.
-__global__ void __launch_bounds__(256) finish_kernel(const Job job, float4* __restrict__ out,
+__global__ void __launch_bounds__(256) finish_kernel(const Job job, void* __restrict__ out,
                                                      long long pitch) {
   __shared__ float red[8][3][32];
   __shared__ double redw[8][32];
@@ -694,8 +696,16 @@ __global__ void __launch_bounds__(256) finish_kernel(const Job job, float4* __re
       tw += redw[ww][lane];
     }
     const double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / tw);
-    out[(long long)i * pitch + x] =
-        make_float4((float)(t0 * norm), (float)(t1 * norm), (float)(t2 * norm), 1.0f);
+    const float r = (float)(t0 * norm), g = (float)(t1 * norm), b = (float)(t2 * norm);
+    if (job.out_half) {
+      const __half2 rg = __floats2half2_rn(r, g), ba = __floats2half2_rn(b, 1.0f);
+      uint2 v;
+      v.x = *reinterpret_cast<const uint32_t*>(&rg);
+      v.y = *reinterpret_cast<const uint32_t*>(&ba);
+      reinterpret_cast<uint2*>(out)[(long long)i * pitch + x] = v;
+    } else {
+      reinterpret_cast<float4*>(out)[(long long)i * pitch + x] = make_float4(r, g, b, 1.0f);
+    }
   }
 }
 
@@ -882,10 +892,7 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
 extern "C" size_t althea_ibl_tc_workspace_size(int w, int h, const althea_ibl_mip_target* mips,
                                                int n, const int* levels, int irr_w, int irr_h,
                                                int irr_level) {
-  if (check_env(w, h)) return 0;
-  TcPlan P;
-  if (make_plan(w, h, mips, n, levels, irr_w, irr_h, irr_level, P)) return 0;
-  return P.total;
+  return tc_workspace_bytes(w, h, mips, n, levels, irr_w, irr_h, irr_level);
 }
 
 extern "C" int althea_ibl_tc_plan(int w, int h, const althea_ibl_mip_target* mips, int n,
@@ -899,21 +906,27 @@ extern "C" int althea_ibl_tc_plan(int w, int h, const althea_ibl_mip_target* mip
   return ALTHEA_IBL_OK;
 }
 
-extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
-                                  const althea_ibl_mip_target* mips, int n, const int* levels,
-                                  float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
-                                  int irr_level, void* ws, size_t ws_bytes, void* stream) {
+namespace ibl {
+
+int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
+            const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
+            int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream) {
   int st = check_env(w, h);
   if (st) return st;
+  if (out_format != ALTHEA_IBL_FORMAT_RGBA32F && out_format != ALTHEA_IBL_FORMAT_RGBA16F)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "tensor path: output format %d",
+                     out_format);
+  const int out_half = out_format == ALTHEA_IBL_FORMAT_RGBA16F;
+  const size_t texel = out_half ? 8 : 16;
   if (!chain || ((uintptr_t)chain) % 16 || n < 0 || n > ALTHEA_IBL_MAX_MIPS || (n && !mips))
     return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "tensor path: chain/mips");
   for (int m = 0; m < n; ++m) {
-    st = check_image(mips[m].out_dev, mips[m].width, mips[m].height, mips[m].pitch_bytes, 16,
+    st = check_image(mips[m].out_dev, mips[m].width, mips[m].height, mips[m].pitch_bytes, texel,
                      "tc mip");
     if (st) return st;
   }
   if (irr_out) {
-    st = check_image(irr_out, irr_w, irr_h, irr_pitch, 16, "tc irradiance");
+    st = check_image(irr_out, irr_w, irr_h, irr_pitch, texel, "tc irradiance");
     if (st) return st;
   }
   TcPlan P;
@@ -922,7 +935,7 @@ extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
   if (!ws || ws_bytes < P.total || ((uintptr_t)ws) % 256)
     return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
                      "tensor path workspace needs %zu bytes (256-byte aligned)", P.total);
-  cudaStream_t s = (cudaStream_t)stream;
+  cudaStream_t s = stream;
   char* base = static_cast<char*>(ws);
   cudaError_t e = cudaMemsetAsync(base, 0, 256, s);
   if (e != cudaSuccess) return cuda_status(e, "tc error flag");
@@ -971,6 +984,7 @@ extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
     J.partial = reinterpret_cast<float*>(base + jp.partial_off);
     J.wsum_part = reinterpret_cast<double*>(base + jp.wsum_off);
     J.error = reinterpret_cast<int*>(base);
+    J.out_half = out_half;
     // At least 120 KB so no two CTAs share an SM (each allocates all of TMEM).
     int smem = (int)smem_plan(J).total;
     if (smem < 120 * 1024) smem = 120 * 1024;
@@ -986,24 +1000,51 @@ extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
       if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
       contract_kernel<1><<<grid, kThreads, smem, s>>>(J);
     }
-    float4* out;
+    void* out;
     long long pitch;
     if ((int)k < n) {
-      out = reinterpret_cast<float4*>(mips[k].out_dev);
-      pitch = (long long)(mips[k].pitch_bytes / 16);
+      out = mips[k].out_dev;
+      pitch = (long long)(mips[k].pitch_bytes / texel);
     } else {
-      out = reinterpret_cast<float4*>(irr_out);
-      pitch = (long long)(irr_pitch / 16);
+      out = irr_out;
+      pitch = (long long)(irr_pitch / texel);
     }
     finish_kernel<<<dim3((J.ho + 31) / 32, J.wo), 256, 0, s>>>(J, out, pitch);
   }
   // Roughness-0 mips are a delta (no contraction): the reflected sample itself.
   for (int m = 0; m < n; ++m) {
     if (P.jobs[m].level >= 0) continue;
-    st = launch_delta_mip(chain, w, h, &mips[m], s);
+    st = launch_delta_mip(chain, w, h, &mips[m], out_half, s);
     if (st) return st;
   }
   return cuda_status(cudaGetLastError(), "tensor path launch");
+}
+
+size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n,
+                          const int* levels, int irr_w, int irr_h, int irr_level) {
+  if (check_env(w, h)) return 0;
+  TcPlan P;
+  if (make_plan(w, h, mips, n, levels, irr_w, irr_h, irr_level, P)) return 0;
+  return P.total;
+}
+
+}  // namespace ibl
+
+extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
+                                  const althea_ibl_mip_target* mips, int n, const int* levels,
+                                  float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
+                                  int irr_level, void* ws, size_t ws_bytes, void* stream) {
+  return tc_bake(chain, w, h, mips, n, levels, irr_out, irr_w, irr_h, irr_pitch, irr_level, ws,
+                 ws_bytes, ALTHEA_IBL_FORMAT_RGBA32F, (cudaStream_t)stream);
+}
+
+extern "C" int althea_ibl_bake_tc_ex(const float* chain, int w, int h,
+                                     const althea_ibl_mip_target* mips, int n, const int* levels,
+                                     void* irr_out, int irr_w, int irr_h, size_t irr_pitch,
+                                     int irr_level, void* ws, size_t ws_bytes, int out_format,
+                                     void* stream) {
+  return tc_bake(chain, w, h, mips, n, levels, static_cast<float*>(irr_out), irr_w, irr_h,
+                 irr_pitch, irr_level, ws, ws_bytes, out_format, (cudaStream_t)stream);
 }
 
 extern "C" int althea_ibl_tc_error(const void* ws, void* stream) {

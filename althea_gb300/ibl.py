@@ -89,12 +89,19 @@ class BatchInfo(ctypes.Structure):
 
 BATCH_AUTOTUNE = 1
 BATCH_GRAPH = 2
+BATCH_PRECISION = 4
+BATCH_HALF = 8
+PATH_PLAIN = 0
+PATH_PRECISION = 1
+FORMAT_RGBA32F = 0
+FORMAT_RGBA16F = 1
 
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("budget_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int),
                 ("samples", ctypes.c_int), ("generator", ctypes.c_int),
-                ("irradiance_width", ctypes.c_int), ("irradiance_height", ctypes.c_int)]
+                ("irradiance_width", ctypes.c_int), ("irradiance_height", ctypes.c_int),
+                ("path", ctypes.c_int)]
 
 
 class Request(ctypes.Structure):
@@ -173,6 +180,8 @@ def load(build_if_missing: bool = True):
         "althea_ibl_bake_tc": (i, [vp, i, i, ctypes.POINTER(MipTarget), i, ctypes.POINTER(i),
                                    vp, i, i, sz, i, vp, sz, vp]),
         "althea_ibl_tc_error": (i, [vp, vp]),
+        "althea_ibl_bake_tc_ex": (i, [vp, i, i, ctypes.POINTER(MipTarget), i, ctypes.POINTER(i),
+                                      vp, i, i, sz, i, vp, sz, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -199,18 +208,19 @@ def _stream_ptr(stream) -> Optional[int]:
     return s.cuda_stream
 
 
-def _require_cuda(t, name, ncomp):
+def _require_cuda(t, name, ncomp, allow_half=False):
     torch = _torch()
     if not isinstance(t, torch.Tensor) or not t.is_cuda:
         raise IBLError(ERR_INVALID_ARGUMENT, f"{name} must be a CUDA tensor")
-    if t.dtype != torch.float32:
-        raise IBLError(ERR_INVALID_ARGUMENT, f"{name} must be float32")
+    if t.dtype != torch.float32 and not (allow_half and t.dtype == torch.float16):
+        raise IBLError(ERR_INVALID_ARGUMENT,
+                       f"{name} must be float32" + (" or float16" if allow_half else ""))
     if t.dim() != 3 or t.shape[2] != ncomp or t.stride(2) != 1 or t.stride(1) != ncomp:
         raise IBLError(ERR_INVALID_ARGUMENT, f"{name} must be (H, W, {ncomp}) with packed texels")
 
 
 def _pitch(t, ncomp) -> int:
-    return t.stride(0) * 4
+    return t.stride(0) * t.element_size()
 
 
 # ---- stateless kernels -------------------------------------------------------
@@ -501,9 +511,12 @@ class ProbeBatch:
     def __init__(self, specs: List[ProbeSpec], levels0: List, samples: int = 1024,
                  generator: int = GEN_HAMMERSLEY, lut_size: int = 0, lut_samples: int = 1024,
                  lut_orientation: int = LUT_ASSET, autotune: bool = True, graph: bool = True,
-                 stream=None, device="cuda"):
+                 stream=None, device="cuda", precision: bool = False, half: bool = False):
         torch = _torch()
         self.specs = specs
+        # precision: mips and irradiance by the tensor-core path; half: RGBA16F outputs
+        out_dtype = torch.float16 if half else torch.float32
+        texel = 8 if half else 16
         self.levels0 = levels0
         self.chains, self.mips, self.irradiance = [], [], []
         n = len(specs)
@@ -514,12 +527,12 @@ class ProbeBatch:
                 raise IBLError(ERR_INVALID_ARGUMENT, f"env {i} shape {tuple(env.shape)}")
             chain = torch.empty((chain_texels(s.env_width, s.env_height), 4),
                                 dtype=torch.float32, device=device)
-            mips = [torch.empty((h, w, 4), dtype=torch.float32, device=device)
+            mips = [torch.empty((h, w, 4), dtype=out_dtype, device=device)
                     for w, h in s.mip_sizes]
             irr = None
             if s.irradiance_size is not None:
                 iw, ih = s.irradiance_size
-                irr = torch.empty((ih, iw, 4), dtype=torch.float32, device=device)
+                irr = torch.empty((ih, iw, 4), dtype=out_dtype, device=device)
             self.chains.append(chain)
             self.mips.append(mips)
             self.irradiance.append(irr)
@@ -530,11 +543,11 @@ class ProbeBatch:
             if irr is not None:
                 p.irradiance_dev = irr.data_ptr()
                 p.irradiance_width, p.irradiance_height = s.irradiance_size
-                p.irradiance_pitch_bytes = _pitch(irr, 4)
+                p.irradiance_pitch_bytes = irr.stride(0) * irr.element_size()
             p.mip_count = len(mips)
             for m, (t, r) in enumerate(zip(mips, s.roughness)):
                 p.mip_dev[m] = t.data_ptr()
-                p.mip_pitch_bytes[m] = _pitch(t, 4)
+                p.mip_pitch_bytes[m] = t.stride(0) * t.element_size()
                 p.mip_width[m], p.mip_height[m] = t.shape[1], t.shape[0]
                 p.mip_roughness[m] = float(r)
         self.lut = None
@@ -545,7 +558,9 @@ class ProbeBatch:
             params.lut_dev, params.lut_size = self.lut.data_ptr(), lut_size
             params.lut_pitch_bytes = _pitch(self.lut, 2)
             params.lut_samples, params.lut_orientation = lut_samples, lut_orientation
-        params.flags = (BATCH_AUTOTUNE if autotune else 0) | (BATCH_GRAPH if graph else 0)
+        params.flags = ((BATCH_AUTOTUNE if autotune else 0) | (BATCH_GRAPH if graph else 0) |
+                        (BATCH_PRECISION if precision else 0) | (BATCH_HALF if half else 0))
+        del texel
         self._plan = ctypes.c_void_p()
         _check(load().althea_ibl_batch_create(self._probes, n, ctypes.byref(params),
                                               _stream_ptr(stream), ctypes.byref(self._plan)))
@@ -589,12 +604,17 @@ def tc_plan(w: int, h: int, mip_sizes: List[tuple], roughness: List[float],
 def bake_tc(chain, w: int, h: int, outs: List, roughness: List[float], irradiance=None,
             levels: Optional[List[int]] = None, irradiance_level: int = -1, workspace=None,
             stream=None, check: bool = True):
-    """Precision-path bake into CUDA tensors (mips and optional irradiance)."""
+    """Precision-path bake into CUDA tensors (mips and optional irradiance):
+    float32 outputs are RGBA32F, float16 outputs RGBA16F (all of one type)."""
     torch = _torch()
     n = len(outs)
     arr = (MipTarget * max(n, 1))()
+    all_out = list(outs) + ([irradiance] if irradiance is not None else [])
+    half = bool(all_out) and all_out[0].dtype == torch.float16
+    if any((t.dtype == torch.float16) != half for t in all_out):
+        raise IBLError(ERR_INVALID_ARGUMENT, "precision outputs must all be float32 or float16")
     for k, (o, r) in enumerate(zip(outs, roughness)):
-        _require_cuda(o, f"mip {k}", 4)
+        _require_cuda(o, f"mip {k}", 4, allow_half=True)
         arr[k] = MipTarget(o.data_ptr(), _pitch(o, 4), o.shape[1], o.shape[0], float(r))
     lv = None
     if levels is not None:
@@ -603,7 +623,7 @@ def bake_tc(chain, w: int, h: int, outs: List, roughness: List[float], irradianc
     ip = 0
     ipitch = 0
     if irradiance is not None:
-        _require_cuda(irradiance, "irradiance", 4)
+        _require_cuda(irradiance, "irradiance", 4, allow_half=True)
         ih, iw = irradiance.shape[:2]
         ip, ipitch = irradiance.data_ptr(), _pitch(irradiance, 4)
     L = load()
@@ -613,8 +633,9 @@ def bake_tc(chain, w: int, h: int, outs: List, roughness: List[float], irradianc
     if workspace is None or workspace.numel() < need:
         workspace = torch.empty(need, dtype=torch.uint8, device=chain.device)
     sp = _stream_ptr(stream)
-    _check(L.althea_ibl_bake_tc(chain.data_ptr(), w, h, arr, n, lv, ip, iw, ih, ipitch,
-                                irradiance_level, workspace.data_ptr(), need, sp))
+    _check(L.althea_ibl_bake_tc_ex(chain.data_ptr(), w, h, arr, n, lv, ip, iw, ih, ipitch,
+                                   irradiance_level, workspace.data_ptr(), need,
+                                   FORMAT_RGBA16F if half else FORMAT_RGBA32F, sp))
     if check:
         _check(L.althea_ibl_tc_error(workspace.data_ptr(), sp))
     return workspace

@@ -33,9 +33,10 @@ def mip_sizes_for(w: int, h: int, mip_count: int) -> List[tuple]:
 
 class ProbeServer:
     def __init__(self, budget_bytes: int, max_inflight: int = 8, samples: int = 1024,
-                 generator: int = ibl.GEN_HAMMERSLEY, irradiance_size=(32, 16)):
+                 generator: int = ibl.GEN_HAMMERSLEY, irradiance_size=(32, 16),
+                 path: int = ibl.PATH_PLAIN):
         self.cfg = ibl.ServerConfig(budget_bytes, max_inflight, samples, generator,
-                                    irradiance_size[0], irradiance_size[1])
+                                    irradiance_size[0], irradiance_size[1], path)
         self.irradiance_size = irradiance_size
         self._s = ctypes.c_void_p()
         ibl._check(ibl.load().althea_ibl_server_create(ctypes.byref(self.cfg),

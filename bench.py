@@ -646,12 +646,15 @@ def run_batch(args):
     from althea_gb300 import ibl, synth
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
+    precision = args.path == "tc"
     specs = batch_specs(args.batch, seed=rank)
-    envs = [torch.from_numpy(synth.make_env(s.env_width, s.env_height, seed=1000 * rank + i))
+    envs = [torch.from_numpy(synth.make_env(s.env_width, s.env_height, seed=1000 * rank + i,
+                                            sun_max=args.sun_max if precision else 1e4))
             .cuda() for i, s in enumerate(specs)]
     stream = torch.cuda.Stream()
     batch = ibl.ProbeBatch(specs, envs, samples=SAMPLES, generator=GENERATOR, lut_size=256,
-                           lut_samples=LUT_SAMPLES, autotune=True, graph=True, stream=stream)
+                           lut_samples=LUT_SAMPLES, autotune=True, graph=True, stream=stream,
+                           precision=precision, half=precision)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -676,21 +679,25 @@ def run_batch(args):
     widths = {}
     for s in specs:
         widths[s.env_width] = widths.get(s.env_width, 0) + 1
+    path_desc = ("precision path (BF16 hi/lo tcgen05 contractions, RGBA16F outputs)" if precision
+                 else f"plain path FP32, N=1024 {'Hammersley' if GENERATOR else 'reference-hash'}")
     line = {"metric": METRIC, "value": args.batch / (ms / 1e3), "unit": "probes/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 hi/lo (fp32 accumulate)" if precision else "f32",
             "data": "synthetic", "config": {
                 "workload": f"batch of {args.batch} probes (widths {dict(sorted(widths.items()))}"
                             f", 2:1, log2(W)-3 mips from W/2, 32x16 irradiance, shared 256x256 "
-                            f"LUT, N=1024 {'Hammersley' if GENERATOR else 'reference-hash'}), "
-                            "plain path FP32, one CUDA-graph launch per step",
+                            f"LUT), {path_desc}, one CUDA-graph launch per step",
+                "path": "tensor" if precision else "plain",
                 "tile": [info.tile_x, info.tile_y], "persistent_blocks": info.persistent_blocks,
                 "irradiance_target_blocks": info.irradiance_target_blocks,
                 "l2": "flushed (256 MB write) between timed steps"},
             "gpu_launches": None,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": "whole batch graph", "peak_source": peak_kind},
+            "roofline": None if precision else {
+                "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "kernel": "whole batch graph",
+                "peak_source": peak_kind},
             "clocks": clk.summary()}
     if rank == 0:
         print(json.dumps(line))
@@ -706,14 +713,18 @@ def run_serve(args):
     world, rank, local = dist_setup()
     import torch
     torch.cuda.set_device(local)
+    from althea_gb300 import ibl
+    precision = args.path == "tc"
     server = serving.ProbeServer(budget_bytes=int(args.budget_gb * (1 << 30)),
                                  max_inflight=args.inflight, samples=SAMPLES,
-                                 generator=GENERATOR, irradiance_size=(32, 16))
+                                 generator=GENERATOR, irradiance_size=(32, 16),
+                                 path=ibl.PATH_PRECISION if precision else ibl.PATH_PLAIN)
     rng = np.random.default_rng(rank)
     pool = []
     for k in range(args.pool):
         w = int(rng.choice([256, 512, 1024, 2048]))
-        env = synth.make_env(w, w // 2, seed=5000 + 100 * rank + k)
+        env = synth.make_env(w, w // 2, seed=5000 + 100 * rank + k,
+                             sun_max=args.sun_max if precision else 1e4)
         pool.append(server.buffers(env, max(1, w.bit_length() - 1 - 3)))
     serving.run_poisson(server, pool, rate=200.0, n_requests=min(64, 4 * len(pool)), seed=1)
     rows = []
@@ -730,7 +741,7 @@ def run_serve(args):
                                    f"N=1024, {args.inflight} slots, {args.budget_gb} GB budget, "
                                    f"{args.pool} pre-generated maps (suns re-seeded per map), "
                                    "latency = completion callback - arrival, host pinned I/O",
-                       "path": "plain"},
+                       "path": "tensor" if precision else "plain"},
             "serving": rows}
     if rank == 0:
         print(json.dumps(line))

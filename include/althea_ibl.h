@@ -197,6 +197,18 @@ int althea_ibl_bake_tc(const float* chain_dev, int env_width, int env_height,
                        size_t workspace_bytes, void* stream);
 int althea_ibl_tc_error(const void* workspace_dev, void* stream);
 
+/* Output formats of althea_ibl_bake_tc_ex (every mip and the irradiance). */
+#define ALTHEA_IBL_FORMAT_RGBA32F 0   /* 16-byte texels, as althea_ibl_bake_tc */
+#define ALTHEA_IBL_FORMAT_RGBA16F 1   /* 8-byte texels (IEEE half), alpha 1 */
+/* althea_ibl_bake_tc with the output format chosen: the images the renderer
+ * binds as VK_FORMAT_R16G16B16A16_SFLOAT (the mips' out_dev and
+ * irradiance_dev then point to RGBA16F texels; pitches in bytes). */
+int althea_ibl_bake_tc_ex(const float* chain_dev, int env_width, int env_height,
+                          const althea_ibl_mip_target* mips, int mip_count, const int* levels,
+                          void* irradiance_dev, int irradiance_width, int irradiance_height,
+                          size_t irradiance_pitch_bytes, int irradiance_level, void* workspace_dev,
+                          size_t workspace_bytes, int out_format, void* stream);
+
 /* ---- batched bakes -----------------------------------------------------------
  * No single counterpart in the reference, which bakes one probe per
  * createResources call (Src/GlobalResources.cpp:18-22); a batch bakes many
@@ -224,6 +236,11 @@ typedef struct {
 
 #define ALTHEA_IBL_BATCH_AUTOTUNE 1
 #define ALTHEA_IBL_BATCH_GRAPH 2
+/* Mips and irradiance by the precision path (althea_ibl_bake_tc_ex per probe
+ * after the shared chain pass; probes of one shape share a workspace). */
+#define ALTHEA_IBL_BATCH_PRECISION 4
+/* With ALTHEA_IBL_BATCH_PRECISION: RGBA16F outputs (8-byte texels). */
+#define ALTHEA_IBL_BATCH_HALF 8
 
 typedef struct {
   int samples;
@@ -267,11 +284,16 @@ int althea_ibl_batch_destroy(althea_ibl_batch* batch);
  * cudaFree on the request path).  Results are identical whether a request runs
  * alone or among others (the kernels are deterministic and independent of
  * concurrency).  The API is single-threaded: call submit/poll from one thread. */
+#define ALTHEA_IBL_PATH_PLAIN 0       /* the reference estimator */
+#define ALTHEA_IBL_PATH_PRECISION 1   /* tensor-core contraction, <= 1e-3 vs FP64 */
+
 typedef struct {
   size_t budget_bytes;       /* device memory the server may hold */
   int max_inflight;          /* requests on the GPU at once (streams) */
-  int samples, generator;    /* prefilter sample count and generator */
+  int samples, generator;    /* prefilter sample count and generator (plain path) */
   int irradiance_width, irradiance_height;
+  int path;                  /* ALTHEA_IBL_PATH_*; the precision workspace counts against
+                                the budget */
 } althea_ibl_server_config;
 
 typedef struct {

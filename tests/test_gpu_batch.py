@@ -80,3 +80,47 @@ def test_autotune_choice_is_cached_per_shape():
         (ib.tile_x, ib.tile_y, ib.irradiance_target_blocks)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("half", [False, True])
+def test_precision_batch_equals_probes_alone(half):
+    """The precision path in a batch (one graph, shared workspaces per shape)
+    gives every probe exactly its solo tensor-core bake; RGBA16F outputs are
+    the RGBA32F results rounded to half."""
+    sizes = [(256, 128), (64, 32), (256, 128), (128, 64), (512, 256)]
+    specs = [ibl.spec_for(w, h) for w, h in sizes]
+    specs[3].irradiance_size = None
+    envs = [torch.from_numpy(synth.make_env(w, h, seed=60 + i, sun_max=1e6)).cuda()
+            for i, (w, h) in enumerate(sizes)]
+    stream = torch.cuda.Stream()
+    batch = ibl.ProbeBatch(specs, envs, lut_size=64, lut_samples=128, graph=True, stream=stream,
+                           precision=True, half=half)
+    for _ in range(2):  # the second run replays the graph
+        batch.run(stream)
+    stream.synchronize()
+    assert batch.info().graph == 1
+    for i, (s, env) in enumerate(zip(specs, envs)):
+        chain = ibl.build_env_chain(env)
+        mips = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+                for w, h in s.mip_sizes]
+        irr = None
+        if s.irradiance_size is not None:
+            iw, ih = s.irradiance_size
+            irr = torch.empty((ih, iw, 4), dtype=torch.float32, device="cuda")
+        ibl.bake_tc(chain, s.env_width, s.env_height, mips, s.roughness, irradiance=irr)
+        torch.cuda.synchronize()
+        assert torch.equal(batch.chains[i], chain), i
+        for m in range(len(mips)):
+            want = mips[m].half() if half else mips[m]
+            assert batch.mips[i][m].dtype == want.dtype
+            assert torch.equal(batch.mips[i][m], want), (i, m)
+        if irr is not None:
+            assert torch.equal(batch.irradiance[i], irr.half() if half else irr), i
+    batch.close()
+
+
+def test_half_outputs_need_the_precision_path():
+    spec = ibl.spec_for(64, 32)
+    env = torch.from_numpy(synth.make_env(64, 32, seed=3)).cuda()
+    with pytest.raises(ibl.IBLError):
+        ibl.ProbeBatch([spec], [env], half=True)

@@ -77,3 +77,38 @@ def test_poisson_run_reports_latency():
     r = serving.run_poisson(server, pool, rate=500.0, n_requests=64, seed=3)
     assert r["ok"] == 64 and r["p99_ms"] >= r["p50_ms"] > 0
     server.close()
+
+
+def test_precision_server_alone_equals_mixed_and_solo_bake():
+    """Requests on the precision path: the same alone, in the mix, and as the
+    stateless tensor-core bake of the same map."""
+    sizes = [256, 128, 512, 256, 64]
+    alone = serving.ProbeServer(budget_bytes=1 << 31, max_inflight=1, path=ibl.PATH_PRECISION)
+    mixed = serving.ProbeServer(budget_bytes=1 << 31, max_inflight=8, path=ibl.PATH_PRECISION)
+    pa = _pool(alone, sizes, 300)
+    pm = _pool(mixed, sizes, 300)
+    for i, b in enumerate(pa):
+        alone.submit(i, b)
+        alone.drain()
+    for i, b in enumerate(pm):
+        mixed.submit(i, b)
+    comps = mixed.drain()
+    assert sorted(c.tag for c in comps) == list(range(len(sizes)))
+    assert all(c.status == ibl.OK for c in comps)
+    for a, m in zip(pa, pm):
+        assert torch.equal(a.mips, m.mips)
+        assert torch.equal(a.irradiance, m.irradiance)
+    # the first request against the stateless precision bake
+    env = synth.make_env(256, 128, seed=300)
+    chain = ibl.build_env_chain(torch.from_numpy(env).cuda())
+    sizes0 = pa[0].mip_sizes
+    mips = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda") for w, h in sizes0]
+    rough = [k / (len(sizes0) - 1) for k in range(len(sizes0))]
+    irr = torch.empty((16, 32, 4), dtype=torch.float32, device="cuda")
+    ibl.bake_tc(chain, 256, 128, mips, rough, irradiance=irr)
+    torch.cuda.synchronize()
+    flat = torch.cat([t.reshape(-1) for t in mips]).cpu()
+    assert torch.equal(pa[0].mips, flat)
+    assert torch.equal(pa[0].irradiance, irr.cpu())
+    alone.close()
+    mixed.close()

@@ -88,3 +88,23 @@ def test_plan_meets_1e3_against_level0_quadrature():
     ref = oracle.quad_irradiance(lvl0, 64, 32, xy)[:, :3]
     got = irr.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
     assert _rel(got, ref).max() <= 1e-3, _rel(got, ref).max()
+
+
+def test_half_outputs_are_the_float_outputs_rounded():
+    w, h = 256, 128
+    env = synth.make_env(w, h, seed=12, sun_max=1e6)
+    chain = ibl.build_env_chain(torch.from_numpy(env).cuda())
+    sizes = [(128, 64), (64, 32), (16, 8)]
+    rough = [0.0, 0.4, 1.0]
+    f32 = [torch.empty((mh, mw, 4), dtype=torch.float32, device="cuda") for mw, mh in sizes]
+    f16 = [torch.empty((mh, mw, 4), dtype=torch.float16, device="cuda") for mw, mh in sizes]
+    irr32 = torch.empty((16, 32, 4), dtype=torch.float32, device="cuda")
+    irr16 = torch.empty((16, 32, 4), dtype=torch.float16, device="cuda")
+    ibl.bake_tc(chain, w, h, f32, rough, irradiance=irr32)
+    ibl.bake_tc(chain, w, h, f16, rough, irradiance=irr16)
+    torch.cuda.synchronize()
+    for a, b in zip(f32, f16):
+        assert torch.equal(a.half(), b)
+    assert torch.equal(irr32.half(), irr16)
+    with pytest.raises(ibl.IBLError):  # mixed output types
+        ibl.bake_tc(chain, w, h, [f32[0], f16[1]], rough[:2])
