@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
           "--expt-relaxed-constexpr"]
 # Units whose float arithmetic must stay unfused (parity with the oracle).
-NO_FMA_UNITS = {"ibl_plain.cu", "ibl_batch.cu"}
+NO_FMA_UNITS = {"ibl_plain.cu", "ibl_batch.cu", "ibl_ssr.cu"}
 
 
 def nvcc() -> str:

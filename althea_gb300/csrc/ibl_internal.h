@@ -47,5 +47,8 @@ size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n
                           const int* levels, int irr_w, int irr_h, int irr_level);
 int launch_brdf_lut(float* out, int n, size_t pitch_bytes, int samples, int orientation,
                     cudaStream_t st);
+// Reflection-buffer convolution (ibl_ssr.cu): levels 1..mips-1 from level 0.
+int ssr_convolve(void* const* levels, const size_t* pitch_bytes, int w, int h, int mips,
+                 cudaStream_t st);
 
 }  // namespace ibl

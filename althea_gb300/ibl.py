@@ -182,6 +182,9 @@ def load(build_if_missing: bool = True):
         "althea_ibl_tc_error": (i, [vp, vp]),
         "althea_ibl_bake_tc_ex": (i, [vp, i, i, ctypes.POINTER(MipTarget), i, ctypes.POINTER(i),
                                       vp, i, i, sz, i, vp, sz, i, vp]),
+        "althea_ssr_level_offset": (sz, [i, i, i]),
+        "althea_ssr_convolve": (i, [vp, i, i, i, vp]),
+        "althea_ssr_convolve_levels": (i, [ctypes.POINTER(vp), ctypes.POINTER(sz), i, i, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -639,3 +642,66 @@ def bake_tc(chain, w: int, h: int, outs: List, roughness: List[float], irradianc
     if check:
         _check(L.althea_ibl_tc_error(workspace.data_ptr(), sp))
     return workspace
+
+
+# ---- reflection-buffer glossy convolution ------------------------------------
+
+def ssr_level_offset(w: int, h: int, level: int) -> int:
+    """Texel offset of level `level` in a packed reflection-buffer chain."""
+    return load().althea_ssr_level_offset(w, h, level)
+
+
+def ssr_convolve(chain, w: int, h: int, mip_count: int = 5, stream=None) -> None:
+    """Convolves levels 1..mip_count-1 of a packed RGBA16F chain in place.
+
+    chain: contiguous CUDA float16 tensor holding ssr_level_offset(w, h,
+    mip_count) texels (4 halfs each), level 0 first."""
+    torch = _torch()
+    if not isinstance(chain, torch.Tensor) or not chain.is_cuda or chain.dtype != torch.float16:
+        raise IBLError(ERR_INVALID_ARGUMENT, "chain must be a CUDA float16 tensor")
+    if not chain.is_contiguous() or chain.numel() < 4 * ssr_level_offset(w, h, mip_count):
+        raise IBLError(ERR_INVALID_ARGUMENT, "chain tensor too small or not contiguous")
+    _check(load().althea_ssr_convolve(chain.data_ptr(), w, h, mip_count, _stream_ptr(stream)))
+
+
+def ssr_convolve_levels(levels, stream=None) -> None:
+    """levels: list of CUDA (H_l, W_l, 4) float16 tensors, level 0 first, each
+    max(1, W >> l) x max(1, H >> l); fills levels 1.. from level 0."""
+    torch = _torch()
+    n = len(levels)
+    if n < 1:
+        raise IBLError(ERR_INVALID_ARGUMENT, "need at least one level")
+    for l, t in enumerate(levels):
+        if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float16:
+            raise IBLError(ERR_INVALID_ARGUMENT, f"level {l} must be a CUDA float16 tensor")
+        if t.dim() != 3 or t.shape[2] != 4 or t.stride(2) != 1 or t.stride(1) != 4:
+            raise IBLError(ERR_INVALID_ARGUMENT, f"level {l} must be (H, W, 4) with packed texels")
+    h, w = levels[0].shape[:2]
+    for l, t in enumerate(levels):
+        if tuple(t.shape[:2]) != (max(1, h >> l), max(1, w >> l)):
+            raise IBLError(ERR_INVALID_ARGUMENT, f"level {l} has shape {tuple(t.shape[:2])}")
+    ptrs = (ctypes.c_void_p * n)(*[t.data_ptr() for t in levels])
+    pitch = (ctypes.c_size_t * n)(*[t.stride(0) * 2 for t in levels])
+    _check(load().althea_ssr_convolve_levels(ptrs, pitch, w, h, n, _stream_ptr(stream)))
+
+
+class ReflectionBuffer:
+    """The reflection buffer of Src/ReflectionBuffer.cpp:20-100 as device
+    memory: an RGBA16F chain of `mip_count` levels at the swapchain extent,
+    packed in one tensor.  `level(0)` is where the SSR pass writes;
+    convolveReflectionBuffer() fills the glossy levels 1.. from it
+    (Src/ReflectionBuffer.cpp:163-275)."""
+
+    def __init__(self, width: int, height: int, mip_count: int = 5, device="cuda"):
+        torch = _torch()
+        self.width, self.height, self.mip_count = width, height, mip_count
+        self.chain = torch.zeros(4 * ssr_level_offset(width, height, mip_count),
+                                 dtype=torch.float16, device=device)
+
+    def level(self, l: int):
+        w, h = max(1, self.width >> l), max(1, self.height >> l)
+        off = 4 * ssr_level_offset(self.width, self.height, l)
+        return self.chain[off:off + 4 * w * h].view(h, w, 4)
+
+    def convolveReflectionBuffer(self, stream=None) -> None:
+        ssr_convolve(self.chain, self.width, self.height, self.mip_count, stream)

@@ -67,3 +67,46 @@ def make_tinted_env(w: int, h: int, seed: int = 0) -> np.ndarray:
     tint = rng.uniform(0.25, 1.0, size=(h, w, 3)).astype(np.float32)
     env[..., :3] *= tint
     return env
+
+
+def make_reflection(w: int, h: int, seed: int = 0, extremes: bool = False) -> np.ndarray:
+    """(H, W, 4) float16 level 0 of a reflection buffer (what the SSR pass
+    writes into the RGBA16F buffer of Src/ReflectionBuffer.cpp:28-36).
+
+    RGB: a screen-space gradient 0.2..1.5 times a log-normal(0, 0.75) texel
+    noise, plus 16 Gaussian highlights (radius 1-4 % of the width, peak
+    log-uniform in [1, 2000]); texels whose ray missed (10 %, in horizontal
+    runs) are 0.  Alpha: the hit confidence, uniform in [0, 1], 0 on misses.
+    extremes=True also plants binary16 edge values -- subnormals, -0, the
+    largest finite half and its neighbours -- for the rounding paths.
+    Draws: PCG64, in the order noise, highlights, misses, alpha, extremes."""
+    rng = np.random.default_rng(seed)
+    ys, xs = np.mgrid[0:h, 0:w].astype(np.float64)
+    u, v = (xs + 0.5) / w, (ys + 0.5) / h
+    base = 0.2 + 1.3 * (0.5 * u + 0.5 * (1.0 - v))
+    rgb = base[..., None] * np.array([1.0, 0.9, 0.8]) * rng.lognormal(0.0, 0.75, (h, w, 1))
+    for _ in range(16):
+        cx, cy = rng.uniform(0, w), rng.uniform(0, h)
+        r = rng.uniform(0.01, 0.04) * w
+        peak = np.exp(rng.uniform(0.0, np.log(2000.0)))
+        tint = rng.uniform(0.6, 1.0, 3)
+        # the Gaussian below 1e-7 of its peak (beyond 5.7 r) is left out
+        x0, x1 = max(0, int(cx - 6 * r)), min(w, int(cx + 6 * r) + 1)
+        y0, y1 = max(0, int(cy - 6 * r)), min(h, int(cy + 6 * r) + 1)
+        d2 = (xs[y0:y1, x0:x1] - cx) ** 2 + (ys[y0:y1, x0:x1] - cy) ** 2
+        rgb[y0:y1, x0:x1] += peak * tint * np.exp(-d2 / (2 * r * r))[..., None]
+    miss = np.zeros((h, w), dtype=bool)
+    for _ in range(max(1, (h * w) // 200)):
+        y0, x0 = rng.integers(0, h), rng.integers(0, w)
+        miss[y0, x0:x0 + rng.integers(1, 40)] = True
+    alpha = rng.uniform(0.0, 1.0, (h, w))
+    rgb[miss] = 0.0
+    alpha[miss] = 0.0
+    out = np.concatenate([rgb, alpha[..., None]], axis=2).astype(np.float16)
+    if extremes:
+        flat = out.reshape(-1)
+        vals = np.array([0x0001, 0x03ff, 0x0400, 0x8000, 0x8001, 0x7bff, 0x7bfe, 0x3c00,
+                         0xfbff, 0x0200], dtype=np.uint16).view(np.float16)
+        idx = rng.choice(flat.size, size=min(flat.size, 64 * len(vals)), replace=False)
+        flat[idx] = np.resize(vals, idx.size)
+    return out

@@ -24,7 +24,9 @@ Hammersley) is timed on the same map in the same run.
 ``--path plain``: the plain production configuration (suns up to 1e4, the
 reference estimator bit-for-bit) with its HBM roofline.  ``--impl reference``
 times only the reference's CPU implementation (rank 0).  ``--workload batch``
-and ``--workload serve`` run the batching and serving configurations.
+and ``--workload serve`` run the batching and serving configurations;
+``--workload ssr`` the reflection-buffer glossy convolution of a 3840x2160
+RGBA16F frame (frames/s, level-1 kernel against the HBM roofline).
 Multi-GPU: one process per GPU, each bakes its own probe (independent units,
 no collective) -> weak scaling; value = all probes / max rank time.
 """
@@ -748,6 +750,216 @@ def run_serve(args):
     return 0
 
 
+# ----------------------------------------------------------------------------
+# Reflection-buffer glossy convolution (--workload ssr)
+# ----------------------------------------------------------------------------
+SSR_METRIC = "reflection-buffer glossy convolutions/s (frames/s), 1 GB300"
+SSR_W, SSR_H, SSR_MIPS = 3840, 2160, 5
+SSR_RING = 4  # frames cycled through: 4 x 88 MB > the 129 MB L2
+SSR_WORKLOAD = ("3840x2160 RGBA16F reflection buffer, 5 mips: levels 1-4 = 7-tap Gaussian of the "
+                "level before (vertical on odd levels), bit-identical to SSRGlossyConvolve.comp")
+
+
+def ssr_dims():
+    return [(max(SSR_W >> l, 1), max(SSR_H >> l, 1)) for l in range(SSR_MIPS)]
+
+
+def ssr_level1_bytes():
+    """Algorithmic bytes of the level-1 kernel: level 0 read once, level 1
+    written once (8 bytes per RGBA16F texel)."""
+    (w0, h0), (w1, h1) = ssr_dims()[:2]
+    return 8 * (w0 * h0 + w1 * h1)
+
+
+def ssr_frame_bytes():
+    """Compulsory HBM bytes of one frame: level 0 read, levels 1-4 written
+    (levels 1-3 are re-read from L2 by the next level)."""
+    return 8 * sum(w * h for w, h in ssr_dims())
+
+
+def ssr_frames():
+    from althea_gb300 import synth
+    base = synth.make_reflection(SSR_W, SSR_H, seed=0)
+    return [np.ascontiguousarray(np.roll(base, 97 * k, axis=1)) for k in range(SSR_RING)]
+
+
+def ssr_cpu_time(frame, steps=1):
+    """Seconds per frame of the reference shader compiled as C++ (oracle/_ref;
+    the C restatement when absent) on every host core, whole frames."""
+    import oracle
+    use_ref = oracle.ref_lib() is not None
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        if use_ref:
+            oracle.ref_ssr_convolve(frame, SSR_MIPS, nthreads=os.cpu_count())
+        else:
+            oracle.ssr_convolve(frame, SSR_MIPS)
+        ts.append(time.perf_counter() - t0)
+    return float(np.mean(ts)), ("reference" if use_ref else "port"), os.cpu_count()
+
+
+def run_ssr_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    frame = ssr_frames()[0]
+    ssr_cpu_time(frame, args.warmup)
+    sec, kind, cores = ssr_cpu_time(frame, args.steps)
+    value = 1.0 / sec
+    line = {"metric": SSR_METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f16 storage, f32 arithmetic", "data": "synthetic", "impl": "reference",
+            "config": {"workload": SSR_WORKLOAD,
+                       "path": "SSRGlossyConvolve.comp compiled as C++ (CPU, all host threads), "
+                               "dispatched level by level as convolveReflectionBuffer does"},
+            "cpu_baseline": {"value": value, "unit": "frames/s", "cores": cores, "kind": kind,
+                             "sample": "one whole 3840x2160 frame per step"},
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ssr(args):
+    import torch
+    from althea_gb300 import ibl
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    frames = ssr_frames()
+    bufs = []
+    for f in frames:
+        rb = ibl.ReflectionBuffer(SSR_W, SSR_H, SSR_MIPS, device=dev)
+        rb.level(0).copy_(torch.from_numpy(f).to(dev))
+        bufs.append(rb)
+    stream = torch.cuda.Stream(device=dev)
+    n = args.steps
+
+    def run_steps(k):
+        for i in range(k):
+            bufs[i % SSR_RING].convolveReflectionBuffer(stream)
+
+    with torch.cuda.stream(stream):
+        run_steps(max(args.warmup, SSR_RING))
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            run_steps(n)
+            ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        wall = time.perf_counter() - t_wall
+    total_ms = ev0.elapsed_time(ev1)
+    if pg is not None:
+        t = torch.tensor([total_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = n * world / (total_ms / 1e3)
+
+    # The dominant kernel alone: level 0 -> 1 through the per-level call
+    # (mip_count 2 launches exactly that kernel), back to back over the ring.
+    pairs = [[rb.level(0), rb.level(1)] for rb in bufs]
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for i in range(SSR_RING):
+            ibl.ssr_convolve_levels(pairs[i], stream)
+        k0.record(stream)
+        for i in range(n):
+            ibl.ssr_convolve_levels(pairs[i % SSR_RING], stream)
+        k1.record(stream)
+    torch.cuda.synchronize()
+    level1_ms = k0.elapsed_time(k1) / n
+
+    # ---- end to end through the public call with host buffers --------------
+    host_in = [torch.from_numpy(f).pin_memory() for f in frames]
+    out_texels = ibl.ssr_level_offset(SSR_W, SSR_H, SSR_MIPS) - SSR_W * SSR_H
+    host_out = [torch.empty(4 * out_texels, dtype=torch.float16, pin_memory=True)
+                for _ in range(SSR_RING)]
+    h2d = host_in[0].numel() * 2
+    d2h = host_out[0].numel() * 2
+
+    def e2e_step(i):
+        rb = bufs[i % SSR_RING]
+        rb.level(0).copy_(host_in[i % SSR_RING], non_blocking=True)
+        rb.convolveReflectionBuffer(stream)
+        host_out[i % SSR_RING].copy_(rb.chain[4 * SSR_W * SSR_H:], non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            e2e_step(i)
+    stream.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for i in range(n):
+            e2e_step(i)
+        e1.record(stream)
+    stream.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if pg is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = n * world / (e2e_ms / 1e3)
+
+    if rank == 0:
+        peak, peak_kind = read_peaks()
+        achieved = ssr_level1_bytes() / (level1_ms / 1e3) / 1e9
+        frame_gbs = ssr_frame_bytes() / (total_ms / n / 1e3) / 1e9
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            sec, kind, cores = ssr_cpu_time(frames[0], 3)
+            cpu = {"value": 1.0 / sec, "unit": "frames/s", "cores": cores, "kind": kind,
+                   "sample": "3 whole 3840x2160 frames"}
+        line = {
+            "metric": SSR_METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
+            "steps": n, "warmup": args.warmup, "ms_per_step": total_ms / n,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f16 storage, f32 arithmetic",
+            "data": "synthetic (seeded gradient x log-normal noise + 16 highlights, 10% misses)",
+            "config": {"workload": SSR_WORKLOAD, "global_batch": world,
+                       "parallelism": f"replicas x{world}",
+                       "l2": f"inputs larger than L2: {SSR_RING} frames cycled "
+                             f"({SSR_RING * ssr_frame_bytes() / 1e6:.0f} MB)",
+                       "frame_gbs": frame_gbs, "frame_bytes": ssr_frame_bytes()},
+            "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": (SSR_MIPS - 1) * n,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "ssr_level_kernel<true> (level 0 -> 1)",
+                         "kernel_ms": level1_ms, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": ssr_level1_bytes()},
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+            "wall_s": wall,
+        }
+        print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -756,9 +968,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--generator", default="hammersley", choices=["hammersley", "ref-hash"])
-    ap.add_argument("--workload", default="probe", choices=["probe", "batch", "serve"],
+    ap.add_argument("--workload", default="probe", choices=["probe", "batch", "serve", "ssr"],
                     help="probe: one 4096x2048 bake per step (default); batch: many probes; "
-                         "serve: Poisson request stream against the server")
+                         "serve: Poisson request stream against the server; ssr: the "
+                         "reflection-buffer glossy convolution of a 3840x2160 frame")
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--path", default="tc", choices=["plain", "tc"],
                     help="probe workload: tensor-core precision path (default, suns <= 1e6) "
@@ -774,7 +987,9 @@ def main():
     global GENERATOR
     GENERATOR = 1 if args.generator == "hammersley" else 0
     if args.impl == "reference":
-        return run_reference(args)
+        return run_ssr_reference(args) if args.workload == "ssr" else run_reference(args)
+    if args.workload == "ssr":
+        return run_ssr(args)
     if args.workload == "batch":
         return run_batch(args)
     if args.workload == "serve":

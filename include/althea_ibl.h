@@ -344,6 +344,25 @@ int althea_ibl_hdr_read(const char* path, float** rgba_out, int* width, int* hei
 void althea_ibl_hdr_free(float* rgba);
 int althea_ibl_hdr_write(const char* path, const float* rgba, int width, int height);
 
+/* ---- Reflection-buffer glossy convolution ----------------------------------
+ * Replaces ReflectionBuffer::convolveReflectionBuffer (Src/ReflectionBuffer.cpp:
+ * 163-275), the per-frame dispatch of Shaders/SSRGlossyConvolve.comp:25-53 over
+ * the RGBA16F reflection buffer (Src/ReflectionBuffer.cpp:28-36): levels
+ * 1..mip_count-1 become the 7-tap Gaussian of the level before, vertical for odd
+ * levels and horizontal for even ones, bit-identical to the shader's FP32
+ * arithmetic with a Vulkan LINEAR / CLAMP_TO_EDGE sampler.  Level l is
+ * max(1, width >> l) x max(1, height >> l) texels of 4 IEEE halfs (8 bytes);
+ * mip_count 1..16 (the reference uses 5).  Launches only; no allocation.
+ *
+ * althea_ssr_convolve: every level packed back to back in one device buffer,
+ *   level l at texel althea_ssr_level_offset(width, height, l).
+ * althea_ssr_convolve_levels: one device pointer and row pitch (bytes, a
+ *   multiple of 8) per level, e.g. buffers imported per mip. */
+size_t althea_ssr_level_offset(int width, int height, int level);  /* in texels */
+int althea_ssr_convolve(void* chain_dev, int width, int height, int mip_count, void* stream);
+int althea_ssr_convolve_levels(void* const* levels_dev, const size_t* pitch_bytes, int width,
+                               int height, int mip_count, void* stream);
+
 const char* althea_ibl_last_error(void);
 int althea_ibl_abi_version(void);
 

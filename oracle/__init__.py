@@ -38,9 +38,10 @@ _I = ctypes.POINTER(ctypes.c_int)
 
 
 def build(force: bool = False) -> str:
-    """Compile ibl_oracle.c into a shared library (gcc, OpenMP)."""
+    """Compile ibl_oracle.c and ssr_oracle.c into a shared library (gcc, OpenMP)."""
     src = os.path.join(HERE, "ibl_oracle.c")
-    deps = [src, os.path.join(HERE, "ibl_oracle.h"),
+    ssr = os.path.join(HERE, "ssr_oracle.c")
+    deps = [src, ssr, os.path.join(HERE, "ibl_oracle.h"),
             os.path.join(HERE, "..", "althea_gb300", "csrc", "glsl_builtins.h")]
     if not force and os.path.exists(LIB_PATH):
         t = os.path.getmtime(LIB_PATH)
@@ -48,7 +49,7 @@ def build(force: bool = False) -> str:
             return LIB_PATH
     tmp = LIB_PATH + f".tmp{os.getpid()}"
     subprocess.check_call(["gcc", "-std=gnu11", "-O2", "-fPIC", "-shared", "-fopenmp",
-                           "-ffp-contract=off", "-o", tmp, src, "-lm"])
+                           "-ffp-contract=off", "-o", tmp, src, ssr, "-lm"])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -236,3 +237,61 @@ def ref_irradiance_envsize(chain, w, h, xy, nthreads=0):
     ref_lib().ref_irradiance_raw(_fp(chain), w, h, level_count(w, h), _fp(out), w, h, _ip(xy),
                                  len(xy), nthreads)
     return out
+
+
+def ref_ssr_convolve(level0_half, mips, nthreads=0):
+    """SSRGlossyConvolve.comp (the reference shader compiled as C++) dispatched
+    the way ReflectionBuffer::convolveReflectionBuffer does it
+    (Src/ReflectionBuffer.cpp:224-268): for level l = 1..mips-1, push constants
+    width/height = level l's size, direction (0,1) for odd l and (1,0) for even
+    l, roughness l/4, source = level l-1.  Returns the packed chain (flat
+    float16, level 0 first) like ssr_convolve."""
+    R = ref_lib()
+    U16 = ctypes.POINTER(ctypes.c_uint16)
+    R.ref_ssr_dispatch.restype = None
+    R.ref_ssr_dispatch.argtypes = [U16, ctypes.c_int, ctypes.c_int, U16, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_float,
+                                   ctypes.c_float, ctypes.c_float, ctypes.c_int]
+    h, w = level0_half.shape[:2]
+    dims = [(max(1, w >> l), max(1, h >> l)) for l in range(mips)]
+    levels = [np.ascontiguousarray(level0_half, dtype=np.float16).view(np.uint16).copy()]
+    for l in range(1, mips):
+        (sw, sh), (dw, dh) = dims[l - 1], dims[l]
+        dst = np.zeros((dh, dw, 4), dtype=np.uint16)
+        dx, dy = (0.0, 1.0) if l & 1 else (1.0, 0.0)
+        R.ref_ssr_dispatch(levels[-1].ctypes.data_as(U16), sw, sh, dst.ctypes.data_as(U16), dw,
+                           dh, dw, dh, dx, dy, l / 4.0, nthreads)
+        levels.append(dst)
+    return np.concatenate([a.ravel() for a in levels]).view(np.float16)
+
+
+# ---- reflection-buffer glossy convolution (ssr_oracle.c) --------------------------
+
+def ssr_level_offset(w: int, h: int, level: int) -> int:
+    L = lib()
+    L.oracle_ssr_level_offset.restype = ctypes.c_size_t
+    L.oracle_ssr_level_offset.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    return int(L.oracle_ssr_level_offset(w, h, level))
+
+
+def ssr_convolve(level0_half: np.ndarray, mips: int) -> np.ndarray:
+    """level0_half: (H, W, 4) float16.  Returns every level packed back to back
+    as a flat float16 array (level 0 first), levels 1..mips-1 convolved."""
+    h, w = level0_half.shape[:2]
+    total = ssr_level_offset(w, h, mips)
+    chain = np.zeros(total * 4, dtype=np.uint16)
+    chain[:w * h * 4] = np.ascontiguousarray(level0_half, dtype=np.float16).view(np.uint16).ravel()
+    L = lib()
+    L.oracle_ssr_convolve.restype = None
+    L.oracle_ssr_convolve.argtypes = [ctypes.POINTER(ctypes.c_uint16), ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int]
+    L.oracle_ssr_convolve(chain.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)), w, h, mips)
+    return chain.view(np.float16)
+
+
+def float_to_half_bits(x: np.ndarray) -> np.ndarray:
+    L = lib()
+    L.oracle_float_to_half.restype = ctypes.c_uint16
+    L.oracle_float_to_half.argtypes = [ctypes.c_float]
+    return np.array([L.oracle_float_to_half(float(v)) for v in np.asarray(x, np.float32).ravel()],
+                    dtype=np.uint16)

@@ -1,7 +1,8 @@
-// glsl_compat.hpp -- just enough GLSL 450 for the two IBL compute shaders of
-// the reference (Shaders/IBL_Precompute/GenIrradianceMap.comp and
-// PreFilterEnvMap.comp) to compile unmodified-in-substance as C++ after the
-// mechanical rewrite done by oracle/make_ref.py.  TEST INFRASTRUCTURE ONLY.
+// glsl_compat.hpp -- just enough GLSL 450 for three compute shaders of the
+// reference (Shaders/IBL_Precompute/GenIrradianceMap.comp, PreFilterEnvMap.comp
+// and Shaders/SSRGlossyConvolve.comp) to compile unmodified-in-substance as C++
+// after the mechanical rewrite done by oracle/make_ref.py.  TEST INFRASTRUCTURE
+// ONLY.
 //
 // Semantics chosen where GLSL leaves them to the implementation:
 //  * transcendental built-ins -> glsl_builtins.h (fixed, portable);
@@ -10,10 +11,16 @@
 //  * length/normalize/dot sum left to right; mat3*vec3 = c0*v.x + c1*v.y + c2*v.z;
 //  * textureLod -> the Vulkan-spec trilinear filter (REPEAT, LINEAR, LINEAR)
 //    over a vkCmdBlitImage-equivalent mip chain, both written again here
-//    independently of oracle/ibl_oracle.c.
+//    independently of oracle/ibl_oracle.c;
+//  * bindless heap textures (SAMPLER2D / IMAGE2D_W of Bindless/GlobalHeap.glsl)
+//    -> one-level RGBA16F views sampled LINEAR with CLAMP_TO_EDGE (the
+//    reference's default SamplerOptions, Include/Althea/Sampler.h:16-29), and
+//    RGBA16F stores rounded to nearest even; the binary16 conversions are
+//    written from the format's definition, independently of oracle/ssr_oracle.c.
 // Build with -ffp-contract=off so no multiply-add is fused.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -53,9 +60,17 @@ struct vec3 {
 struct vec4 {
   float x, y, z, w;
   vec4() : x(0), y(0), z(0), w(0) {}
+  explicit vec4(float s) : x(s), y(s), z(s), w(s) {}
   vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
   vec4(const vec3& v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
   vec3 rgb() const { return vec3(x, y, z); }
+  vec4& operator+=(const vec4& o) {
+    x = x + o.x;
+    y = y + o.y;
+    z = z + o.z;
+    w = w + o.w;
+    return *this;
+  }
 };
 struct uvec2 {
   uint32_t x, y;
@@ -87,6 +102,11 @@ inline uvec2 operator*(uint32_t s, const uvec2& a) { return uvec2(s * a.x, s * a
 inline vec2 operator*(float s, const vec2& a) { return vec2(s * a.x, s * a.y); }
 inline vec2 operator-(const vec2& a, float s) { return vec2(a.x - s, a.y - s); }
 inline vec2 operator/(const vec2& a, const vec2& b) { return vec2(a.x / b.x, a.y / b.y); }
+inline vec2 operator/(const vec2& a, float s) { return vec2(a.x / s, a.y / s); }
+inline vec2 operator*(const vec2& a, const vec2& b) { return vec2(a.x * b.x, a.y * b.y); }
+inline vec2 operator+(const vec2& a, const vec2& b) { return vec2(a.x + b.x, a.y + b.y); }
+inline vec2 operator-(const vec2& a, const vec2& b) { return vec2(a.x - b.x, a.y - b.y); }
+inline vec4 operator*(const vec4& a, float s) { return vec4(a.x * s, a.y * s, a.z * s, a.w * s); }
 
 inline vec3 operator+(const vec3& a, const vec3& b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
 inline vec3 operator-(const vec3& a, const vec3& b) { return vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
@@ -190,6 +210,79 @@ inline void imageStore(const image2D&, const ivec2& p, const vec4& c) {
   o[1] = c.y;
   o[2] = c.z;
   o[3] = c.w;
+}
+
+// ---- bindless heap of one-level RGBA16F views (SSRGlossyConvolve) ---------
+struct HalfView {
+  const uint16_t* src = nullptr;  // sampled view: 4 halfs per texel, row-major
+  uint16_t* dst = nullptr;        // storage view
+  int w = 0, h = 0;
+};
+extern HalfView g_heap_tex[4], g_heap_img[4];
+struct HeapTexture { uint idx; };
+struct HeapImage { uint idx; };
+struct SamplerHeap {
+  HeapTexture operator[](uint i) const { return HeapTexture{i}; }
+};
+struct ImageHeap {
+  HeapImage operator[](uint i) const { return HeapImage{i}; }
+};
+#define SAMPLER2D(NAME) glslc::SamplerHeap NAME
+#define IMAGE2D_W(NAME) glslc::ImageHeap NAME
+
+// binary16 -> binary32: (-1)^s * 2^(e-15) * (1 + m/1024), subnormals 2^-14 * m/1024.
+inline float half_value(uint16_t hbits) {
+  int e = (hbits >> 10) & 31, m = hbits & 1023;
+  float mag;
+  if (e == 31)
+    mag = m ? NAN : INFINITY;
+  else if (e == 0)
+    mag = ldexpf((float)m, -24);
+  else
+    mag = ldexpf((float)(1024 + m), e - 25);
+  return (hbits & 0x8000) ? -mag : mag;
+}
+// binary32 -> binary16, round to nearest even: scale the magnitude so the
+// kept bits are the integer part (exact, a power of two) and round that with
+// nearbyintf in the default round-to-nearest-even mode.
+inline uint16_t half_bits(float f) {
+  uint16_t sign = signbit(f) ? 0x8000 : 0;
+  float a = fabsf(f);
+  if (isnan(a)) return (uint16_t)(sign | 0x7e00);
+  if (a >= 65520.0f) return (uint16_t)(sign | 0x7c00);  // ties above 65504 round to inf
+  if (a < ldexpf(1.0f, -14)) return (uint16_t)(sign | (uint16_t)nearbyintf(ldexpf(a, 24)));
+  int k;
+  frexpf(a, &k);  // a in [2^(k-1), 2^k)
+  int e = k - 1;
+  int q = (int)nearbyintf(ldexpf(a, 10 - e));  // 1024..2048
+  if (q == 2048) {
+    q = 1024;
+    e += 1;
+  }
+  return (uint16_t)(sign | ((e + 15) << 10) | (q - 1024));
+}
+inline vec4 fetch_half(const HalfView& v, int i, int j) {
+  const uint16_t* p = v.src + 4 * ((size_t)j * v.w + i);
+  return vec4(half_value(p[0]), half_value(p[1]), half_value(p[2]), half_value(p[3]));
+}
+inline int clamp_to_edge(int i, int n) { return i < 0 ? 0 : (i >= n ? n - 1 : i); }
+// The view has one level and the sampler minLod = maxLod = 0: level 0, LINEAR.
+inline vec4 textureLod(const HeapTexture& t, const vec2& uv, float) {
+  const HalfView& v = g_heap_tex[t.idx];
+  float x = uv.x * (float)v.w - 0.5f, y = uv.y * (float)v.h - 0.5f;
+  float fx = floorf(x), fy = floorf(y);
+  int i0 = clamp_to_edge((int)fx, v.w), i1 = clamp_to_edge((int)fx + 1, v.w);
+  int j0 = clamp_to_edge((int)fy, v.h), j1 = clamp_to_edge((int)fy + 1, v.h);
+  return bilinear(fetch_half(v, i0, j0), fetch_half(v, i1, j0), fetch_half(v, i0, j1),
+                  fetch_half(v, i1, j1), x - fx, y - fy);
+}
+inline void imageStore(const HeapImage& im, const ivec2& p, const vec4& c) {
+  const HalfView& v = g_heap_img[im.idx];
+  uint16_t* o = v.dst + 4 * ((size_t)p.y * v.w + p.x);
+  o[0] = half_bits(c.x);
+  o[1] = half_bits(c.y);
+  o[2] = half_bits(c.z);
+  o[3] = half_bits(c.w);
 }
 
 // Sample-index counter for the Hammersley variant of sampleGGX's xi source.

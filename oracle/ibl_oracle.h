@@ -79,6 +79,15 @@ int oracle_max_threads(void);
 /* Portable GLSL built-in over an array: 0 sin, 1 cos, 2 atan, 3 atan2(a,b), 4 log2. */
 void oracle_builtin_eval(int fn, const float* a, const float* b, float* out, int n);
 
+/* Reflection-buffer glossy convolution (ssr_oracle.c; Shaders/SSRGlossyConvolve.comp
+ * as dispatched by Src/ReflectionBuffer.cpp:163-275).  chain: RGBA16F levels
+ * packed back to back (4 uint16 per texel, level 0 first); fills levels
+ * 1..mips-1 from level 0.  IEEE binary16 conversions, round to nearest even. */
+float oracle_half_to_float(uint16_t h);
+uint16_t oracle_float_to_half(float f);
+size_t oracle_ssr_level_offset(int w, int h, int level); /* in texels */
+void oracle_ssr_convolve(uint16_t* chain, int w, int h, int mips);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,11 +1,13 @@
 """Build the reference-shader CPU library ``oracle/_ref/libref_ibl.so``.
 
 TEST INFRASTRUCTURE ONLY.  Reads the reference's own compute shaders
-(Shaders/IBL_Precompute/GenIrradianceMap.comp and PreFilterEnvMap.comp) from
-the reference checkout, applies a purely mechanical GLSL -> C++ rewrite and
-compiles the result against ``oracle/glsl_compat.hpp``:
+(Shaders/IBL_Precompute/GenIrradianceMap.comp, PreFilterEnvMap.comp and
+Shaders/SSRGlossyConvolve.comp) from the reference checkout, applies a purely
+mechanical GLSL -> C++ rewrite and compiles the result against
+``oracle/glsl_compat.hpp``:
 
-* drop ``#version``, ``layout(local_size...) in;`` and ``//`` comments;
+* drop ``#version``, ``layout(local_size...) in;``, ``//`` comments and the
+  ``#include <Bindless/...>`` line (the compat header defines the heap macros);
 * ``layout(...) uniform [writeonly] T name;`` -> ``T name;``;
 * the push-constant block -> a ``struct`` with a global instance;
 * top-level mutable globals (``uvec2 seed;``) -> ``thread_local``;
@@ -18,7 +20,8 @@ compiles the result against ``oracle/glsl_compat.hpp``:
   ``hammersley`` variant;
 * ``#define MAX_SAMPLES 10000`` -> a run-time sample count;
 * ``main`` -> ``shader_main``, plus a driver that sets
-  ``gl_GlobalInvocationID`` for each texel.
+  ``gl_GlobalInvocationID`` for each texel (for SSRGlossyConvolve: for every
+  invocation of the reference's dispatch, Src/ReflectionBuffer.cpp:266-268).
 
 Outputs go only to ``oracle/_ref/`` (git-ignored): the generated ``.cpp``
 files and the shared library.  The generated sources are kept there so that a
@@ -48,7 +51,7 @@ def transform(src: str) -> str:
         s = code.strip()
         if not s:
             continue
-        if s.startswith("#version"):
+        if s.startswith("#version") or s.startswith("#include <Bindless/"):
             continue
         if re.match(r"layout\s*\(\s*local_size", s):
             continue
@@ -129,6 +132,49 @@ def make_unit(shader_file: str, ns: str, xi: str, fn: str, prefilter: bool) -> s
     )
 
 
+SSR_DRIVER = r"""
+// ---- driver (generated) ----------------------------------------------------
+// One vkCmdDispatch of the convolution pass: texture heap slot 0 = level l-1,
+// image heap slot 0 = level l, push constants as the caller sets them.
+extern "C" void ref_ssr_dispatch(const uint16_t* src, int sw, int sh, uint16_t* dst, int dw,
+                                 int dh, unsigned width, unsigned height, float dirx, float diry,
+                                 float roughness, int nthreads) {
+  glslc::g_heap_tex[0].src = src;
+  glslc::g_heap_tex[0].w = sw;
+  glslc::g_heap_tex[0].h = sh;
+  glslc::g_heap_img[0].dst = dst;
+  glslc::g_heap_img[0].w = dw;
+  glslc::g_heap_img[0].h = dh;
+  pushConstants.srcMipTexHandle = 0;
+  pushConstants.targetMipImgHandle = 0;
+  pushConstants.width = width;
+  pushConstants.height = height;
+  pushConstants.direction = vec2(dirx, diry);
+  pushConstants.roughness = roughness;
+  const unsigned gx = (width - 1) / 16 + 1, gy = (height - 1) / 16 + 1;
+  int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (long long i = 0; i < (long long)gx * 16 * gy * 16; ++i) {
+    glslc::gl_GlobalInvocationID.x = (uint32_t)(i % (gx * 16));
+    glslc::gl_GlobalInvocationID.y = (uint32_t)(i / (gx * 16));
+    glslc::gl_GlobalInvocationID.z = 0;
+    shader_main();
+  }
+}
+"""
+
+
+def make_ssr_unit() -> str:
+    path = os.path.join(REF_ROOT, "Shaders", "SSRGlossyConvolve.comp")
+    with open(path, "r", encoding="utf-8") as f:
+        body = transform(f.read())
+    return (
+        "// GENERATED by oracle/make_ref.py from SSRGlossyConvolve.comp -- do not edit.\n"
+        "#include <omp.h>\n#include \"../glsl_compat.hpp\"\n"
+        "namespace ref_ssr {\nGLSLC_USING\n" + body + SSR_DRIVER + "}\n"
+    )
+
+
 UNITS = [
     ("PreFilterEnvMap.comp", "ref_prefilter_hash", "vec2{rng(), rng()}", "ref_prefilter_hash", True),
     ("PreFilterEnvMap.comp", "ref_prefilter_hammersley", "glslc::hammersley_next()", "ref_prefilter_hammersley", True),
@@ -141,10 +187,14 @@ def generate() -> None:
     for shader, ns, xi, fn, pre in UNITS:
         with open(os.path.join(OUT, ns + ".cpp"), "w", encoding="utf-8") as f:
             f.write(make_unit(shader, ns, xi, fn, pre))
+    with open(os.path.join(OUT, "ref_ssr.cpp"), "w", encoding="utf-8") as f:
+        f.write(make_ssr_unit())
 
 
 def compile_lib() -> str:
     srcs = [os.path.join(OUT, ns + ".cpp") for _, ns, _, _, _ in UNITS]
+    if os.path.exists(os.path.join(OUT, "ref_ssr.cpp")):
+        srcs.append(os.path.join(OUT, "ref_ssr.cpp"))
     srcs.append(os.path.join(HERE, "ref_support.cpp"))
     lib = os.path.join(OUT, "libref_ibl.so")
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",

@@ -11,6 +11,7 @@ Resources g_res;
 thread_local uvec3 gl_GlobalInvocationID;
 thread_local int g_sample_index = 0;
 int g_sample_count = 1;
+HalfView g_heap_tex[4], g_heap_img[4];
 }  // namespace glslc
 
 namespace {

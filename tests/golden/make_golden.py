@@ -14,6 +14,10 @@ reference next to it; the fixtures themselves travel, the reference does not).
   shipped Content/PrecomputedMaps/*/Prefiltered{2..5}.hdr (RGBE).
 * ``ref_LuxuryRoom_Prefiltered5.hdr`` -- one of those files, copied as is
   (25 KB), for the run-length RGBE reader.
+* ``ref_ssr.npz`` -- the reference's Shaders/SSRGlossyConvolve.comp (rewritten
+  to C++ by oracle/make_ref.py), dispatched level by level as
+  Src/ReflectionBuffer.cpp:224-268 does, on seeded RGBA16F level-0 images of
+  several shapes (odd, 16:9, tall, collapsing to 1x1, binary16 edge values).
 
 Usage: python tests/golden/make_golden.py
 """
@@ -57,6 +61,22 @@ def ref_shader_fixture():
     out["irradiance_envsize"] = oracle.ref_irradiance_envsize(chain, w, h, xy)
     out["rng_seed00_first8"] = oracle.rng_stream(0, 0, 8)
     np.savez_compressed(os.path.join(HERE, "ref_shaders_64x32.npz"), **out)
+
+
+SSR_CASES = [(61, 37, 5, False), (96, 54, 5, False), (5, 3, 5, False), (33, 200, 5, False),
+             (40, 24, 5, True), (128, 72, 7, True)]
+
+
+def ref_ssr_fixture():
+    if oracle.ref_lib() is None:
+        raise SystemExit("oracle/_ref/libref_ibl.so missing: run python oracle/make_ref.py")
+    out = {}
+    for k, (w, h, mips, ext) in enumerate(SSR_CASES):
+        l0 = synth.make_reflection(w, h, seed=40 + k, extremes=ext)
+        out[f"in{k}"] = l0.view(np.uint16)
+        out[f"out{k}"] = oracle.ref_ssr_convolve(l0, mips).view(np.uint16)
+        out[f"shape{k}"] = np.array([w, h, mips])
+    np.savez_compressed(os.path.join(HERE, "ref_ssr.npz"), **out)
 
 
 def decode_png(path):
@@ -166,4 +186,5 @@ if __name__ == "__main__":
     lut_fixture()
     hdr_fixture()
     hdr_file_fixture()
+    ref_ssr_fixture()
     print("fixtures written to", HERE)

@@ -16,7 +16,8 @@ def declared_symbols():
     for f in os.listdir(os.path.join(ROOT, "include")):
         if f.endswith(".h"):
             text = open(os.path.join(ROOT, "include", f)).read()
-            names |= set(re.findall(r"\b(althea_ibl_[a-z0-9_]+)\s*\(", text))
+            names |= set(re.findall(r"\b(althea_(?:ibl|ssr)_[a-z0-9_]+)\s*\(", text))
+            names |= set(re.findall(r"\b(althea_ssr_convolve)\s*\(", text))
     return sorted(names)
 
 
