@@ -45,6 +45,7 @@ struct Level {
   uint2* dst;        // level l
   long long src_pitch, dst_pitch;  // in texels
   int sw, sh, dw, dh;
+  float q1, q2, q3;  // offsets / resolution: kOff_k / (float)dw (IEEE division, on the host)
 };
 
 __device__ __forceinline__ float2 halves(uint32_t v) {
@@ -54,9 +55,11 @@ __device__ __forceinline__ float2 halves(uint32_t v) {
 __device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
 
 // Channel pairs, each product and sum rounded on its own (__fmul_rn/__fadd_rn
-// are never fused into a multiply-add).  The packed FP32x2 forms were tried
-// and gave results one unit in the last place away from separately rounded
-// scalar ones on rare texels, so they are not used here.
+// are never fused into a multiply-add).  The packed FP32x2 instructions are not
+// used: written as FMUL2/FADD2, or as FFMA2 with a -0 addend / unit multiplier
+// (even with those constants opaque to the compiler), they gave results one
+// unit in the last place away from the separately rounded scalar ones on rare
+// texels.
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) {
   return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
 }
@@ -115,25 +118,39 @@ __global__ void __launch_bounds__(kBlockX* kBlockY) ssr_level_kernel(Level L) {
   const int x = blockIdx.x * kBlockX + threadIdx.x;
   const int y = blockIdx.y * kBlockY + threadIdx.y;
   const bool live = x < L.dw && y < L.dh;
-  // texelUv and the offsets / resolution (resolution = the level's width)
+  // texelUv; the offsets / resolution (resolution = the level's width) come in L
   const float u = __fdiv_rn((float)x, (float)L.dw);
   const float v = __fdiv_rn((float)y, (float)L.dh);
-  const float res = (float)L.dw;
-  const float q1 = __fdiv_rn(kOff1, res), q2 = __fdiv_rn(kOff2, res), q3 = __fdiv_rn(kOff3, res);
+  const float q1 = L.q1, q2 = L.q2, q3 = L.q3;
   // The level before this one was written by the previous launch.
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  if (!live) return;
   float2 rg = make_float2(0.0f, 0.0f), ba = make_float2(0.0f, 0.0f);
   if (VERT) {
+    // A warp is one output row, so the seven row footprints are the same on
+    // every lane: lanes 0-6 compute one tap each and the warp shares them.
+    if (y >= L.dh) return;  // the whole warp
+    const int lane = threadIdx.x, k = lane < 7 ? lane : 0;
+    const float d = k == 0 ? 0.0f : (k <= 2 ? q1 : (k <= 4 ? q2 : q3));
+    const float p = k == 0 ? v : ((k & 1) ? __fadd_rn(v, d) : __fsub_rn(v, d));
+    const Axis mine = axis(p, L.sh);
+    Axis m[7];
+#pragma unroll
+    for (int t = 0; t < 7; ++t) {
+      m[t].i0 = __shfl_sync(0xffffffffu, mine.i0, t);
+      m[t].i1 = __shfl_sync(0xffffffffu, mine.i1, t);
+      m[t].frac = __shfl_sync(0xffffffffu, mine.frac, t);
+    }
+    if (x >= L.dw) return;
     const Axis ax = axis(u, L.sw);
-    tap(L, ax, axis(v, L.sh), kW0, rg, ba);
-    tap(L, ax, axis(__fadd_rn(v, q1), L.sh), kW1, rg, ba);
-    tap(L, ax, axis(__fsub_rn(v, q1), L.sh), kW1, rg, ba);
-    tap(L, ax, axis(__fadd_rn(v, q2), L.sh), kW2, rg, ba);
-    tap(L, ax, axis(__fsub_rn(v, q2), L.sh), kW2, rg, ba);
-    tap(L, ax, axis(__fadd_rn(v, q3), L.sh), kW3, rg, ba);
-    tap(L, ax, axis(__fsub_rn(v, q3), L.sh), kW3, rg, ba);
+    tap(L, ax, m[0], kW0, rg, ba);
+    tap(L, ax, m[1], kW1, rg, ba);
+    tap(L, ax, m[2], kW1, rg, ba);
+    tap(L, ax, m[3], kW2, rg, ba);
+    tap(L, ax, m[4], kW2, rg, ba);
+    tap(L, ax, m[5], kW3, rg, ba);
+    tap(L, ax, m[6], kW3, rg, ba);
   } else {
+    if (!live) return;
     const Axis ay = axis(v, L.sh);
     tap(L, axis(u, L.sw), ay, kW0, rg, ba);
     tap(L, axis(__fadd_rn(u, q1), L.sw), ay, kW1, rg, ba);
@@ -196,6 +213,10 @@ int ssr_convolve(void* const* levels, const size_t* pitch_bytes, int w, int h, i
     L.sh = dim(h, l - 1);
     L.dw = dim(w, l);
     L.dh = dim(h, l);
+    const float res = (float)L.dw;  // resolution = the level's width
+    L.q1 = kOff1 / res;
+    L.q2 = kOff2 / res;
+    L.q3 = kOff3 / res;
     const int s = launch_level(L, (l & 1) != 0, st);
     if (s != ALTHEA_IBL_OK) return s;
   }
