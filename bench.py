@@ -756,6 +756,10 @@ def run_serve(args):
 SSR_METRIC = "reflection-buffer glossy convolutions/s (frames/s), 1 GB300"
 SSR_W, SSR_H, SSR_MIPS = 3840, 2160, 5
 SSR_RING = 4  # frames cycled through: 4 x 88 MB > the 129 MB L2
+# DRAM bytes (read + write) of one level-1 launch of the 3840x2160 workload, from
+# the ncu capture summarised in profiles/ssr_convolve_3840x2160_ncu.md (writes
+# still in L2 when the kernel ends are not counted there).
+NCU_SSR_LEVEL1_TRAFFIC = 69.73e6
 SSR_WORKLOAD = ("3840x2160 RGBA16F reflection buffer, 5 mips: levels 1-4 = 7-tap Gaussian of the "
                 "level before (vertical on odd levels), bit-identical to SSRGlossyConvolve.comp")
 
@@ -946,7 +950,7 @@ def run_ssr(args):
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": (SSR_MIPS - 1) * n,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": NCU_SSR_LEVEL1_TRAFFIC,
                          "kernel": "ssr_level_kernel<true> (level 0 -> 1)",
                          "kernel_ms": level1_ms, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": ssr_level1_bytes()},
