@@ -279,6 +279,7 @@ struct althea_ibl_batch {
   // graph
   cudaGraphExec_t exec = nullptr;
   cudaStream_t exec_stream = nullptr;
+  int graph_kernels = -1;  // kernel nodes of the captured bake (-1: not captured)
   // precision path (ALTHEA_IBL_BATCH_PRECISION): one tensor-core bake per
   // probe after the shared chain pass; probes of one shape share a workspace
   // (every launch is stream-ordered, so the bakes never overlap)
@@ -819,6 +820,19 @@ extern "C" int althea_ibl_batch_run(althea_ibl_batch* b, void* stream) {
     return r;
   }
   if (e != cudaSuccess) return cuda_status(e, "batch graph capture end");
+  size_t nodes = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &nodes) == cudaSuccess && nodes > 0) {
+    std::vector<cudaGraphNode_t> list(nodes);
+    int kernels = 0;
+    if (cudaGraphGetNodes(graph, list.data(), &nodes) == cudaSuccess) {
+      for (size_t i = 0; i < nodes; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(list[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+          ++kernels;
+      }
+      b->graph_kernels = kernels;
+    }
+  }
   e = cudaGraphInstantiate(&b->exec, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) {
@@ -841,6 +855,7 @@ extern "C" int althea_ibl_batch_describe(const althea_ibl_batch* b, althea_ibl_b
   info->irradiance_target_blocks = b->choice.irr_target;
   info->tuned = b->tuned;
   info->graph = b->exec != nullptr;
+  info->graph_kernels = b->exec ? b->graph_kernels : -1;
   return ALTHEA_IBL_OK;
 }
 

@@ -84,7 +84,7 @@ class BatchParams(ctypes.Structure):
 class BatchInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in (
         "probes", "prefilter_jobs", "prefilter_tiles", "irradiance_blocks", "tile_x", "tile_y",
-        "persistent_blocks", "irradiance_target_blocks", "tuned", "graph")]
+        "persistent_blocks", "irradiance_target_blocks", "tuned", "graph", "graph_kernels")]
 
 
 BATCH_AUTOTUNE = 1

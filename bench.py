@@ -85,6 +85,17 @@ def prefilter_algorithmic_bytes():
     return total
 
 
+def read_tensor_peak():
+    """Dense BF16 burst peak (TFLOP/s) from MEASURED_PEAKS.json, else the fallback."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        if "bf16_tflops" in d:
+            return float(d["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
 def read_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -570,10 +581,7 @@ def run_tc(args):
     errs = error_table(env, {"tensor": tc_outs, "plain": [t.cpu().numpy() for t in p_mips]},
                        {"tensor": tc_irr, "plain": p_irr.cpu().numpy()})
     if rank == 0:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-        peak = float(peaks.get("bf16_tflops", 1900.0))
-        peak_kind = "measured" if "bf16_tflops" in peaks else "fallback"
+        peak, peak_kind = read_tensor_peak()
         alg_flops, split_flops = tc_flops(levels, irr_level)
         achieved = alg_flops / (tc_ms / 1e3) / 1e12
         executed = split_flops / (tc_ms / 1e3) / 1e12
@@ -631,6 +639,23 @@ def batch_specs(n, seed=0):
     return [ibl.spec_for(int(w), int(w) // 2) for w in widths]
 
 
+def batch_tc_flops(specs):
+    """Algorithmic flops of a precision batch: per probe, the planner's source
+    level per mip and for the irradiance, 2 flops x 4 channels per (output,
+    source) texel pair (the single-probe rule of tc_flops)."""
+    from althea_gb300 import ibl
+    total = 0
+    for s in specs:
+        iw, ih = s.irradiance_size or (0, 0)
+        levels, il = ibl.tc_plan(s.env_width, s.env_height, s.mip_sizes, s.roughness, iw)
+        for (w, h), lv in list(zip(s.mip_sizes, levels)) + [((iw, ih), il)]:
+            if lv < 0 or w == 0:
+                continue
+            ws, hs = max(s.env_width >> lv, 1), max(s.env_height >> lv, 1)
+            total += 2 * 4 * w * h * ws * hs
+    return total
+
+
 def batch_algorithmic_bytes(specs):
     total = 0
     for s in specs:
@@ -681,6 +706,14 @@ def run_batch(args):
     widths = {}
     for s in specs:
         widths[s.env_width] = widths.get(s.env_width, 0) + 1
+    tc_roofline = None
+    if precision:
+        tpeak, tkind = read_tensor_peak()
+        tflops = batch_tc_flops(specs) / (ms / 1e3) / 1e12
+        tc_roofline = {"bound": "tensor", "achieved": tflops, "peak": tpeak, "unit": "TFLOP/s",
+                       "frac": tflops / tpeak, "traffic": None,
+                       "kernel": "whole batch graph (algorithmic flops of every contraction)",
+                       "peak_source": tkind}
     path_desc = ("precision path (BF16 hi/lo tcgen05 contractions, RGBA16F outputs)" if precision
                  else f"plain path FP32, N=1024 {'Hammersley' if GENERATOR else 'reference-hash'}")
     line = {"metric": METRIC, "value": args.batch / (ms / 1e3), "unit": "probes/s",
@@ -695,8 +728,9 @@ def run_batch(args):
                 "tile": [info.tile_x, info.tile_y], "persistent_blocks": info.persistent_blocks,
                 "irradiance_target_blocks": info.irradiance_target_blocks,
                 "l2": "flushed (256 MB write) between timed steps"},
-            "gpu_launches": None,
-            "roofline": None if precision else {
+            "gpu_launches": (info.graph_kernels * args.steps if info.graph_kernels >= 0
+                             else None),
+            "roofline": tc_roofline if precision else {
                 "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": None, "kernel": "whole batch graph",
                 "peak_source": peak_kind},
@@ -737,10 +771,12 @@ def run_serve(args):
     best = max(r["throughput"] for r in rows)
     line = {"metric": METRIC, "value": best, "unit": "probes/s", "n_gpus": world,
             "steps": len(rows), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 hi/lo (fp32 accumulate)" if precision else "f32", "data": "synthetic",
             "config": {"workload": f"serving: Poisson re-bake requests, sizes uniform over "
                                    f"256..2048 wide (2:1), log2(W)-3 mips, 32x16 irradiance, "
-                                   f"N=1024, {args.inflight} slots, {args.budget_gb} GB budget, "
+                                   f"{'precision path' if precision else 'N=1024'}, "
+                                   f"{args.inflight} slots, {args.budget_gb} GB budget, "
                                    f"{args.pool} pre-generated maps (suns re-seeded per map), "
                                    "latency = completion callback - arrival, host pinned I/O",
                        "path": "tensor" if precision else "plain"},

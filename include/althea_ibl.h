@@ -260,6 +260,7 @@ typedef struct {
   int irradiance_target_blocks;
   int tuned;                 /* 1 if the choice came from timing (now or cached) */
   int graph;                 /* 1 once the bake is a captured CUDA graph */
+  int graph_kernels;         /* kernel launches in that graph (-1 before capture) */
 } althea_ibl_batch_info;
 
 typedef struct althea_ibl_batch althea_ibl_batch;
