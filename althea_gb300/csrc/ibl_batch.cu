@@ -191,6 +191,8 @@ constexpr TileShape kTileShapes[] = {{16, 8}, {32, 4}, {8, 8}, {16, 16}};
 constexpr int kNumTileShapes = 4;
 constexpr int kIrrTargets[] = {152 * 4, 152 * 8, 152 * 16};
 constexpr int kNumIrrTargets = 3;
+// Streams the precision bakes of a batch are spread over.
+constexpr int kTcLanes = 4;
 
 typedef void (*PfKernel)(const PfJob*, const long long*, int, long long, int, int, int,
                          unsigned long long*);
@@ -281,9 +283,14 @@ struct althea_ibl_batch {
   cudaStream_t exec_stream = nullptr;
   int graph_kernels = -1;  // kernel nodes of the captured bake (-1: not captured)
   // precision path (ALTHEA_IBL_BATCH_PRECISION): one tensor-core bake per
-  // probe after the shared chain pass; probes of one shape share a workspace
-  // (every launch is stream-ordered, so the bakes never overlap)
+  // probe after the shared chain pass.  The bakes run on kTcLanes streams
+  // forked from the caller's (joined back before the run ends), so the small
+  // contractions of different probes overlap on the GPU; probes of one shape
+  // on one lane share a workspace (their bakes are ordered on that lane).
   bool precision = false;
+  std::vector<cudaStream_t> lanes;
+  cudaEvent_t fork_ev = nullptr;
+  std::vector<cudaEvent_t> join_ev;
   int out_format = ALTHEA_IBL_FORMAT_RGBA32F;
   struct TcProbe {
     const float* chain;
@@ -292,7 +299,8 @@ struct althea_ibl_batch {
     float* irr;
     int irr_w, irr_h;
     size_t irr_pitch;
-    int ws;  // index into tc_ws
+    int ws;    // index into tc_ws
+    int lane;  // index into lanes
   };
   std::vector<TcProbe> tc;
   std::vector<void*> tc_ws;
@@ -314,6 +322,9 @@ void free_batch(althea_ibl_batch* b) {
   cudaFree(b->d_irr_texel_begins);
   cudaFree(b->d_partial);
   for (void* p : b->tc_ws) cudaFree(p);
+  for (cudaStream_t l : b->lanes) cudaStreamDestroy(l);
+  for (cudaEvent_t e : b->join_ev) cudaEventDestroy(e);
+  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
   delete b;
 }
 
@@ -457,12 +468,23 @@ int launch_irradiance_batch(althea_ibl_batch* b, cudaStream_t st) {
 }
 
 int launch_tc(althea_ibl_batch* b, cudaStream_t st) {
+  // fork: every lane starts after the chain pass on `st`
+  cudaError_t e = cudaEventRecord(b->fork_ev, st);
+  for (size_t l = 0; l < b->lanes.size() && e == cudaSuccess; ++l)
+    e = cudaStreamWaitEvent(b->lanes[l], b->fork_ev, 0);
+  if (e != cudaSuccess) return cuda_status(e, "precision lanes fork");
   int r = ALTHEA_IBL_OK;
   for (size_t i = 0; i < b->tc.size() && !r; ++i) {
     const althea_ibl_batch::TcProbe& p = b->tc[i];
     r = tc_bake(p.chain, p.w, p.h, p.mips.data(), (int)p.mips.size(), nullptr, p.irr, p.irr_w,
                 p.irr_h, p.irr_pitch, -1, b->tc_ws[p.ws], b->tc_ws_bytes[p.ws], b->out_format,
-                st);
+                b->lanes[p.lane]);
+  }
+  // join (also after an error, so that a stream capture can end cleanly)
+  for (size_t l = 0; l < b->lanes.size(); ++l) {
+    cudaError_t j = cudaEventRecord(b->join_ev[l], b->lanes[l]);
+    if (j == cudaSuccess) j = cudaStreamWaitEvent(st, b->join_ev[l], 0);
+    if (j != cudaSuccess && !r) r = cuda_status(j, "precision lanes join");
   }
   return r;
 }
@@ -655,6 +677,39 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
   }
   // ---- precision path: one planned tensor-core bake per probe --------------
   if (precision) {
+    // Lanes: longest-processing-time assignment by level-0 area.
+    const int nl = std::min(kTcLanes, n);
+    for (int l = 0; l < nl; ++l) {
+      cudaStream_t ls = nullptr;
+      cudaEvent_t ev = nullptr;
+      cudaError_t e = cudaStreamCreateWithFlags(&ls, cudaStreamNonBlocking);
+      if (e == cudaSuccess) b->lanes.push_back(ls);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e == cudaSuccess) b->join_ev.push_back(ev);
+      if (e != cudaSuccess) {
+        free_batch(b);
+        return cuda_status(e, "precision lanes");
+      }
+    }
+    {
+      cudaError_t e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+      if (e != cudaSuccess) {
+        free_batch(b);
+        return cuda_status(e, "precision lanes");
+      }
+    }
+    std::vector<int> order(n), lane_of(n, 0);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+      return (double)probes[a].env_width * probes[a].env_height >
+             (double)probes[c].env_width * probes[c].env_height;
+    });
+    std::vector<double> load(nl, 0.0);
+    for (int i : order) {
+      const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      lane_of[i] = l;
+      load[l] += (double)probes[i].env_width * probes[i].env_height;
+    }
     std::map<std::string, int> ws_of;
     for (int i = 0; i < n; ++i) {
       const althea_ibl_probe& p = probes[i];
@@ -678,7 +733,8 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
       t.irr_w = p.irradiance_dev ? p.irradiance_width : 0;
       t.irr_h = p.irradiance_dev ? p.irradiance_height : 0;
       t.irr_pitch = p.irradiance_pitch_bytes;
-      key << '|' << t.irr_w << 'x' << t.irr_h;
+      t.lane = lane_of[i];
+      key << '|' << t.irr_w << 'x' << t.irr_h << "#lane" << t.lane;
       auto it = ws_of.find(key.str());
       if (it == ws_of.end()) {
         const size_t bytes = tc_workspace_bytes(t.w, t.h, t.mips.data(), (int)t.mips.size(),
