@@ -632,12 +632,22 @@ __global__ void tables_kernel(const TableArgs a) {
 }
 
 // One RGBA32F source row -> 6 bf16 planes (R hi, R lo, G hi, G lo, B hi, B lo) in
-// phase order: out[plane][j][ph][u] = split(src[j][g u + ph]).  Block per
-// source row; the row is split into shared memory, then written out
-// contiguously.  Dynamic shared memory: 6 * ws bf16.
-__global__ void rows_kernel(const float4* __restrict__ src, int ws, int hs, int g,
-                           __nv_bfloat16* __restrict__ out) {
+// phase order: out[plane][j][ph][u] = split(src[j][g u + ph]), for every phase
+// count g the plan uses on this level (the row is read and split once).  Block
+// per source row; the row is split into shared memory, then written out
+// contiguously once per g.  Dynamic shared memory: 6 * ws bf16.
+constexpr int kMaxRowsOut = 8;
+struct RowsArgs {
+  const float4* src;
+  int ws, hs, n;
+  int g[kMaxRowsOut];
+  __nv_bfloat16* out[kMaxRowsOut];
+};
+
+__global__ void rows_kernel(const RowsArgs a) {
   extern __shared__ __nv_bfloat16 row_sm[];
+  const float4* __restrict__ src = a.src;
+  const int ws = a.ws, hs = a.hs;
   const int j = blockIdx.x;
   for (int x = threadIdx.x; x < ws; x += blockDim.x) {
     const float4 v = src[(size_t)j * ws + x];
@@ -650,11 +660,14 @@ __global__ void rows_kernel(const float4* __restrict__ src, int ws, int hs, int 
     }
   }
   __syncthreads();
-  const int krow = ws / g;
-  for (int e = threadIdx.x; e < 6 * ws; e += blockDim.x) {
-    const int p = e / ws, t = e - p * ws;
-    const int ph = t / krow, u = t - ph * krow;
-    out[((size_t)p * hs + j) * ws + t] = row_sm[p * ws + g * u + ph];
+  for (int q = 0; q < a.n; ++q) {
+    const int g = a.g[q], krow = ws / g;
+    __nv_bfloat16* __restrict__ out = a.out[q];
+    for (int e = threadIdx.x; e < 6 * ws; e += blockDim.x) {
+      const int p = e / ws, t = e - p * ws;
+      const int ph = t / krow, u = t - ph * krow;
+      out[((size_t)p * hs + j) * ws + t] = row_sm[p * ws + g * u + ph];
+    }
   }
 }
 
@@ -672,13 +685,35 @@ __global__ void __launch_bounds__(256) finish_kernel(const Job job, void* __rest
   float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
   double sw = 0.0;
   if (i < job.ho) {
+    // Four splits' loads in flight at a time; the sums keep the order k = w,
+    // w + 8, w + 16, ...
     const size_t plane = (size_t)job.wo * job.ho;
-    for (int k = w; k < job.ksplit; k += 8) {
-      const float* p = job.partial + (((size_t)k * 3) * job.wo + x) * job.ho + i;
-      s0 += p[0];
-      s1 += p[plane];
-      s2 += p[2 * plane];
-      if (job.kind == 0) sw += job.wsum_part[(size_t)k * job.ho + i];
+    constexpr int kU = 4;
+    for (int k0 = w; k0 < job.ksplit; k0 += 8 * kU) {
+      float v0[kU], v1[kU], v2[kU];
+      double vw[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int k = k0 + 8 * u;
+        v0[u] = v1[u] = v2[u] = 0.0f;
+        vw[u] = 0.0;
+        if (k < job.ksplit) {
+          const float* p = job.partial + (((size_t)k * 3) * job.wo + x) * job.ho + i;
+          v0[u] = p[0];
+          v1[u] = p[plane];
+          v2[u] = p[2 * plane];
+          if (job.kind == 0) vw[u] = job.wsum_part[(size_t)k * job.ho + i];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (k0 + 8 * u < job.ksplit) {
+          s0 += v0[u];
+          s1 += v1[u];
+          s2 += v2[u];
+          sw += vw[u];
+        }
+      }
     }
   }
   red[w][0][lane] = s0;
@@ -720,10 +755,13 @@ using namespace ibl::tc;
 
 namespace {
 
-// Source level per output mip / irradiance: the coarsest level whose measured
-// max relative error against the level-0 FP64 quadrature stayed <= 3e-4 on a
-// 4096x2048 map with 1e6 suns (sampled texels per mip), expressed as the
-// angular size of a source texel relative to the env: level = log2(W / target).
+// Source level per output mip / irradiance: the coarsest level whose max
+// relative error against the level-0 FP64 quadrature stays within 1e-3 on a
+// 4096x2048 map with 1e6 suns -- checked on every texel within 5 degrees of a
+// sun, the u = 0 seam, the pole rows and 1024 random texels per output --
+// expressed as the angular size of a source texel relative to the env:
+// level = log2(W / target).  Coarse source texels straddling the horizon of a
+// wide lobe cost the most: roughness 0.875 from level 3 reached 3.6e-3.
 int planned_level(int w, int ow, float roughness, bool irradiance) {
   // target source width by role (for a 4096-wide env: irradiance and rough
   // mips at level 1, glossy mips at level 2).
@@ -732,8 +770,6 @@ int planned_level(int w, int ow, float roughness, bool irradiance) {
     target = 2048;
   else if (roughness <= 0.55f)
     target = 1024;
-  else if (roughness >= 0.85f && roughness <= 0.90f)
-    target = 512;
   else
     target = 2048;
   // Scale with the env: the error depends on the angular size of a texel.
@@ -941,15 +977,30 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
   if (e != cudaSuccess) return cuda_status(e, "tc error flag");
   ChainTable tab;
   make_table(w, h, &tab);
-  for (auto& L : P.levels) {
-    const float4* src = reinterpret_cast<const float4*>(chain) + tab.off[L.level];
+  // One split pass per source level, writing every phase decomposition of it
+  // (up to kMaxRowsOut per pass).
+  std::vector<char> done(P.levels.size(), 0);
+  for (size_t a0 = 0; a0 < P.levels.size(); ++a0) {
+    if (done[a0]) continue;
+    const LevelPlanes& L = P.levels[a0];
+    RowsArgs ra;
+    memset(&ra, 0, sizeof(ra));
+    ra.src = reinterpret_cast<const float4*>(chain) + tab.off[L.level];
+    ra.ws = L.ws;
+    ra.hs = L.hs;
+    for (size_t a1 = a0; a1 < P.levels.size() && ra.n < kMaxRowsOut; ++a1) {
+      if (done[a1] || P.levels[a1].level != L.level) continue;
+      ra.g[ra.n] = P.levels[a1].g;
+      ra.out[ra.n] = reinterpret_cast<__nv_bfloat16*>(base + P.levels[a1].offset);
+      ++ra.n;
+      done[a1] = 1;
+    }
     const int sm = 6 * L.ws * 2;
     if (sm > 48 * 1024) {
       e = cudaFuncSetAttribute(rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
       if (e != cudaSuccess) return cuda_status(e, "tc rows smem attribute");
     }
-    rows_kernel<<<L.hs, 256, sm, s>>>(src, L.ws, L.hs, L.g,
-                                      reinterpret_cast<__nv_bfloat16*>(base + L.offset));
+    rows_kernel<<<L.hs, 256, sm, s>>>(ra);
   }
   // Direction tables of every job, one launch (FP64 transcendentals spread
   // over many SMs).

@@ -60,6 +60,21 @@ def make_env(w: int, h: int, seed: int = 0, sun_max: float = 1e4, n_suns: int = 
     return env
 
 
+def sun_params(w: int, h: int, seed: int = 0, sun_max: float = 1e4, n_suns: int = 8):
+    """The suns make_env(w, h, seed, sun_max, n_suns) draws: a list of
+    (unit direction, sigma in radians, radiance), replaying its PCG64 stream."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rng.lognormal(mean=0.0, sigma=1.0, size=(h, w))
+    suns = []
+    for _ in range(n_suns):
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        sigma = np.deg2rad(rng.uniform(1.0, 3.0))
+        lum = float(np.exp(rng.uniform(0.0, np.log(sun_max))))
+        suns.append((d, sigma, lum))
+    return suns
+
+
 def make_tinted_env(w: int, h: int, seed: int = 0) -> np.ndarray:
     """A small map whose channels differ (tests that channels stay apart)."""
     rng = np.random.Generator(np.random.PCG64(seed))

@@ -432,7 +432,7 @@ def tc_launches(levels, irr_level):
             levels.count(-1) + 1)
 
 
-def error_table(env, outs_by_path, irr_by_path, per_mip=12, seed=7):
+def error_table(env, outs_by_path, irr_by_path, per_mip=128, seed=7):
     """Max/mean relative error of each path against the FP64 quadrature over
     level 0 (oracle O2) on sampled texels of every mip with roughness > 0 and
     of the irradiance."""

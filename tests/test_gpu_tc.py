@@ -108,3 +108,27 @@ def test_half_outputs_are_the_float_outputs_rounded():
     assert torch.equal(irr32.half(), irr16)
     with pytest.raises(ibl.IBLError):  # mixed output types
         ibl.bake_tc(chain, w, h, [f32[0], f16[1]], rough[:2])
+
+
+def test_single_bright_texel_gives_the_ggx_lobe():
+    """Known answer through the tensor-core contraction: an env that is 0 but
+    for one texel prefilters to L w(n, t0) / sum_t w(n, t) (the normalised GGX
+    weight, written in numpy in tests/test_oracle.py)."""
+    from test_oracle import single_texel_lobe
+    w, h, L = 256, 128, 1000.0
+    x0, y0 = 85, 51
+    env = np.zeros((h, w, 4), dtype=np.float32)
+    env[y0, x0, :3] = L
+    env[..., 3] = 1.0
+    chain = ibl.build_env_chain(torch.from_numpy(env).cuda())
+    sizes, rough = [(64, 32), (32, 16)], [0.3, 0.8]
+    outs = [torch.empty((mh, mw, 4), dtype=torch.float32, device="cuda") for mw, mh in sizes]
+    ibl.bake_tc(chain, w, h, outs, rough, levels=[0, 0])
+    torch.cuda.synchronize()
+    for (mw, mh), r, o in zip(sizes, rough, outs):
+        ys, xs = np.mgrid[0:mh, 0:mw]
+        xy = np.stack([xs.ravel(), ys.ravel()], 1)
+        ref = L * single_texel_lobe(w, h, mw, mh, r, x0, y0, xy)
+        got = o.cpu().numpy()[..., 0].ravel()
+        assert np.allclose(got, ref, rtol=1e-4, atol=1e-6 * L), (r, np.abs(got - ref).max())
+        assert ref.max() > 1e-4 * L  # one texel of 32768 carries a visible share

@@ -119,6 +119,55 @@ def test_constant_env_known_answers():
     assert np.abs(qi[:, :3] - c).max() < 2e-3 * c  # piecewise-constant cosine quadrature
 
 
+def single_texel_lobe(w, h, ow, oh, r, x0, y0, xy):
+    """prefilter of an env that is 0 except texel (x0, y0): w(n, t0) / sum_t w(n, t),
+    with w = D_GGX(n.h; a2 = r^2) max(0, n.w_t) Omega_t, written here in numpy
+    from the definition (texel-centre directions, pitch-band solid angles)."""
+    yaw = np.pi * (2.0 * (np.arange(w) + 0.5) / w - 1.0)
+    pit = np.pi * ((np.arange(h) + 0.5) / h - 0.5)
+    edges = np.pi * (np.arange(h + 1) / h - 0.5)
+    omega = (2.0 * np.pi / w) * np.abs(np.diff(np.sin(edges)))
+    dirs = np.stack([np.cos(pit)[:, None] * np.cos(yaw)[None, :],
+                     np.broadcast_to(np.sin(pit)[:, None], (h, w)),
+                     np.cos(pit)[:, None] * np.sin(yaw)[None, :]], -1)
+    a2 = r * r
+    out = []
+    for x, y in xy:
+        ny, nx = np.pi * (y / oh - 0.5), np.pi * (2.0 * x / ow - 1.0)
+        n = np.array([np.cos(ny) * np.cos(nx), np.sin(ny), np.cos(ny) * np.sin(nx)])
+        c = dirs @ n
+        nh2 = 0.5 * (1.0 + c)
+        wgt = np.where(c > 0, a2 / (np.pi * (nh2 * (a2 - 1.0) + 1.0) ** 2) * c * omega[:, None], 0)
+        out.append(wgt[y0, x0] / wgt.sum())
+    return np.array(out)
+
+
+def test_single_bright_texel_gives_the_ggx_lobe():
+    """Known answer: one bright texel's prefilter response across output
+    directions is its normalised GGX weight w(n, t) (FP64 quadrature)."""
+    w, h, L = 64, 32, 1000.0
+    x0, y0 = 21, 13
+    env = np.zeros((h, w, 4), dtype=np.float32)
+    env[y0, x0, :3] = L
+    ys, xs = np.mgrid[0:8, 0:16]
+    xy = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
+    for r in (0.25, 0.6, 1.0):
+        got = oracle.quad_prefilter(env, 16, 8, r, xy)[:, 0]
+        ref = L * single_texel_lobe(w, h, 16, 8, r, x0, y0, xy)
+        assert np.allclose(got, ref, rtol=1e-9, atol=1e-12 * L), r
+        assert ref.max() > 1e-3 * L  # the lobe is actually sampled
+
+
+def test_lut_known_answer_grazing_free_mirror():
+    """At NoV -> 1 and roughness -> 0 the split-sum scale/bias tend to (1, 0)."""
+    n = 64
+    lut = oracle.brdf_lut_f64(n, 1024, oracle.LUT_CORRECTED)
+    scale, bias = lut[0, n - 1]  # row 0: roughness 0.5/n; column n-1: NoV (n-0.5)/n
+    assert abs(scale - 1.0) < 0.02 and abs(bias) < 0.02, (scale, bias)
+    asset = oracle.brdf_lut_f64(n, 1024, oracle.LUT_ASSET)
+    assert np.array_equal(asset[::-1], lut)  # the asset orientation is the row flip
+
+
 def test_roughness_zero_is_bilinear_resample():
     # a2 = 0: every kept sample is L = N, one bilinear tap of level 0.
     w, h = 64, 32
