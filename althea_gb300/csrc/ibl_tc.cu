@@ -10,6 +10,9 @@
 // averages of level 0), at the reference's texel-corner output directions.
 // The planner (althea_ibl_tc_plan) picks S per mip from a measured error
 // table so the result stays within 1e-3 of the same sum over level 0.
+// Outputs of at most kNarrowMax texels (the roughest mips) are summed on the
+// CUDA cores instead (narrow_kernel): as GEMMs they are a few rows by a few
+// columns, which the tensor cores would spend almost entirely on padding.
 //
 // Structure.  On an equirect map the weight of output texel (i, x) for source
 // texel (j, y) depends only on (i, j, d = y - s*x), s = W_src / W_out, through
@@ -599,6 +602,124 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
                  "r"((uint32_t)kTmemCols));
 }
 
+// ---- narrow outputs on the CUDA cores ----------------------------------------------
+// An output of at most kNarrowMax texels (the last, roughest mips) is a GEMM
+// with M and N of a few rows and columns against a K of a whole source level:
+// on the tensor cores nearly all of each MMA would be padding and the
+// per-stage latency would dominate.  These sum the same quadrature directly:
+// one lane per output texel, the eight warps of a block splitting the source
+// columns, a block per (32 outputs, band of source rows).  Weights in FP32
+// as in the contraction (cos of the column offset by angle addition), sums
+// over one source row in FP32, across rows and warps in FP64, splits combined
+// in FP64 by narrow_finish_kernel in a fixed order.
+constexpr int kNarrowMax = 128;
+constexpr int kNarrowThreads = 256;
+constexpr int kNarrowWarps = kNarrowThreads / 32;
+struct NarrowJob {
+  const float4* src;        // source level, RGBA32F, ws x hs
+  int ws, hs, wo, ho;
+  int ksplit;               // bands of source rows
+  float a2;
+  const float* src_rows;    // [hs][3]  cos q, sin q, Omega
+  const float* out_rows;    // [ho][2]  cos p, sin p
+  double* partial;          // [ksplit][wo * ho][4]  R, G, B, weight sum
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(kNarrowThreads) narrow_kernel(const NarrowJob J) {
+  extern __shared__ __align__(16) float nsm[];
+  float* cya = nsm;                                       // cos of source column yaw
+  float* sya = nsm + J.ws;                                // sin
+  float4* row = reinterpret_cast<float4*>(nsm + ((2 * J.ws + 3) & ~3));  // one source row
+  __shared__ double red[kNarrowWarps][4][32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n_out = J.wo * J.ho;
+  const int o = blockIdx.x * 32 + lane;
+  const bool live = o < n_out;
+  const int x = live ? o % J.wo : 0, i = live ? o / J.wo : 0;
+  for (int y = tid; y < J.ws; y += kNarrowThreads)
+    sincospif(2.0f * ((float)y + 0.5f) / (float)J.ws, &sya[y], &cya[y]);
+  float sb, cb;
+  sincospif(2.0f * (float)x / (float)J.wo, &sb, &cb);
+  const float cp = J.out_rows[2 * i], sp = J.out_rows[2 * i + 1];
+  const float alpha = 0.5f * (1.0f + J.a2), beta = 0.5f * (J.a2 - 1.0f), ka = J.a2 / kPiF;
+  const int j_per = (J.hs + J.ksplit - 1) / J.ksplit;
+  const int j0 = blockIdx.y * j_per, j1 = min(J.hs, j0 + j_per);
+  // warp w takes the columns [w ws / 8, (w + 1) ws / 8) of every row
+  const int c0 = warp * J.ws / kNarrowWarps, c1 = (warp + 1) * J.ws / kNarrowWarps;
+  double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, accw = 0.0;
+  for (int j = j0; j < j1; ++j) {
+    __syncthreads();  // the previous row is no longer read
+    const float4* srow = J.src + (size_t)j * J.ws;
+    for (int y = tid; y < J.ws; y += kNarrowThreads) row[y] = srow[y];
+    __syncthreads();
+    const float cq = J.src_rows[3 * j], sq = J.src_rows[3 * j + 1], om = J.src_rows[3 * j + 2];
+    const float A = cp * cq, B = sp * sq, k1 = KIND == 0 ? ka * om : om;
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, sw = 0.0f;
+    for (int y = c0; y < c1; ++y) {
+      const float cd = fmaf(cya[y], cb, sya[y] * sb);
+      const float c = fmaf(A, cd, B);
+      float wgt;
+      if (KIND == 0) {
+        const float d = fmaf(c, beta, alpha);
+        wgt = k1 * c * rcp_approx(d * d);
+      } else {
+        wgt = k1 * c;
+      }
+      wgt = fmaxf(wgt, 0.0f);
+      const float4 L = row[y];
+      s0 = fmaf(wgt, L.x, s0);
+      s1 = fmaf(wgt, L.y, s1);
+      s2 = fmaf(wgt, L.z, s2);
+      sw += wgt;
+    }
+    acc0 += s0;
+    acc1 += s1;
+    acc2 += s2;
+    accw += sw;
+  }
+  red[warp][0][lane] = acc0;
+  red[warp][1][lane] = acc1;
+  red[warp][2][lane] = acc2;
+  red[warp][3][lane] = accw;
+  __syncthreads();
+  if (warp == 0 && live) {
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < kNarrowWarps; ++w)
+      for (int c = 0; c < 4; ++c) t[c] += red[w][c][lane];
+    double* dst = J.partial + ((size_t)blockIdx.y * n_out + o) * 4;
+    for (int c = 0; c < 4; ++c) dst[c] = t[c];
+  }
+}
+
+// One warp per output texel: the splits in a fixed order (lane k takes k,
+// k + 32, ...; then a fixed shuffle tree), normalised, written.
+__global__ void narrow_finish_kernel(const NarrowJob J, int kind, void* __restrict__ out,
+                                     long long pitch, int out_half) {
+  const int o = blockIdx.x, lane = threadIdx.x;
+  const int n_out = J.wo * J.ho;
+  double t[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int k = lane; k < J.ksplit; k += 32) {
+    const double* p = J.partial + ((size_t)k * n_out + o) * 4;
+    for (int c = 0; c < 4; ++c) t[c] += p[c];
+  }
+  for (int off = 16; off > 0; off >>= 1)
+    for (int c = 0; c < 4; ++c) t[c] += __shfl_down_sync(0xffffffffu, t[c], off);
+  if (lane != 0) return;
+  const double norm = kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / t[3]);
+  const float r = (float)(t[0] * norm), g = (float)(t[1] * norm), b = (float)(t[2] * norm);
+  const int x = o % J.wo, i = o / J.wo;
+  if (out_half) {
+    const __half2 rg = __floats2half2_rn(r, g), ba = __floats2half2_rn(b, 1.0f);
+    uint2 v;
+    v.x = *reinterpret_cast<const uint32_t*>(&rg);
+    v.y = *reinterpret_cast<const uint32_t*>(&ba);
+    reinterpret_cast<uint2*>(out)[(long long)i * pitch + x] = v;
+  } else {
+    reinterpret_cast<float4*>(out)[(long long)i * pitch + x] = make_float4(r, g, b, 1.0f);
+  }
+}
+
 // Direction tables in FP64, stored as FP32: cos of the column offsets
 // (2 pi (d + 0.5) / ws), source rows (cos q, sin q, solid angle) and output
 // rows (cos p, sin p at texel corners).  One launch for every job of a bake:
@@ -788,6 +909,8 @@ struct LevelPlanes {
 struct JobPlan {
   Job J;
   int level = -1;  // index into TcPlan::levels; -1 = roughness 0 (plain path)
+  bool narrow = false;  // summed on the CUDA cores (narrow_kernel)
+  int src_level = 0;    // chain level of a narrow job's source
   size_t cosd_off = 0, rows_off = 0, orows_off = 0, partial_off = 0,
          wsum_off = 0;
 };
@@ -834,6 +957,28 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   } else {
     J.g = J.s;
     J.m = 8;
+  }
+  J.kind = kind;
+  J.a2 = roughness * roughness;
+  if (ow * oh <= kNarrowMax) {
+    // CUDA-core job: bands of source rows so that about four blocks run per SM
+    const int tiles = (ow * oh + 31) / 32;
+    int ks = (4 * 152 + tiles - 1) / tiles;
+    if (ks > J.hs) ks = J.hs;
+    J.ksplit = ks;
+    jp.narrow = true;
+    jp.level = -2;
+    jp.src_level = level;
+    jp.cosd_off = off;
+    off = al256(off + (size_t)J.ws * 4);
+    jp.rows_off = off;
+    off = al256(off + (size_t)J.hs * 12);
+    jp.orows_off = off;
+    off = al256(off + (size_t)oh * 8);
+    jp.partial_off = off;
+    off = al256(off + (size_t)ks * ow * oh * 4 * 8);
+    P.jobs.push_back(jp);
+    return ALTHEA_IBL_OK;
   }
   const int li = level_index(P, w, h, level, J.g, off);
   J.krow = J.ws / J.g;
@@ -1010,7 +1155,7 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     int nt = 0, nmax = 1;
     for (size_t k = 0; k < P.jobs.size(); ++k) {
       JobPlan& jp = P.jobs[k];
-      if (jp.level < 0) continue;
+      if (jp.level < 0 && !jp.narrow) continue;
       Job& J = jp.J;
       J.cos_d = reinterpret_cast<float*>(base + jp.cosd_off);
       J.src_rows = reinterpret_cast<float*>(base + jp.rows_off);
@@ -1028,6 +1173,50 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
   }
   for (size_t k = 0; k < P.jobs.size(); ++k) {
     JobPlan& jp = P.jobs[k];
+    void* out = nullptr;
+    long long pitch = 0;
+    if ((int)k < n) {
+      out = mips[k].out_dev;
+      pitch = (long long)(mips[k].pitch_bytes / texel);
+    } else {
+      out = irr_out;
+      pitch = (long long)(irr_pitch / texel);
+    }
+    if (jp.narrow) {
+      const Job& J = jp.J;
+      NarrowJob nj;
+      nj.src = reinterpret_cast<const float4*>(chain) + tab.off[jp.src_level];
+      nj.ws = J.ws;
+      nj.hs = J.hs;
+      nj.wo = J.wo;
+      nj.ho = J.ho;
+      nj.ksplit = J.ksplit;
+      nj.a2 = J.a2;
+      nj.src_rows = J.src_rows;
+      nj.out_rows = J.out_rows;
+      nj.partial = reinterpret_cast<double*>(base + jp.partial_off);
+      // dynamic part; with the 8 KB static reduction buffer it can pass the
+      // 48 KB default, so the limit is always raised to what this job needs
+      const int smem = ((2 * J.ws + 3) & ~3) * 4 + J.ws * 16;
+      const dim3 grid((J.wo * J.ho + 31) / 32, J.ksplit);
+      if (J.kind == 0) {
+        e = cudaFuncSetAttribute(narrow_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+        if (e != cudaSuccess) return cuda_status(e, "tc narrow smem attribute");
+        narrow_kernel<0><<<grid, kNarrowThreads, smem, s>>>(nj);
+      } else {
+        e = cudaFuncSetAttribute(narrow_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+        if (e != cudaSuccess) return cuda_status(e, "tc narrow smem attribute");
+        narrow_kernel<1><<<grid, kNarrowThreads, smem, s>>>(nj);
+      }
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return cuda_status(e, "tc narrow launch");
+      narrow_finish_kernel<<<J.wo * J.ho, 32, 0, s>>>(nj, J.kind, out, pitch, out_half);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return cuda_status(e, "tc narrow finish launch");
+      continue;
+    }
     if (jp.level < 0) continue;
     Job& J = jp.J;
     const LevelPlanes& L = P.levels[jp.level];
@@ -1051,20 +1240,15 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
       if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
       contract_kernel<1><<<grid, kThreads, smem, s>>>(J);
     }
-    void* out;
-    long long pitch;
-    if ((int)k < n) {
-      out = mips[k].out_dev;
-      pitch = (long long)(mips[k].pitch_bytes / texel);
-    } else {
-      out = irr_out;
-      pitch = (long long)(irr_pitch / texel);
-    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e, "tc contraction launch");
     finish_kernel<<<dim3((J.ho + 31) / 32, J.wo), 256, 0, s>>>(J, out, pitch);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e, "tc finish launch");
   }
   // Roughness-0 mips are a delta (no contraction): the reflected sample itself.
   for (int m = 0; m < n; ++m) {
-    if (P.jobs[m].level >= 0) continue;
+    if (P.jobs[m].level >= 0 || P.jobs[m].narrow) continue;
     st = launch_delta_mip(chain, w, h, &mips[m], out_half, s);
     if (st) return st;
   }

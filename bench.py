@@ -421,14 +421,20 @@ def tc_flops(levels, irr_level):
     return 2 * 4 * pairs, 2 * 9 * pairs
 
 
+# Outputs of at most this many texels are summed on the CUDA cores instead of
+# the tensor cores (the library's narrow-job limit).
+TC_NARROW_MAX = 128
+
+
 def tc_launches(levels, irr_level):
-    """Kernels of one precision probe step: chain blits, one split+phase pass per
-    (level, g), one tables pass, contraction + finish per job, one delta pass per
+    """Kernels of one precision probe step: chain blits, one split pass per
+    source level of a tensor-core job, one tables pass, two kernels per job
+    (contraction + finish, or the narrow sum + its finish), one delta pass per
     roughness-0 mip, the LUT."""
     from althea_gb300 import ibl
     jobs = tc_jobs(levels, irr_level)
-    groups = {(lv, g) for _, _, _, _, lv, g in jobs}
-    return ((ibl.chain_levels(ENV_W, ENV_H) - 1) + len(groups) + 1 + 2 * len(jobs) +
+    split_levels = {lv for w, h, _, _, lv, _ in jobs if w * h > TC_NARROW_MAX}
+    return ((ibl.chain_levels(ENV_W, ENV_H) - 1) + len(split_levels) + 1 + 2 * len(jobs) +
             levels.count(-1) + 1)
 
 
@@ -449,6 +455,7 @@ def error_table(env, outs_by_path, irr_by_path, per_mip=128, seed=7):
         for k, outs in outs_by_path.items():
             got = outs[m][xy[:, 1], xy[:, 0], :3]
             e = np.abs(got - ref) / np.abs(ref)
+            e = np.where(np.isfinite(got), e, np.inf)  # a missing output is a failure
             res[k][f"mip{m}"] = [float(e.max()), float(e.mean())]
     idx = rng.choice(IRR_W * IRR_H, size=per_mip, replace=False)
     xy = np.stack([idx % IRR_W, idx // IRR_W], 1).astype(np.int32)
@@ -456,6 +463,7 @@ def error_table(env, outs_by_path, irr_by_path, per_mip=128, seed=7):
     for k, irr in irr_by_path.items():
         got = irr[xy[:, 1], xy[:, 0], :3]
         e = np.abs(got - ref) / np.abs(ref)
+        e = np.where(np.isfinite(got), e, np.inf)
         res[k]["irradiance"] = [float(e.max()), float(e.mean())]
     for k in res:
         res[k]["max"] = max(v[0] for v in res[k].values())
@@ -616,7 +624,8 @@ def run_tc(args):
                              "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
                              "kernel": "contract_kernel (every contraction of one bake; the "
                                        "timed stage also holds the split, tables, finish and "
-                                       "delta kernels)",
+                                       "delta kernels, and the outputs of <= 128 texels, "
+                                       "summed on the CUDA cores)",
                              "peak_source": peak_kind + " (bf16 burst)",
                              "algorithmic_flops_per_bake": alg_flops,
                              "executed_split_flops_per_bake": split_flops,

@@ -59,6 +59,7 @@ def texel_set(ow, oh, suns, rng, per, sun_deg, cap):
 def errors(got, ref):
     scale = 1e-6 * np.abs(ref).max()
     e = np.abs(got - ref) / np.maximum(np.abs(ref), scale)
+    e = np.where(np.isfinite(got), e, np.inf)  # a missing output is a failure
     return {"max": float(e.max()), "mean": float(e.mean()),
             "p99.99": float(np.percentile(e, 99.99))}
 
