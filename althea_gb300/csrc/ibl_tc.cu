@@ -603,62 +603,82 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
 }
 
 // ---- narrow outputs on the CUDA cores ----------------------------------------------
-// An output of at most kNarrowMax texels (the last, roughest mips) is a GEMM
-// with M and N of a few rows and columns against a K of a whole source level:
-// on the tensor cores nearly all of each MMA would be padding and the
-// per-stage latency would dominate.  These sum the same quadrature directly:
-// one lane per output texel, the eight warps of a block splitting the source
-// columns, a block per (32 outputs, band of source rows).  Weights in FP32
-// as in the contraction (cos of the column offset by angle addition), sums
-// over one source row in FP32, across rows and warps in FP64, splits combined
-// in FP64 by narrow_finish_kernel in a fixed order.
+// An output of at most kNarrowMax texels and kNarrowMaxW columns (the
+// roughest mips) is a GEMM with M and N of a few rows and columns against a K
+// of a whole source level: on the tensor cores most of each MMA would be
+// padding.  These sum the same quadrature on the CUDA cores, sharing weights:
+// the weight of output (i, x) and source (j, y) depends on (i, j) and the
+// column offset t = (y - s x) mod ws only.  A block takes one output row i and
+// a band of source rows; per source row it stages the row and the ws weights
+// of row i (computed once, with their sum, which is the same for every x).
+// Lanes are output columns (x = lane mod wo; with wo < 32 the lanes of one x
+// split the columns further): each walks source columns y, reading the staged
+// texel L[y] (one address per warp, a broadcast) and the weight W[t].  The
+// weights are stored skewed, W[t] at t + t / s, which puts the lanes' t
+// (s apart) in different banks.  FP32 within a row, FP64 across rows, a fixed
+// order across warps; bands are combined by narrow_finish_kernel.  Measured
+// on a 2048-wide source: 16x8 in 129 us (the tensor path: 334 us), 8x4 in
+// 81 us (414 us); a 32x16 output took 405 us here against 323 us on the
+// tensor cores, hence the 128-texel limit.
 constexpr int kNarrowMax = 128;
+constexpr int kNarrowMaxW = 32;
 constexpr int kNarrowThreads = 256;
 constexpr int kNarrowWarps = kNarrowThreads / 32;
 struct NarrowJob {
   const float4* src;        // source level, RGBA32F, ws x hs
   int ws, hs, wo, ho;
+  int s;                    // ws / wo
   int ksplit;               // bands of source rows
   float a2;
+  const float* cos_d;       // [ws]  cos(2 pi (d + 0.5) / ws)
   const float* src_rows;    // [hs][3]  cos q, sin q, Omega
   const float* out_rows;    // [ho][2]  cos p, sin p
   double* partial;          // [ksplit][wo * ho][4]  R, G, B, weight sum
 };
 
+// Dynamic shared memory of narrow_kernel: the staged row (ws float4), the
+// skewed weights (ws + wo floats), the cos table (ws floats), both float
+// arrays rounded up to a multiple of 4, and the per-lane FP64 sums of the
+// final reduction (8 warps x 32 lanes x 3).
+__host__ __device__ inline size_t narrow_smem_bytes(int ws, int wo) {
+  const size_t wsk = (size_t)((ws + wo + 3) & ~3), cdn = (size_t)((ws + 3) & ~3);
+  return (size_t)ws * 16 + (wsk + cdn) * 4 + (size_t)kNarrowThreads * 3 * 8;
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kNarrowThreads) narrow_kernel(const NarrowJob J) {
-  extern __shared__ __align__(16) float nsm[];
-  float* cya = nsm;                                       // cos of source column yaw
-  float* sya = nsm + J.ws;                                // sin
-  float4* row = reinterpret_cast<float4*>(nsm + ((2 * J.ws + 3) & ~3));  // one source row
-  __shared__ double red[kNarrowWarps][4][32];
+  extern __shared__ __align__(16) unsigned char nsm[];
+  const int ws = J.ws, wo = J.wo, s = J.s;
+  float4* row = reinterpret_cast<float4*>(nsm);        // staged L_j
+  float* Wsk = reinterpret_cast<float*>(row + ws);      // weights of (i, j), skewed
+  float* cd = Wsk + ((ws + wo + 3) & ~3);               // cos_d
+  double* fin = reinterpret_cast<double*>(cd + ((ws + 3) & ~3));  // [256][3]
+  __shared__ float red[kNarrowWarps];
+  __shared__ double wsum_sh;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int n_out = J.wo * J.ho;
-  const int o = blockIdx.x * 32 + lane;
-  const bool live = o < n_out;
-  const int x = live ? o % J.wo : 0, i = live ? o / J.wo : 0;
-  for (int y = tid; y < J.ws; y += kNarrowThreads)
-    sincospif(2.0f * ((float)y + 0.5f) / (float)J.ws, &sya[y], &cya[y]);
-  float sb, cb;
-  sincospif(2.0f * (float)x / (float)J.wo, &sb, &cb);
+  const int i = blockIdx.x;
+  // lane -> (output column x, sub-range r of the warp's source columns)
+  const int R = 32 / wo, x = lane % wo, r = lane / wo;
+  const bool lane_live = r < R;
+  // this lane's source columns: warp range split into R contiguous pieces
+  const int wy0 = warp * ws / kNarrowWarps, wy1 = (warp + 1) * ws / kNarrowWarps;
+  const int y0 = wy0 + r * (wy1 - wy0) / R, y1 = wy0 + (r + 1) * (wy1 - wy0) / R;
+  for (int t = tid; t < ws; t += kNarrowThreads) cd[t] = J.cos_d[t];
   const float cp = J.out_rows[2 * i], sp = J.out_rows[2 * i + 1];
   const float alpha = 0.5f * (1.0f + J.a2), beta = 0.5f * (J.a2 - 1.0f), ka = J.a2 / kPiF;
   const int j_per = (J.hs + J.ksplit - 1) / J.ksplit;
   const int j0 = blockIdx.y * j_per, j1 = min(J.hs, j0 + j_per);
-  // warp w takes the columns [w ws / 8, (w + 1) ws / 8) of every row
-  const int c0 = warp * J.ws / kNarrowWarps, c1 = (warp + 1) * J.ws / kNarrowWarps;
-  double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, accw = 0.0;
+  const int sx = (int)(((long long)s * x) % ws);
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, wsum = 0.0;
   for (int j = j0; j < j1; ++j) {
-    __syncthreads();  // the previous row is no longer read
-    const float4* srow = J.src + (size_t)j * J.ws;
-    for (int y = tid; y < J.ws; y += kNarrowThreads) row[y] = srow[y];
-    __syncthreads();
+    __syncthreads();  // the previous row and weights are no longer read
+    const float4* srow = J.src + (size_t)j * ws;
+    for (int y = tid; y < ws; y += kNarrowThreads) row[y] = srow[y];
     const float cq = J.src_rows[3 * j], sq = J.src_rows[3 * j + 1], om = J.src_rows[3 * j + 2];
     const float A = cp * cq, B = sp * sq, k1 = KIND == 0 ? ka * om : om;
-    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, sw = 0.0f;
-    for (int y = c0; y < c1; ++y) {
-      const float cd = fmaf(cya[y], cb, sya[y] * sb);
-      const float c = fmaf(A, cd, B);
+    float part = 0.0f;
+    for (int t = tid; t < ws; t += kNarrowThreads) {
+      const float c = fmaf(A, cd[t], B);
       float wgt;
       if (KIND == 0) {
         const float d = fmaf(c, beta, alpha);
@@ -667,28 +687,61 @@ __global__ void __launch_bounds__(kNarrowThreads) narrow_kernel(const NarrowJob 
         wgt = k1 * c;
       }
       wgt = fmaxf(wgt, 0.0f);
-      const float4 L = row[y];
-      s0 = fmaf(wgt, L.x, s0);
-      s1 = fmaf(wgt, L.y, s1);
-      s2 = fmaf(wgt, L.z, s2);
-      sw += wgt;
+      Wsk[t + t / s] = wgt;
+      part += wgt;
     }
-    acc0 += s0;
-    acc1 += s1;
-    acc2 += s2;
-    accw += sw;
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    if (tid == 0) {
+      float rs = 0.0f;
+      for (int w = 0; w < kNarrowWarps; ++w) rs += red[w];
+      wsum += rs;
+    }
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+    if (lane_live) {
+      // segments of y that stay inside one block of s weights
+      for (int yc = y0; yc < y1;) {
+        int t0 = yc - sx;
+        if (t0 < 0) t0 += ws;
+        const int seg = min(y1 - yc, s - t0 % s);
+        const float* wp = Wsk + t0 + t0 / s;
+        const float4* lp = row + yc;
+#pragma unroll 4
+        for (int k = 0; k < seg; ++k) {
+          const float w = wp[k];
+          const float4 L = lp[k];
+          s0 = fmaf(w, L.x, s0);
+          s1 = fmaf(w, L.y, s1);
+          s2 = fmaf(w, L.z, s2);
+        }
+        yc += seg;
+      }
+    }
+    a0 += s0;
+    a1 += s1;
+    a2 += s2;
   }
-  red[warp][0][lane] = acc0;
-  red[warp][1][lane] = acc1;
-  red[warp][2][lane] = acc2;
-  red[warp][3][lane] = accw;
+  // every (warp, r) holds a partial sum of its columns for output x
+  fin[3 * tid] = a0;
+  fin[3 * tid + 1] = a1;
+  fin[3 * tid + 2] = a2;
+  if (tid == 0) wsum_sh = wsum;
   __syncthreads();
-  if (warp == 0 && live) {
-    double t[4] = {0.0, 0.0, 0.0, 0.0};
+  if (tid < wo) {
+    double t0 = 0.0, t1 = 0.0, t2 = 0.0;
     for (int w = 0; w < kNarrowWarps; ++w)
-      for (int c = 0; c < 4; ++c) t[c] += red[w][c][lane];
-    double* dst = J.partial + ((size_t)blockIdx.y * n_out + o) * 4;
-    for (int c = 0; c < 4; ++c) dst[c] = t[c];
+      for (int rr = 0; rr < R; ++rr) {
+        const int src_t = 32 * w + rr * wo + tid;
+        t0 += fin[3 * src_t];
+        t1 += fin[3 * src_t + 1];
+        t2 += fin[3 * src_t + 2];
+      }
+    double* dst = J.partial + ((size_t)blockIdx.y * wo * J.ho + (size_t)i * wo + tid) * 4;
+    dst[0] = t0;
+    dst[1] = t1;
+    dst[2] = t2;
+    dst[3] = wsum_sh;
   }
 }
 
@@ -960,10 +1013,10 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   }
   J.kind = kind;
   J.a2 = roughness * roughness;
-  if (ow * oh <= kNarrowMax) {
-    // CUDA-core job: bands of source rows so that about four blocks run per SM
-    const int tiles = (ow * oh + 31) / 32;
-    int ks = (4 * 152 + tiles - 1) / tiles;
+  if (ow * oh <= kNarrowMax && ow <= kNarrowMaxW && 32 % ow == 0) {
+    // CUDA-core job: one block per (output row, band of source rows), about
+    // four blocks per SM
+    int ks = (4 * 152 + oh - 1) / oh;
     if (ks > J.hs) ks = J.hs;
     J.ksplit = ks;
     jp.narrow = true;
@@ -1190,15 +1243,17 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
       nj.hs = J.hs;
       nj.wo = J.wo;
       nj.ho = J.ho;
+      nj.s = J.ws / J.wo;
       nj.ksplit = J.ksplit;
       nj.a2 = J.a2;
+      nj.cos_d = J.cos_d;
       nj.src_rows = J.src_rows;
       nj.out_rows = J.out_rows;
       nj.partial = reinterpret_cast<double*>(base + jp.partial_off);
       // dynamic part; with the 8 KB static reduction buffer it can pass the
       // 48 KB default, so the limit is always raised to what this job needs
-      const int smem = ((2 * J.ws + 3) & ~3) * 4 + J.ws * 16;
-      const dim3 grid((J.wo * J.ho + 31) / 32, J.ksplit);
+      const int smem = (int)narrow_smem_bytes(J.ws, J.wo);
+      const dim3 grid(J.ho, J.ksplit);
       if (J.kind == 0) {
         e = cudaFuncSetAttribute(narrow_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem);

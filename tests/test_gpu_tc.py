@@ -141,10 +141,11 @@ def test_narrow_outputs_on_wide_source_levels():
     env = synth.make_env(w, h, seed=21, sun_max=1e6)
     chain_np = oracle.build_chain(env)
     chain = torch.from_numpy(chain_np).cuda()
-    sizes, rough = [(16, 8), (8, 4), (4, 2)], [0.875, 1.0, 0.6]
+    sizes, rough = [(32, 16), (16, 8), (8, 4), (4, 2)], [0.75, 0.875, 1.0, 0.6]
     outs = [torch.full((mh, mw, 4), float("nan"), device="cuda") for mw, mh in sizes]
     irr = torch.full((4, 8, 4), float("nan"), device="cuda")
-    ibl.bake_tc(chain, w, h, outs, rough, irradiance=irr, levels=[0, 0, 0], irradiance_level=0)
+    ibl.bake_tc(chain, w, h, outs, rough, irradiance=irr, levels=[0, 0, 0, 0],
+                irradiance_level=0)
     torch.cuda.synchronize()
     lvl0 = oracle.chain_level(chain_np, w, h, 0)
     for (mw, mh), r, o in zip(sizes, rough, outs):
@@ -153,7 +154,9 @@ def test_narrow_outputs_on_wide_source_levels():
         ref = oracle.quad_prefilter(lvl0, mw, mh, r, xy)[:, :3]
         got = o.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
         assert np.isfinite(got).all()
-        assert _rel(got, ref).max() <= 1e-5, (mw, _rel(got, ref).max())
+        # FP32 weights on the CUDA cores (<= 128 texels); BF16 hi/lo beyond
+        tol = 1e-5 if mw * mh <= 128 else 1e-4
+        assert _rel(got, ref).max() <= tol, (mw, _rel(got, ref).max())
     ys, xs = np.mgrid[0:4, 0:8]
     xy = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
     ref = oracle.quad_irradiance(lvl0, 8, 4, xy)[:, :3]
