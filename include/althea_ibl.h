@@ -172,7 +172,8 @@ const float* althea_ibl_env_chain(const althea_ibl_context* ctx);
 int althea_ibl_bake(althea_ibl_context* ctx, const althea_ibl_outputs* outs, void* stream);
 
 /* ---- precision path: dense contraction on the tensor cores -------------------
- * Replaces the two estimators of Shaders/IBL_Precompute/*.comp by the
+ * Replaces the two estimators of Shaders/IBL_Precompute (GenIrradianceMap.comp,
+ * PreFilterEnvMap.comp) by the
  * quadrature they estimate: prefilter(n) = sum_t L_t w / sum_t w with
  * w = D_GGX(n.h) max(0, n.w_t) Omega_t, irradiance(n) = (1/pi) sum_t L_t
  * max(0, n.w_t) Omega_t, over the texels of one env level per output (picked
