@@ -109,3 +109,16 @@ def test_c_abi_rejects_bad_arguments_without_gpu():
     ptrs = (ctypes.c_void_p * 2)(8, 16)
     pitch = (ctypes.c_size_t * 2)(12, 64)  # 12 bytes: not a whole texel
     assert L.althea_ssr_convolve_levels(ptrs, pitch, 1, 1, 2, None) == ibl.ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.skipif(oracle.ref_lib() is None, reason="oracle/_ref not built on this machine")
+def test_ref_shader_agrees_on_random_case():
+    """The reference shader compiled as C++ here and the C restatement agree on
+    a fresh random case (beyond the committed fixtures)."""
+    rng = np.random.default_rng(77)
+    for w, h in [(50, 29), (128, 64), (3, 97)]:
+        l0 = (rng.lognormal(0.0, 2.0, (h, w, 4)) * rng.choice([-1.0, 1.0], (h, w, 4)))
+        l0 = l0.astype(np.float16)
+        a = oracle.ssr_convolve(l0, 6)
+        b = oracle.ref_ssr_convolve(l0, 6)
+        assert np.array_equal(a.view(np.uint16), b.view(np.uint16)), (w, h)
