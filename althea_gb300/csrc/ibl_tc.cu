@@ -152,19 +152,41 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// Bounded wait: false when the abort flag is up or after kWaitNs (which
+// Bounded wait: false when the abort flag is up or after `limit_ns` (which
 // raises the flag so every other role stops too).
-__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, volatile int* abort) {
+__device__ __forceinline__ bool wait_bar_for(uint64_t* bar, uint32_t parity, volatile int* abort,
+                                             unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (;;) {
     if (mbar_try_wait_sleep(bar, parity, kSleepNs)) return true;
     if (*abort) return false;
-    if (global_ns() - t0 > kWaitNs) {
+    if (global_ns() - t0 > limit_ns) {
       *abort = 1;
       return false;
     }
   }
+}
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  return wait_bar_for(bar, parity, abort, kWaitNs);
+}
+
+// Self-test of the bounded wait: an mbarrier that nothing completes is waited
+// on with a short limit; the wait must give up, raise the abort flag and let
+// the kernel report through an error word and return.
+__global__ void wait_selftest_kernel(int* result, unsigned long long limit_ns) {
+  __shared__ uint64_t bar;
+  __shared__ int abort_sh;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  abort_sh = 0;
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  const unsigned long long t0 = global_ns();
+  const bool completed = wait_bar_for(&bar, 0u, &abort_sh, limit_ns);
+  const unsigned long long waited = global_ns() - t0;
+  result[0] = completed ? 0 : 1;        // 1: the wait gave up
+  result[1] = abort_sh;                 // 1: the abort flag went up
+  result[2] = (int)(waited / 1000000);  // milliseconds waited
 }
 
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
@@ -1319,6 +1341,31 @@ size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n
 }
 
 }  // namespace ibl
+
+extern "C" int althea_ibl_tc_wait_selftest(unsigned long long limit_ns, int* waited_ms,
+                                           void* stream) {
+  if (limit_ns == 0 || limit_ns > 1000000000ull)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "wait self-test: limit 1 ns .. 1 s");
+  int* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, 3 * sizeof(int));
+  if (e != cudaSuccess) return cuda_status(e, "wait self-test buffer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int h[3] = {0, 0, 0};
+  e = cudaMemsetAsync(d, 0, 3 * sizeof(int), s);
+  if (e == cudaSuccess) {
+    wait_selftest_kernel<<<1, 32, 0, s>>>(d, limit_ns);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_status(e, "wait self-test");
+  if (waited_ms) *waited_ms = h[2];
+  if (h[0] != 1 || h[1] != 1)
+    return set_error(ALTHEA_IBL_ERR_CUDA, "wait self-test: the wait did not give up (%d, %d)",
+                     h[0], h[1]);
+  return ALTHEA_IBL_OK;
+}
 
 extern "C" int althea_ibl_bake_tc(const float* chain, int w, int h,
                                   const althea_ibl_mip_target* mips, int n, const int* levels,

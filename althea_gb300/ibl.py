@@ -180,6 +180,7 @@ def load(build_if_missing: bool = True):
         "althea_ibl_bake_tc": (i, [vp, i, i, ctypes.POINTER(MipTarget), i, ctypes.POINTER(i),
                                    vp, i, i, sz, i, vp, sz, vp]),
         "althea_ibl_tc_error": (i, [vp, vp]),
+        "althea_ibl_tc_wait_selftest": (i, [ctypes.c_ulonglong, ctypes.POINTER(i), vp]),
         "althea_ibl_bake_tc_ex": (i, [vp, i, i, ctypes.POINTER(MipTarget), i, ctypes.POINTER(i),
                                       vp, i, i, sz, i, vp, sz, i, vp]),
         "althea_ssr_level_offset": (sz, [i, i, i]),
@@ -602,6 +603,16 @@ def tc_plan(w: int, h: int, mip_sizes: List[tuple], roughness: List[float],
     il = ctypes.c_int()
     _check(load().althea_ibl_tc_plan(w, h, arr, n, irradiance_width, lv, ctypes.byref(il)))
     return [lv[k] for k in range(n)], il.value
+
+
+def tc_wait_selftest(limit_ms: float = 20.0, stream=None) -> int:
+    """Runs the precision kernel's bounded wait against a barrier nothing
+    completes; raises IBLError unless it gave up and reported.  Returns the
+    milliseconds it waited."""
+    waited = ctypes.c_int(0)
+    _check(load().althea_ibl_tc_wait_selftest(int(limit_ms * 1e6), ctypes.byref(waited),
+                                              _stream_ptr(stream)))
+    return waited.value
 
 
 def bake_tc(chain, w: int, h: int, outs: List, roughness: List[float], irradiance=None,

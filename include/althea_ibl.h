@@ -197,6 +197,12 @@ int althea_ibl_bake_tc(const float* chain_dev, int env_width, int env_height,
                        size_t irradiance_pitch_bytes, int irradiance_level, void* workspace_dev,
                        size_t workspace_bytes, void* stream);
 int althea_ibl_tc_error(const void* workspace_dev, void* stream);
+/* Diagnostics: runs the precision kernel's bounded mbarrier wait on a barrier
+ * that nothing completes, with a limit of limit_ns (1 ns .. 1 s).  Returns
+ * ALTHEA_IBL_OK when the wait gave up, raised its abort flag and the kernel
+ * returned (the context stays usable); *waited_ms = the time it waited.
+ * Synchronises the stream. */
+int althea_ibl_tc_wait_selftest(unsigned long long limit_ns, int* waited_ms, void* stream);
 
 /* Output formats of althea_ibl_bake_tc_ex (every mip and the irradiance). */
 #define ALTHEA_IBL_FORMAT_RGBA32F 0   /* 16-byte texels, as althea_ibl_bake_tc */

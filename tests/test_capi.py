@@ -76,3 +76,9 @@ def test_python_errors_carry_status():
     with pytest.raises(ibl.IBLError) as e:
         ibl._check(ibl.ERR_UNSUPPORTED)
     assert e.value.status == ibl.ERR_UNSUPPORTED
+
+
+def test_wait_selftest_rejects_bad_limits_without_gpu():
+    L = ibl.load()
+    assert L.althea_ibl_tc_wait_selftest(0, None, None) == ibl.ERR_INVALID_ARGUMENT
+    assert L.althea_ibl_tc_wait_selftest(2 * 10**9, None, None) == ibl.ERR_INVALID_ARGUMENT

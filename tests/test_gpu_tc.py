@@ -162,3 +162,13 @@ def test_narrow_outputs_on_wide_source_levels():
     ref = oracle.quad_irradiance(lvl0, 8, 4, xy)[:, :3]
     got = irr.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
     assert np.isfinite(got).all() and _rel(got, ref).max() <= 1e-5
+
+
+def test_bounded_wait_gives_up_and_reports():
+    """Failure detection without a fault: the kernel's mbarrier wait on a
+    barrier that nothing completes gives up after its limit, raises the abort
+    flag and returns; the context stays usable for a normal bake after it."""
+    waited = ibl.tc_wait_selftest(limit_ms=20.0)
+    assert 20 <= waited < 1000
+    test_half_outputs_are_the_float_outputs_rounded()
+
