@@ -956,15 +956,18 @@ namespace {
 // 4096x2048 map with 1e6 suns -- checked on every texel within 5 degrees of a
 // sun, the u = 0 seam, the pole rows and 1024 random texels per output --
 // expressed as the angular size of a source texel relative to the env:
-// level = log2(W / target).  Coarse source texels straddling the horizon of a
-// wide lobe cost the most: roughness 0.875 from level 3 reached 3.6e-3.
+// level = log2(W / target).  The error grows with the roughness for a given
+// source width (a 1024-wide source: 1.8e-4 at r = 0.14, 6.5e-4 at 0.29, 7.6e-4
+// at 0.375, 9.6e-4 at 0.5 and 1.1e-3 at 0.43 on a 2048-wide map), hence the
+// finer source above r = 0.40; roughness 0.875 from a 512-wide source
+// reached 3.6e-3.
 int planned_level(int w, int ow, float roughness, bool irradiance) {
   // target source width by role (for a 4096-wide env: irradiance and rough
   // mips at level 1, glossy mips at level 2).
   int target;
   if (irradiance)
     target = 2048;
-  else if (roughness <= 0.55f)
+  else if (roughness <= 0.40f)
     target = 1024;
   else
     target = 2048;

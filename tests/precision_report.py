@@ -12,6 +12,7 @@ Error per channel: |x - ref| / max(|ref|, 1e-6 max|ref|); the table gives
 max, mean and the 99.99th percentile per output.
 
 Usage: python tests/precision_report.py [--per-mip N] [--sun-deg D] [--cap C]
+                                       [--env-width 4096|2048|1024|512|256]
 """
 import argparse
 import json
@@ -27,10 +28,19 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 from althea_gb300 import ibl, synth  # noqa: E402
 
-ENV_W, ENV_H, SUN_MAX, SEED = 4096, 2048, 1e6, 0
-MIPS = [(2048 >> m, 1024 >> m) for m in range(9)]
-ROUGH = [m / 8 for m in range(9)]
-IRR = (128, 64)
+SUN_MAX = 1e6
+
+
+def config(env_w):
+    """The benchmark map (4096 wide: 9 mips from W/2, 128x64 irradiance) or a
+    batch-configuration probe (log2(W) - 3 mips from W/2, 32x16 irradiance)."""
+    if env_w == 4096:
+        mips, irr = [(2048 >> m, 1024 >> m) for m in range(9)], (128, 64)
+    else:
+        n = env_w.bit_length() - 1 - 3
+        mips, irr = [((env_w // 2) >> m, (env_w // 4) >> m) for m in range(n)], (32, 16)
+    rough = [m / (len(mips) - 1) for m in range(len(mips))]
+    return env_w, env_w // 2, mips, rough, irr
 
 
 def out_dirs(ow, oh):
@@ -70,7 +80,12 @@ def main():
     ap.add_argument("--per-mip", type=int, default=1024)
     ap.add_argument("--sun-deg", type=float, default=5.0)
     ap.add_argument("--cap", type=int, default=4096)
+    ap.add_argument("--env-width", type=int, default=4096,
+                    help="4096: the benchmark map; 256..2048: a batch-configuration probe")
+    ap.add_argument("--seed", type=int, default=0, help="map seed (the benchmark uses 0)")
     args = ap.parse_args()
+    SEED = args.seed
+    ENV_W, ENV_H, MIPS, ROUGH, IRR = config(args.env_width)
     env = synth.make_env(ENV_W, ENV_H, seed=SEED, sun_max=SUN_MAX)
     suns = synth.sun_params(ENV_W, ENV_H, seed=SEED, sun_max=SUN_MAX)
     chain = ibl.build_env_chain(torch.from_numpy(env).cuda())
