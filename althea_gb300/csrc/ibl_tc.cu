@@ -304,6 +304,15 @@ struct Job {
   double* wsum_part;         // [ksplit][ho]  (kind 0)
   int* error;                // set when a bounded wait gave up
   int out_half;              // 1: outputs are RGBA16F (8-byte texels), else RGBA32F
+  // A second output of the same geometry (same source level, phase count,
+  // columns) in TMEM lanes 64-127, so that two outputs of <= 64 rows fill one
+  // M = 128 tile: they share every radiance operand, only the weights differ.
+  int pair;                  // 1: lanes 64-127 hold the second output
+  int ho_b, kind_b;
+  float a2_b;
+  const float* out_rows_b;   // [ho_b][2]
+  float* partial_b;          // [ksplit][3][wo][ho_b]
+  double* wsum_part_b;       // [ksplit][ho_b]  (kind_b 0)
 };
 
 struct SmemPlan {
@@ -342,10 +351,17 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
 
   // Producer warps only for lane quarters that hold output rows (four per
   // quarter); the others have nothing to generate and stay out of the loop.
-  const int live_quarters = min(4, (job.ho - i0 + 31) / 32);
+  // quarters 0-1 hold rows of the first output and 2-3 of the second (pair),
+  // or all four the first output's rows i0 ..
+  auto quarter_live = [&](int q) -> bool {
+    if (job.pair) return q < 2 ? 32 * q < job.ho : 32 * (q - 2) < job.ho_b;
+    return i0 + 32 * q < job.ho;
+  };
+  int live_count = 0;
+  for (int q = 0; q < 4; ++q) live_count += quarter_live(q) ? 1 : 0;
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&a_full[s], 4 * live_quarters);
+      mbar_init(&a_full[s], 4 * live_count);
       mbar_init(&a_empty[s], 3 * job.nsplit);
     }
     for (int s = 0; s < kMaxSlots; ++s) {
@@ -385,18 +401,26 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   const int kchunks = job.kpad / kKS;
   const long long total = (long long)nrows * job.g * kchunks;
   const bool want_wsum = KIND == 0 && blockIdx.y == 0;
+  const bool want_wsum_b = job.pair && job.kind_b == 0 && blockIdx.y == 0;
 
   if (warp < kProducerWarps) {
     // ---- weight producers: rows 32q + lane, K sub-range [8h, 8h + 8) of each stage
     const int q = warp & 3, h = warp >> 2;
-    const int row = 32 * q + lane, gi = i0 + row;
-    const bool live = q < live_quarters;
+    const int row = 32 * q + lane;
+    const bool live = quarter_live(q);
+    // second output of a pair in quarters 2-3 (its own rows, kind, roughness)
+    const bool second = job.pair && q >= 2;
+    const int gi = second ? row - 64 : i0 + row;
+    const int ho_here = second ? job.ho_b : job.ho;
+    const float* orows = second ? job.out_rows_b : job.out_rows;
+    const bool ggx = second ? job.kind_b == 0 : KIND == 0;
+    const bool want = second ? want_wsum_b : want_wsum;
     float cp = 0.0f, sp_ = 0.0f;
-    if (gi < job.ho) {
-      cp = job.out_rows[2 * gi];
-      sp_ = job.out_rows[2 * gi + 1];
+    if (gi < ho_here) {
+      cp = orows[2 * gi];
+      sp_ = orows[2 * gi + 1];
     }
-    const float a2 = job.a2;
+    const float a2 = second ? job.a2_b : job.a2;
     const float alpha = 0.5f * (1.0f + a2), beta = 0.5f * (a2 - 1.0f), ka = a2 / kPiF;
     const float2 alpha2 = make_float2(alpha, alpha), beta2 = make_float2(beta, beta);
     const float2 minus1 = make_float2(-1.0f, -1.0f);
@@ -409,7 +433,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
       const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
       const float om = job.src_rows[3 * j + 2];
       const float ccq = cp * cq, ssq = sp_ * sq;
-      const float k1 = KIND == 0 ? ka * om : om;
+      const float k1 = ggx ? ka * om : om;
       const float2 ccq2 = make_float2(ccq, ccq), ssq2 = make_float2(ssq, ssq);
       const float2 k12 = make_float2(k1, k1);
       for (int ph = 0; ph < job.g && ok; ++ph) {
@@ -428,7 +452,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
               const float4 cd = *reinterpret_cast<const float4*>(cdrow + kb + 4 * e);
               const float2 c01 = __ffma2_rn(ccq2, make_float2(cd.x, cd.y), ssq2);
               const float2 c23 = __ffma2_rn(ccq2, make_float2(cd.z, cd.w), ssq2);
-              if (KIND == 0) {
+              if (ggx) {
                 const float2 d01 = __ffma2_rn(c01, beta2, alpha2);
                 const float2 d23 = __ffma2_rn(c23, beta2, alpha2);
                 const float2 q01 = __fmul2_rn(d01, d01), q23 = __fmul2_rn(d23, d23);
@@ -464,7 +488,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
               hw[e] = *reinterpret_cast<const uint32_t*>(&h2);
               lw[e] = *reinterpret_cast<const uint32_t*>(&l2);
             }
-            if (want_wsum)
+            if (want)
               rowsum2 = __fadd2_rn(__fadd2_rn(rowsum2, w[0]), __fadd2_rn(__fadd2_rn(w[1], w[2]), w[3]));
           }
           // Software pipeline: the previous stage's TMEM stores landed while
@@ -593,10 +617,13 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     if (tid == 0) atomicExch(job.error, 1);
   } else {
     const int q = warp & 3;
-    if (warp < kProducerWarps && i0 + 32 * q < job.ho) {
+    if (warp < kProducerWarps && quarter_live(q)) {
       // accumulators -> partial sums (lane = output row, column = (channel, n));
       // the four warps of a lane quarter take every fourth 16-column chunk
-      const int gi = i0 + 32 * q + lane;
+      const bool second = job.pair && q >= 2;
+      const int gi = second ? 32 * (q - 2) + lane : i0 + 32 * q + lane;
+      const int ho_here = second ? job.ho_b : job.ho;
+      float* part = second ? job.partial_b : job.partial;
       for (int c0 = 16 * (warp >> 2); c0 < 3 * job.nb; c0 += 16 * (kProducerWarps / 4)) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
@@ -604,16 +631,23 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
         for (int u = 0; u < 16; ++u) {
           const int col = c0 + u, ch = col / job.nb, n = col - ch * job.nb;
           const int x = x0 + job.m * (n0 + n);
-          if (gi < job.ho && n0 + n < job.nres && x < job.wo)
-            job.partial[(((size_t)split * 3 + ch) * job.wo + x) * job.ho + gi] =
+          if (gi < ho_here && n0 + n < job.nres && x < job.wo)
+            part[(((size_t)split * 3 + ch) * job.wo + x) * ho_here + gi] =
                 total > 0 ? v[u] : 0.0f;
         }
       }
     }
-    if (want_wsum && tid < kM && i0 + tid < job.ho) {
-      double ws = 0.0;
-      for (int hh = 0; hh < kProducerWarps / 4; ++hh) ws += wsum_sh[hh][tid];
-      job.wsum_part[(size_t)split * job.ho + i0 + tid] = ws;
+    if (tid < kM) {
+      const bool second = job.pair && tid >= 64;
+      const int gi = second ? tid - 64 : i0 + tid;
+      if (second ? (want_wsum_b && gi < job.ho_b) : (want_wsum && gi < job.ho)) {
+        double ws = 0.0;
+        for (int hh = 0; hh < kProducerWarps / 4; ++hh) ws += wsum_sh[hh][tid];
+        if (second)
+          job.wsum_part_b[(size_t)split * job.ho_b + gi] = ws;
+        else
+          job.wsum_part[(size_t)split * job.ho + gi] = ws;
+      }
     }
   }
   tc_fence_before();
@@ -989,6 +1023,8 @@ struct JobPlan {
   int level = -1;  // index into TcPlan::levels; -1 = roughness 0 (plain path)
   bool narrow = false;  // summed on the CUDA cores (narrow_kernel)
   int src_level = 0;    // chain level of a narrow job's source
+  int pair_with = -1;   // a second job run in this job's lanes 64-127
+  bool paired = false;  // this job runs inside another's launch (finish only)
   size_t cosd_off = 0, rows_off = 0, orows_off = 0, partial_off = 0,
          wsum_off = 0;
 };
@@ -1141,6 +1177,27 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
                        irr_w, irr_h, lv);
     int st = add_job(P, w, h, irr_w, irr_h, 1.0f, 1, lv, off);
     if (st) return st;
+  }
+  // Pair tensor jobs of at most 64 rows that share every radiance operand
+  // (same source level and phase decomposition, same columns): one launch
+  // runs both, the second in TMEM lanes 64-127.
+  for (size_t a = 0; a < P.jobs.size(); ++a) {
+    JobPlan& A = P.jobs[a];
+    if (A.level < 0 || A.narrow || A.paired || A.pair_with >= 0 || A.J.ho > 64) continue;
+    for (size_t b = a + 1; b < P.jobs.size(); ++b) {
+      JobPlan& B = P.jobs[b];
+      if (B.level != A.level || B.narrow || B.paired || B.pair_with >= 0 || B.J.ho > 64)
+        continue;
+      const Job &x = A.J, &y = B.J;
+      if (x.ws != y.ws || x.hs != y.hs || x.wo != y.wo || x.g != y.g || x.m != y.m ||
+          x.krow != y.krow || x.kpad != y.kpad || x.nres != y.nres || x.nb != y.nb ||
+          x.nblk != y.nblk || x.rlen != y.rlen || x.nslots != y.nslots ||
+          x.nsplit != y.nsplit || x.ksplit != y.ksplit)
+        continue;
+      A.pair_with = (int)b;
+      B.paired = true;
+      break;
+    }
   }
   P.total = off;
   return ALTHEA_IBL_OK;
@@ -1305,6 +1362,23 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     J.wsum_part = reinterpret_cast<double*>(base + jp.wsum_off);
     J.error = reinterpret_cast<int*>(base);
     J.out_half = out_half;
+    if (jp.paired) {  // contracted inside its partner's launch: only the finish
+      finish_kernel<<<dim3((J.ho + 31) / 32, J.wo), 256, 0, s>>>(J, out, pitch);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return cuda_status(e, "tc finish launch");
+      continue;
+    }
+    J.pair = 0;
+    if (jp.pair_with >= 0) {
+      const JobPlan& bp = P.jobs[jp.pair_with];
+      J.pair = 1;
+      J.ho_b = bp.J.ho;
+      J.kind_b = bp.J.kind;
+      J.a2_b = bp.J.a2;
+      J.out_rows_b = reinterpret_cast<const float*>(base + bp.orows_off);
+      J.partial_b = reinterpret_cast<float*>(base + bp.partial_off);
+      J.wsum_part_b = reinterpret_cast<double*>(base + bp.wsum_off);
+    }
     // At least 120 KB so no two CTAs share an SM (each allocates all of TMEM).
     int smem = (int)smem_plan(J).total;
     if (smem < 120 * 1024) smem = 120 * 1024;

@@ -433,8 +433,23 @@ def tc_launches(levels, irr_level):
     roughness-0 mip, the LUT."""
     from althea_gb300 import ibl
     jobs = tc_jobs(levels, irr_level)
-    split_levels = {lv for w, h, _, _, lv, _ in jobs if w * h > TC_NARROW_MAX}
-    return ((ibl.chain_levels(ENV_W, ENV_H) - 1) + len(split_levels) + 1 + 2 * len(jobs) +
+    tensor = [j for j in jobs if j[0] * j[1] > TC_NARROW_MAX]
+    split_levels = {lv for _, _, _, _, lv, _ in tensor}
+    # tensor jobs of <= 64 rows with the same source level, phase count and
+    # width run in one launch (the second in lanes 64-127)
+    pairs, used = 0, set()
+    for a in range(len(tensor)):
+        if a in used or tensor[a][1] > 64:
+            continue
+        for b in range(a + 1, len(tensor)):
+            if b in used or tensor[b][1] > 64:
+                continue
+            if (tensor[a][0], tensor[a][2], tensor[a][4], tensor[a][5]) == \
+                    (tensor[b][0], tensor[b][2], tensor[b][4], tensor[b][5]):
+                used |= {a, b}
+                pairs += 1
+                break
+    return ((ibl.chain_levels(ENV_W, ENV_H) - 1) + len(split_levels) + 1 + 2 * len(jobs) - pairs +
             levels.count(-1) + 1)
 
 
