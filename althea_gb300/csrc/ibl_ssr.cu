@@ -55,11 +55,13 @@ __device__ __forceinline__ float2 halves(uint32_t v) {
 __device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
 
 // Channel pairs, each product and sum rounded on its own (__fmul_rn/__fadd_rn
-// are never fused into a multiply-add).  The packed FP32x2 instructions are not
-// used: written as FMUL2/FADD2, or as FFMA2 with a -0 addend / unit multiplier
-// (even with those constants opaque to the compiler), they gave results one
-// unit in the last place away from the separately rounded scalar ones on rare
-// texels.
+// are never fused into a multiply-add).  Packed FP32x2 products feeding packed
+// FP32x2 sums (written as mul/add.rn.f32x2, or as FFMA2 with a -0 addend /
+// unit multiplier) gave results one unit in the last place away on rare
+// texels -- a product and the sum after it evidently became one fused
+// operation.  Packed products alone, or packed sums alone, were exact but no
+// faster (the kernel is bound by loads and conversions), so the scalar forms
+// stay.
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) {
   return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
 }
