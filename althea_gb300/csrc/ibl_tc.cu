@@ -944,13 +944,28 @@ __global__ void rows_kernel(const RowsArgs a) {
     }
   }
   __syncthreads();
+  // Phase rows are krow (a multiple of 8) long: each thread writes four
+  // consecutive elements of one phase row at a time (8-byte stores).
   for (int q = 0; q < a.n; ++q) {
-    const int g = a.g[q], krow = ws / g;
+    const int g = a.g[q], krow = ws / g, quads = krow >> 2;
     __nv_bfloat16* __restrict__ out = a.out[q];
-    for (int e = threadIdx.x; e < 6 * ws; e += blockDim.x) {
-      const int p = e / ws, t = e - p * ws;
-      const int ph = t / krow, u = t - ph * krow;
-      out[((size_t)p * hs + j) * ws + t] = row_sm[p * ws + g * u + ph];
+    for (int p = 0; p < 6; ++p) {
+      const __nv_bfloat16* rp = row_sm + p * ws;
+      __nv_bfloat16* op = out + ((size_t)p * hs + j) * ws;
+      for (int ph = 0; ph < g; ++ph) {
+        for (int c = threadIdx.x; c < quads; c += blockDim.x) {
+          const int u = 4 * c;
+          __nv_bfloat162 v01, v23;
+          v01.x = rp[g * u + ph];
+          v01.y = rp[g * (u + 1) + ph];
+          v23.x = rp[g * (u + 2) + ph];
+          v23.y = rp[g * (u + 3) + ph];
+          uint2 w;
+          w.x = *reinterpret_cast<const uint32_t*>(&v01);
+          w.y = *reinterpret_cast<const uint32_t*>(&v23);
+          *reinterpret_cast<uint2*>(op + ph * krow + u) = w;
+        }
+      }
     }
   }
 }
@@ -960,12 +975,12 @@ __global__ void rows_kernel(const RowsArgs a) {
 // splits k = w mod 8 with the lanes on consecutive rows (the partial layout),
 // then warp 0 combines the eight in order.  FP64 is used only for the weight
 // sums and the final normalisation.
-__global__ void __launch_bounds__(256) finish_kernel(const Job job, void* __restrict__ out,
-                                                     long long pitch) {
+__device__ __forceinline__ void finish_block(const Job& job, void* __restrict__ out,
+                                             long long pitch, int bx, int by) {
   __shared__ float red[8][3][32];
   __shared__ double redw[8][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * 32 + lane, x = blockIdx.y;
+  const int i = bx * 32 + lane, x = by;
   float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
   double sw = 0.0;
   if (i < job.ho) {
@@ -1026,6 +1041,31 @@ __global__ void __launch_bounds__(256) finish_kernel(const Job job, void* __rest
       reinterpret_cast<float4*>(out)[(long long)i * pitch + x] = make_float4(r, g, b, 1.0f);
     }
   }
+}
+
+__global__ void __launch_bounds__(256) finish_kernel(const Job job, void* __restrict__ out,
+                                                     long long pitch) {
+  finish_block(job, out, pitch, blockIdx.x, blockIdx.y);
+}
+
+// Every tensor job's finish in one launch: block b belongs to the job k with
+// begin[k] <= b < begin[k + 1] and covers (32 rows, one column) of it.
+constexpr int kMaxFinishJobs = ALTHEA_IBL_MAX_MIPS + 1;
+struct FinishArgs {
+  Job job[kMaxFinishJobs];
+  void* out[kMaxFinishJobs];
+  long long pitch[kMaxFinishJobs];
+  int begin[kMaxFinishJobs + 1];
+  int n;
+};
+
+__global__ void __launch_bounds__(256) finish_all_kernel(const __grid_constant__ FinishArgs a) {
+  const int b = blockIdx.x;
+  int k = 0;
+  while (k + 1 < a.n && b >= a.begin[k + 1]) ++k;
+  const Job& J = a.job[k];
+  const int local = b - a.begin[k], nbx = (J.ho + 31) / 32;
+  finish_block(J, a.out[k], a.pitch[k], local % nbx, local / nbx);
 }
 
 }  // namespace tc
@@ -1372,6 +1412,10 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     }
     if (nt > 0) tables_kernel<<<dim3((nmax + 31) / 32, nt), 32, 0, s>>>(ta);
   }
+  static_assert(sizeof(FinishArgs) <= 32000, "finish arguments fit the kernel parameter space");
+  FinishArgs fa;
+  memset(&fa, 0, sizeof(fa));
+  int finish_blocks = 0;
   for (size_t k = 0; k < P.jobs.size(); ++k) {
     JobPlan& jp = P.jobs[k];
     void* out = nullptr;
@@ -1428,12 +1472,15 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     J.wsum_part = reinterpret_cast<double*>(base + jp.wsum_off);
     J.error = reinterpret_cast<int*>(base);
     J.out_half = out_half;
-    if (jp.paired) {  // contracted inside its partner's launch: only the finish
-      finish_kernel<<<dim3((J.ho + 31) / 32, J.wo), 256, 0, s>>>(J, out, pitch);
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return cuda_status(e, "tc finish launch");
-      continue;
-    }
+    // every tensor job's finish runs in one launch after the contractions
+    if (fa.n >= kMaxFinishJobs) return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "tc: too many jobs");
+    fa.job[fa.n] = J;
+    fa.out[fa.n] = out;
+    fa.pitch[fa.n] = pitch;
+    fa.begin[fa.n] = finish_blocks;
+    finish_blocks += ((J.ho + 31) / 32) * J.wo;
+    ++fa.n;
+    if (jp.paired) continue;  // contracted inside its partner's launch
     J.pair = 0;
     if (jp.pair_with >= 0) {
       const JobPlan& bp = P.jobs[jp.pair_with];
@@ -1462,7 +1509,10 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "tc contraction launch");
-    finish_kernel<<<dim3((J.ho + 31) / 32, J.wo), 256, 0, s>>>(J, out, pitch);
+  }
+  if (fa.n > 0) {
+    fa.begin[fa.n] = finish_blocks;
+    finish_all_kernel<<<finish_blocks, 256, 0, s>>>(fa);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "tc finish launch");
   }

@@ -428,9 +428,10 @@ TC_NARROW_MAX = 128
 
 def tc_launches(levels, irr_level):
     """Kernels of one precision probe step: chain blits, one split pass per
-    source level of a tensor-core job, one tables pass, two kernels per job
-    (contraction + finish, or the narrow sum + its finish), one delta pass per
-    roughness-0 mip, the LUT."""
+    source level of a tensor-core job, one tables pass, one contraction per
+    tensor job (pairs share one) and one finish launch for all of them, the
+    narrow sum + its finish per CUDA-core job, one delta pass per roughness-0
+    mip, the LUT."""
     from althea_gb300 import ibl
     jobs = tc_jobs(levels, irr_level)
     tensor = [j for j in jobs if j[0] * j[1] > TC_NARROW_MAX]
@@ -449,8 +450,9 @@ def tc_launches(levels, irr_level):
                 used |= {a, b}
                 pairs += 1
                 break
-    return ((ibl.chain_levels(ENV_W, ENV_H) - 1) + len(split_levels) + 1 + 2 * len(jobs) - pairs +
-            levels.count(-1) + 1)
+    narrow = len(jobs) - len(tensor)
+    return ((ibl.chain_levels(ENV_W, ENV_H) - 1) + len(split_levels) + 1 +
+            (len(tensor) - pairs) + (1 if tensor else 0) + 2 * narrow + levels.count(-1) + 1)
 
 
 def error_table(env, outs_by_path, irr_by_path, per_mip=128, seed=7):
