@@ -350,6 +350,8 @@ __global__ void __launch_bounds__(256) brdf_lut_row_kernel(float2* __restrict__ 
   if (i >= n) return;
   float nov = ((float)i + 0.5f) / (float)n;
   float vx = sqrtf(1.0f - nov * nov), vz = nov;
+  // the view term of Smith's G is the same for every sample of this texel
+  const float g1v = nov / (nov * (1.0f - k) + k);
   float sum_a = 0.0f, sum_b = 0.0f;
 #pragma unroll 4
   for (int s = 0; s < samples; ++s) {
@@ -362,7 +364,6 @@ __global__ void __launch_bounds__(256) brdf_lut_row_kernel(float2* __restrict__ 
     float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
     if (nol > 0.0f) {
       float g1l = nol / (nol * (1.0f - k) + k);
-      float g1v = nov / (nov * (1.0f - k) + k);
       float g_vis = g1l * g1v * voh / (noh * nov);
       float tt = 1.0f - voh;
       float t2 = tt * tt;
