@@ -82,3 +82,30 @@ def test_wait_selftest_rejects_bad_limits_without_gpu():
     L = ibl.load()
     assert L.althea_ibl_tc_wait_selftest(0, None, None) == ibl.ERR_INVALID_ARGUMENT
     assert L.althea_ibl_tc_wait_selftest(2 * 10**9, None, None) == ibl.ERR_INVALID_ARGUMENT
+
+
+def test_precision_planner_levels_without_gpu():
+    """The source level per output (host logic only): W/4-wide sources for
+    roughness <= 0.40, W/2 for rougher mips and the irradiance, never coarser
+    than the output, -1 for roughness 0."""
+    mips = [(2048 >> m, 1024 >> m) for m in range(9)]
+    rough = [m / 8 for m in range(9)]
+    levels, irr = ibl.tc_plan(4096, 2048, mips, rough, 128)
+    assert levels == [-1, 2, 2, 2, 1, 1, 1, 1, 1] and irr == 1
+    spec = ibl.spec_for(2048, 1024)
+    levels, irr = ibl.tc_plan(2048, 1024, spec.mip_sizes, spec.roughness, 32)
+    assert levels == [-1, 1, 1, 0, 0, 0, 0, 0] and irr == 0
+    for w in (256, 512, 1024):
+        spec = ibl.spec_for(w, w // 2)
+        levels, irr = ibl.tc_plan(w, w // 2, spec.mip_sizes, spec.roughness, 32)
+        assert levels[0] == -1 and all(l == 0 for l in levels[1:]) and irr == 0
+
+
+def test_precision_workspace_sizes_without_gpu():
+    L = ibl.load()
+    arr = (ibl.MipTarget * 2)(ibl.MipTarget(0, 16 * 256, 256, 128, 0.3),
+                              ibl.MipTarget(0, 16 * 8, 8, 4, 1.0))
+    assert L.althea_ibl_tc_workspace_size(1024, 512, arr, 2, None, 32, 16, -1) > 0
+    # an output width that does not divide the source level's width: unsupported
+    bad = (ibl.MipTarget * 1)(ibl.MipTarget(0, 16 * 96, 96, 48, 0.3))
+    assert L.althea_ibl_tc_workspace_size(4096, 2048, bad, 1, None, 0, 0, -1) == 0
