@@ -312,11 +312,6 @@ struct Job {
   // one quarter spreads over the four SM sub-partitions; each quarter's
   // partial sums are a split of their own (nparts = ksplit * kinter).
   int kinter;                // 1 or 4
-  // Accumulator sets: stage g accumulates into set g mod nsets (columns
-  // set * 3 nb ..); the drain adds the sets in a fixed order.  Kept at 1: two
-  // or four sets for the 64- and 32-column tiles measured slower (4.90 ms
-  // against 4.79 ms for the bake), so the MMA chain is not what bounds them.
-  int nsets;
   int nparts;                // partial sums the finish adds: ksplit * kinter
   int pair;                  // 1: lanes 64-127 hold the second output
   int ho_b, kind_b;
@@ -597,9 +592,8 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
             }
             tc_fence_after();
             const uint32_t a_hi = tmem + (uint32_t)kACol + st * kKS;
-            const uint32_t set = gidx % (uint32_t)job.nsets;
-            mma_stage_ts(d + set * 3u * (uint32_t)job.nb, a_hi, dbh, dbh + r8, dbh + 2,
-                         dbh + 2 + r8, idesc, gidx >= (uint32_t)job.nsets, &a_empty[st]);
+            mma_stage_ts(d, a_hi, dbh, dbh + r8, dbh + 2, dbh + 2 + r8, idesc, gidx != 0,
+                         &a_empty[st]);
             if (kc == kchunks - 1) mma_commit(&slot_empty[slot]);
           }
         }
@@ -669,17 +663,9 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
       const int ho_here = second ? job.ho_b : job.ho;
       float* part = second ? job.partial_b : job.partial;
       const int slot_split = kint ? split * job.kinter + q : split;
-      // sets that hold sums (a CTA with fewer stages than sets leaves some unset)
-      const int nvalid = (int)(total < (long long)job.nsets ? total : (long long)job.nsets);
       for (int c0 = 16 * (warp >> 2); c0 < 3 * job.nb; c0 += 16 * (kProducerWarps / 4)) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
-        for (int s2 = 1; s2 < nvalid; ++s2) {
-          float w2[16];
-          tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(s2 * 3 * job.nb + c0), w2);
-#pragma unroll
-          for (int u = 0; u < 16; ++u) v[u] += w2[u];
-        }
 #pragma unroll
         for (int u = 0; u < 16; ++u) {
           const int col = c0 + u, ch = col / job.nb, n = col - ch * job.nb;
@@ -1043,11 +1029,6 @@ __device__ __forceinline__ void finish_block(const Job& job, void* __restrict__ 
   }
 }
 
-__global__ void __launch_bounds__(256) finish_kernel(const Job job, void* __restrict__ out,
-                                                     long long pitch) {
-  finish_block(job, out, pitch, blockIdx.x, blockIdx.y);
-}
-
 // Every tensor job's finish in one launch: block b belongs to the job k with
 // begin[k] <= b < begin[k + 1] and covers (32 rows, one column) of it.
 constexpr int kMaxFinishJobs = ALTHEA_IBL_MAX_MIPS + 1;
@@ -1231,7 +1212,6 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   J.ksplit = ks;
   J.kinter = 1;
   J.nparts = ks;
-  J.nsets = 1;
   // room for a K interleave (the plan decides after pairing)
   const int parts = oh <= 32 ? 4 * ks : ks;
   jp.level = li;
