@@ -292,6 +292,8 @@ __global__ void __launch_bounds__(256) brdf_lut_kernel(float2* __restrict__ out,
   float alpha = rough * rough;
   float a2 = alpha * alpha;
   float k = alpha / 2.0f;
+  // G1(V) / NoV once per texel, 1 / NoH once per sample
+  const float gv = 1.0f / (nov * (1.0f - k) + k);
   float sum_a = 0.0f, sum_b = 0.0f;
 #pragma unroll 1
   for (int s = 0; s < samples; ++s) {
@@ -306,10 +308,10 @@ __global__ void __launch_bounds__(256) brdf_lut_kernel(float2* __restrict__ out,
     float nol = lz > 0.0f ? (lz < 1.0f ? lz : 1.0f) : 0.0f;
     float noh = hz > 0.0f ? (hz < 1.0f ? hz : 1.0f) : 0.0f;
     float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
+    const float rnoh = 1.0f / noh;
     if (nol > 0.0f) {
       float g1l = nol / (nol * (1.0f - k) + k);
-      float g1v = nov / (nov * (1.0f - k) + k);
-      float g_vis = g1l * g1v * voh / (noh * nov);
+      float g_vis = ((g1l * gv) * voh) * rnoh;
       float tt = 1.0f - voh;
       float t2 = tt * tt;
       float fc = t2 * t2 * tt;
@@ -324,13 +326,13 @@ __global__ void __launch_bounds__(256) brdf_lut_kernel(float2* __restrict__ out,
 // roughness only, not on N.V) tabulated once in shared memory: every texel
 // evaluates the identical IEEE operations in the identical order, so the
 // result is bit-identical to brdf_lut_kernel.  Block per (row, 256 columns);
-// dynamic shared memory: samples * 8 bytes.
+// dynamic shared memory: samples * 16 bytes.
 constexpr int kLutTableMax = 8192;
 
 __global__ void __launch_bounds__(256) brdf_lut_row_kernel(float2* __restrict__ out, int n,
                                                            long long pitch, int samples,
                                                            int orientation) {
-  extern __shared__ float2 hsamp[];  // (hx, hz) per sample
+  extern __shared__ float4 hsamp[];  // (hx, hz, 1 / NoH, -) per sample
   const int j = blockIdx.y;
   float tj = ((float)j + 0.5f) / (float)n;
   float rough = orientation == ALTHEA_IBL_LUT_ASSET ? 1.0f - tj : tj;
@@ -343,28 +345,28 @@ __global__ void __launch_bounds__(256) brdf_lut_row_kernel(float2* __restrict__ 
     float phi = 2.0f * kPi * xi_x;
     float cos_t = sqrtf((1.0f - xi_y) / (1.0f + (a2 - 1.0f) * xi_y));
     float sin_t = sqrtf(1.0f - cos_t * cos_t);
-    hsamp[s] = make_float2(sin_t * agb_cos(phi), cos_t);
+    const float hz = cos_t, noh = hz > 0.0f ? (hz < 1.0f ? hz : 1.0f) : 0.0f;
+    hsamp[s] = make_float4(sin_t * agb_cos(phi), cos_t, 1.0f / noh, 0.0f);
   }
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float nov = ((float)i + 0.5f) / (float)n;
   float vx = sqrtf(1.0f - nov * nov), vz = nov;
-  // the view term of Smith's G is the same for every sample of this texel
-  const float g1v = nov / (nov * (1.0f - k) + k);
+  // G1(V) / NoV once per texel; 1 / NoH comes with the sample
+  const float gv = 1.0f / (nov * (1.0f - k) + k);
   float sum_a = 0.0f, sum_b = 0.0f;
 #pragma unroll 4
   for (int s = 0; s < samples; ++s) {
-    const float2 hv = hsamp[s];
+    const float4 hv = hsamp[s];
     float hx = hv.x, hz = hv.y;
     float vdh = vx * hx + vz * hz;
     float lz = 2.0f * vdh * hz - vz;
     float nol = lz > 0.0f ? (lz < 1.0f ? lz : 1.0f) : 0.0f;
-    float noh = hz > 0.0f ? (hz < 1.0f ? hz : 1.0f) : 0.0f;
     float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
     if (nol > 0.0f) {
       float g1l = nol / (nol * (1.0f - k) + k);
-      float g_vis = g1l * g1v * voh / (noh * nov);
+      float g_vis = ((g1l * gv) * voh) * hv.z;
       float tt = 1.0f - voh;
       float t2 = tt * tt;
       float fc = t2 * t2 * tt;
@@ -379,7 +381,7 @@ int launch_brdf_lut(float* out, int n, size_t pitch_bytes, int samples, int orie
                     cudaStream_t st) {
   const long long pitch = (long long)(pitch_bytes / sizeof(float2));
   if (samples <= kLutTableMax) {
-    const int sm = samples * (int)sizeof(float2);
+    const int sm = samples * (int)sizeof(float4);
     if (sm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(brdf_lut_row_kernel,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, sm);

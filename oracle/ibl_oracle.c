@@ -421,6 +421,9 @@ static void lut_texel_f32(int i, int j, int n, int samples, int orientation,
   float alpha = rough * rough;
   float a2 = alpha * alpha;
   float k = alpha / 2.0f;
+  /* G_vis = G1(L) G1(V) VoH / (NoH NoV) with G1(V) / NoV = 1 / (NoV (1 - k) + k)
+   * taken once per texel and 1 / NoH once per sample */
+  float gv = 1.0f / (nov * (1.0f - k) + k);
   float sum_a = 0.0f, sum_b = 0.0f;
   for (int s = 0; s < samples; ++s) {
     float xi_x, xi_y;
@@ -434,10 +437,10 @@ static void lut_texel_f32(int i, int j, int n, int samples, int orientation,
     float nol = lz > 0.0f ? (lz < 1.0f ? lz : 1.0f) : 0.0f;
     float noh = hz > 0.0f ? (hz < 1.0f ? hz : 1.0f) : 0.0f;
     float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
+    float rnoh = 1.0f / noh;
     if (nol > 0.0f) {
       float g1l = nol / (nol * (1.0f - k) + k);
-      float g1v = nov / (nov * (1.0f - k) + k);
-      float g_vis = g1l * g1v * voh / (noh * nov);
+      float g_vis = ((g1l * gv) * voh) * rnoh;
       float t = 1.0f - voh;
       float t2 = t * t;
       float fc = t2 * t2 * t;
