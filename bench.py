@@ -64,8 +64,8 @@ GENERATOR = 1
 
 def workload():
     return WORKLOAD.format(gen="Hammersley" if GENERATOR == 1 else "reference-hash")
-# DRAM bytes (read + write) of one prefilter_kernel launch of the plain 4096x2048
-# workload, from the ncu capture summarised in profiles/ibl_bake_c2_4096x2048_ncu.md.
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one prefilter_kernel
+# launch of the plain 4096x2048 workload, from an ncu capture of this bench.
 NCU_PREFILTER_TRAFFIC = 156.4e6
 
 
@@ -818,9 +818,9 @@ def run_serve(args):
 SSR_METRIC = "reflection-buffer glossy convolutions/s (frames/s), 1 GB300"
 SSR_W, SSR_H, SSR_MIPS = 3840, 2160, 5
 SSR_RING = 4  # frames cycled through: 4 x 88 MB > the 129 MB L2
-# DRAM bytes (read + write) of one level-1 launch of the 3840x2160 workload, from
-# the ncu capture summarised in profiles/ssr_convolve_3840x2160_ncu.md (writes
-# still in L2 when the kernel ends are not counted there).
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one level-1 launch
+# of the 3840x2160 workload, from an ncu capture of this bench (writes still in
+# L2 when the kernel ends are not counted there).
 NCU_SSR_LEVEL1_TRAFFIC = 69.73e6
 SSR_WORKLOAD = ("3840x2160 RGBA16F reflection buffer, 5 mips: levels 1-4 = 7-tap Gaussian of the "
                 "level before (vertical on odd levels), bit-identical to SSRGlossyConvolve.comp")
