@@ -1,7 +1,8 @@
 /*
  * ibl_oracle.h -- CPU oracle for the IBL precompute.  TEST INFRASTRUCTURE
  * ONLY: the tests, the smoke check and the CPU-baseline leg of the bench
- * call it as the checker.  Nothing in the product library links or calls it.
+ * call it to check the product's results.  Nothing in the product library
+ * links or calls it.
  *
  * O1 (restatement of the reference estimator, parity oracle of the plain
  *     path): env mip chain (vkCmdBlitImage LINEAR), Vulkan trilinear REPEAT

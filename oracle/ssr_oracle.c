@@ -1,7 +1,8 @@
 /*
  * ssr_oracle.c -- CPU oracle for the reflection-buffer glossy convolution.
  * TEST INFRASTRUCTURE ONLY: the tests and the CPU-baseline leg of the bench
- * call it as the checker; nothing in the product library links or calls it.
+ * call it to check the product's results; nothing in the product library
+ * links or calls it.
  *
  * Restates Shaders/SSRGlossyConvolve.comp:25-53 as dispatched by
  * ReflectionBuffer::convolveReflectionBuffer (Src/ReflectionBuffer.cpp:
