@@ -90,6 +90,37 @@ def test_plan_meets_1e3_against_level0_quadrature():
     assert _rel(got, ref).max() <= 1e-3, _rel(got, ref).max()
 
 
+@pytest.mark.parametrize("sun_max", [1e4, 1e6])
+def test_small_probe_every_texel_against_fp64(sun_max):
+    """The 512x256 probe (5 mips of roughness m/4 from 256x128, 32x16
+    irradiance) through the default plan, every output texel against the FP64
+    quadrature over level 0 (the CPU oracle sums all 131072 source texels)."""
+    w, h = 512, 256
+    env = synth.make_env(w, h, seed=0, sun_max=sun_max)
+    chain = oracle.build_chain(env)
+    sizes = [(256 >> m, 128 >> m) for m in range(5)]
+    rough = [m / 4 for m in range(5)]
+    outs = [torch.full((mh, mw, 4), float("nan"), device="cuda") for mw, mh in sizes]
+    irr = torch.full((16, 32, 4), float("nan"), device="cuda")
+    ibl.bake_tc(torch.from_numpy(chain).cuda(), w, h, outs, rough, irradiance=irr)
+    torch.cuda.synchronize()
+    lvl0 = oracle.chain_level(chain, w, h, 0)
+    for (mw, mh), r, o in zip(sizes[1:], rough[1:], outs[1:]):
+        ys, xs = np.mgrid[0:mh, 0:mw]
+        xy = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
+        ref = oracle.quad_prefilter(lvl0, mw, mh, r, xy)[:, :3]
+        got = o.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
+        assert np.isfinite(got).all()
+        assert _rel(got, ref).max() <= 1e-3, (mw, r, _rel(got, ref).max())
+    ref0 = oracle.prefilter(chain, w, h, 256, 128, 0.0, 1024, oracle.GEN_HAMMERSLEY)
+    assert _rel(outs[0].cpu().numpy()[..., :3], ref0[..., :3]).max() <= 1e-4
+    ys, xs = np.mgrid[0:16, 0:32]
+    xy = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
+    ref = oracle.quad_irradiance(lvl0, 32, 16, xy)[:, :3]
+    got = irr.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
+    assert np.isfinite(got).all() and _rel(got, ref).max() <= 1e-3, _rel(got, ref).max()
+
+
 def test_half_outputs_are_the_float_outputs_rounded():
     w, h = 256, 128
     env = synth.make_env(w, h, seed=12, sun_max=1e6)
