@@ -109,3 +109,74 @@ def test_precision_workspace_sizes_without_gpu():
     # an output width that does not divide the source level's width: unsupported
     bad = (ibl.MipTarget * 1)(ibl.MipTarget(0, 16 * 96, 96, 48, 0.3))
     assert L.althea_ibl_tc_workspace_size(4096, 2048, bad, 1, None, 0, 0, -1) == 0
+
+
+# ctypes mirror -> C type of include/althea_ibl.h
+_LAYOUTS = [
+    (ibl.MipTarget, "althea_ibl_mip_target"), (ibl.Config, "althea_ibl_config"),
+    (ibl.Outputs, "althea_ibl_outputs"), (ibl.Probe, "althea_ibl_probe"),
+    (ibl.BatchParams, "althea_ibl_batch_params"), (ibl.BatchInfo, "althea_ibl_batch_info"),
+    (ibl.ServerConfig, "althea_ibl_server_config"), (ibl.Request, "althea_ibl_request"),
+    (ibl.Completion, "althea_ibl_completion"), (ibl.ServerStats, "althea_ibl_server_stats"),
+]
+# Python constant -> C enum constant or macro
+_CONSTANTS = {
+    "OK": "ALTHEA_IBL_OK", "ERR_INVALID_ARGUMENT": "ALTHEA_IBL_ERR_INVALID_ARGUMENT",
+    "ERR_CUDA": "ALTHEA_IBL_ERR_CUDA", "ERR_OUT_OF_MEMORY": "ALTHEA_IBL_ERR_OUT_OF_MEMORY",
+    "ERR_UNSUPPORTED": "ALTHEA_IBL_ERR_UNSUPPORTED", "ERR_BUDGET": "ALTHEA_IBL_ERR_BUDGET",
+    "ERR_NOT_READY": "ALTHEA_IBL_ERR_NOT_READY", "GEN_REF_HASH": "ALTHEA_IBL_GEN_REF_HASH",
+    "GEN_HAMMERSLEY": "ALTHEA_IBL_GEN_HAMMERSLEY", "LUT_ASSET": "ALTHEA_IBL_LUT_ASSET",
+    "LUT_CORRECTED": "ALTHEA_IBL_LUT_CORRECTED", "MAX_MIPS": "ALTHEA_IBL_MAX_MIPS",
+    "BATCH_AUTOTUNE": "ALTHEA_IBL_BATCH_AUTOTUNE", "BATCH_GRAPH": "ALTHEA_IBL_BATCH_GRAPH",
+    "BATCH_PRECISION": "ALTHEA_IBL_BATCH_PRECISION", "BATCH_HALF": "ALTHEA_IBL_BATCH_HALF",
+    "PATH_PLAIN": "ALTHEA_IBL_PATH_PLAIN", "PATH_PRECISION": "ALTHEA_IBL_PATH_PRECISION",
+    "FORMAT_RGBA32F": "ALTHEA_IBL_FORMAT_RGBA32F", "FORMAT_RGBA16F": "ALTHEA_IBL_FORMAT_RGBA16F",
+}
+
+
+def test_ctypes_mirror_matches_the_header(tmp_path):
+    """Every ctypes structure of the Python binding has the size and field
+    offsets the C compiler gives the header's struct, and every mirrored
+    constant has the header's value (gcc on a generated probe program)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "althea_ibl.h"',
+             "int main(void) {"]
+    for cls, ctype in _LAYOUTS:
+        lines.append(f'  printf("{ctype} size %zu\\n", sizeof({ctype}));')
+        for name, _ in cls._fields_:
+            lines.append(f'  printf("{ctype} {name} %zu\\n", offsetof({ctype}, {name}));')
+    for py, c in _CONSTANTS.items():
+        lines.append(f'  printf("const {py} %ld\\n", (long){c});')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-std=c11", "-Wall", "-Werror", "-I",
+                           os.path.join(ROOT, "include"), "-o", str(exe), str(src)])
+    got = {}
+    for line in subprocess.check_output([str(exe)], text=True).splitlines():
+        a, b, v = line.split()
+        got[(a, b)] = int(v)
+    for cls, ctype in _LAYOUTS:
+        assert got[(ctype, "size")] == ctypes.sizeof(cls), ctype
+        for name, _ in cls._fields_:
+            assert got[(ctype, name)] == getattr(cls, name).offset, (ctype, name)
+    for py, c in _CONSTANTS.items():
+        assert got[("const", py)] == getattr(ibl, py), (py, c)
+
+
+def test_header_compiles_as_cpp(tmp_path):
+    """The header is usable from the reference's C++ (extern "C", no C-only syntax)."""
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    src = tmp_path / "use.cpp"
+    src.write_text('#include "althea_ibl.h"\n'
+                   'int f() { althea_ibl_config c; althea_ibl_config_reference(&c, 64, 32);\n'
+                   '          return c.mip_count + althea_ibl_abi_version(); }\n')
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
+                           "-I", os.path.join(ROOT, "include"), str(src)])
