@@ -98,8 +98,11 @@ class BakeCache:
         h, w = env.shape[:2]
         baked = False
         if not self.complete(name):
-            c = cfg or ibl.reference_config(w, h)
+            # a copy: the caller's config is left as it was
+            c = (ibl.Config.from_buffer_copy(cfg) if cfg is not None
+                 else ibl.reference_config(w, h))
             c.mip_count = self.mip_count
+            c.lut_size = 0  # the cache holds no LUT file; the LUT is made below
             ctx = ibl.BakeContext(c)
             try:
                 ctx.upload_env(torch.from_numpy(env), stream)

@@ -227,6 +227,44 @@ def _pitch(t, ncomp) -> int:
     return t.stride(0) * t.element_size()
 
 
+# The C calls receive bare pointers and pitches, so they cannot see how large
+# a caller's tensor is.  These checks hold the tensors to the extents the
+# kernels read or write; they look only at tensor metadata (no device access).
+
+def _require_shape(t, name, shape) -> None:
+    torch = _torch()
+    if not isinstance(t, torch.Tensor):
+        raise IBLError(ERR_INVALID_ARGUMENT, f"{name} must be a tensor, not {type(t).__name__}")
+    if tuple(t.shape) != tuple(shape):
+        raise IBLError(ERR_INVALID_ARGUMENT,
+                       f"{name} has shape {tuple(t.shape)}; this call writes {tuple(shape)}")
+
+
+def _require_chain(chain, w: int, h: int) -> None:
+    """chain must hold every level of a w x h env: chain_texels(w, h) RGBA32F
+    texels, contiguous, on a CUDA device."""
+    torch = _torch()
+    if not isinstance(chain, torch.Tensor) or chain.dtype != torch.float32:
+        raise IBLError(ERR_INVALID_ARGUMENT, "chain must be a float32 tensor")
+    if not chain.is_contiguous():
+        raise IBLError(ERR_INVALID_ARGUMENT, "chain must be contiguous")
+    need = chain_texels(w, h)
+    if chain.numel() < 4 * need:
+        raise IBLError(ERR_INVALID_ARGUMENT,
+                       f"chain holds {chain.numel() // 4} texels; the chain of a {w}x{h} env "
+                       f"has {need}")
+    if not chain.is_cuda:
+        raise IBLError(ERR_INVALID_ARGUMENT, "chain must be a CUDA tensor")
+
+
+def _require_counts(outs, roughness, limit=MAX_MIPS) -> None:
+    if len(outs) != len(roughness):
+        raise IBLError(ERR_INVALID_ARGUMENT,
+                       f"{len(outs)} output mips but {len(roughness)} roughness values")
+    if len(outs) > limit:
+        raise IBLError(ERR_INVALID_ARGUMENT, f"{len(outs)} mips; at most {limit}")
+
+
 # ---- stateless kernels -------------------------------------------------------
 
 def chain_levels(w: int, h: int) -> int:
@@ -257,8 +295,7 @@ def build_env_chain_into(env, chain, stream=None) -> None:
     """Builds the chain of env (CUDA (H, W, 4)) into a preallocated chain tensor."""
     _require_cuda(env, "env", 4)
     h, w = env.shape[:2]
-    if chain.numel() < chain_texels(w, h) * 4 or not chain.is_cuda or not chain.is_contiguous():
-        raise IBLError(ERR_INVALID_ARGUMENT, "chain tensor too small or not contiguous CUDA")
+    _require_chain(chain, w, h)
     _check(load().althea_ibl_build_env_chain(env.contiguous().data_ptr(), w, h, chain.data_ptr(),
                                              _stream_ptr(stream)))
 
@@ -272,6 +309,8 @@ def chain_level(chain, w: int, h: int, level: int):
 def prefilter(chain, w: int, h: int, outs: List, roughness: List[float], samples: int,
               generator: int = GEN_REF_HASH, stream=None) -> None:
     """Writes each prefiltered mip into the given (h_m, w_m, 4) CUDA tensors."""
+    _require_counts(outs, roughness)
+    _require_chain(chain, w, h)
     n = len(outs)
     arr = (MipTarget * max(n, 1))()
     for k, (o, r) in enumerate(zip(outs, roughness)):
@@ -283,6 +322,7 @@ def prefilter(chain, w: int, h: int, outs: List, roughness: List[float], samples
 
 def irradiance(chain, w: int, h: int, out, workspace=None, stream=None) -> None:
     torch = _torch()
+    _require_chain(chain, w, h)
     _require_cuda(out, "irradiance", 4)
     oh, ow = out.shape[:2]
     L = load()
@@ -430,6 +470,22 @@ class BakeContext:
         return irr, mips, lut
 
     def bake(self, irr, mips, lut=None, stream=None):
+        """Bakes into caller tensors of exactly the context's sizes (as
+        allocate_outputs makes them): irradiance (ih, iw, 4), one (h_m, w_m, 4)
+        tensor per mip and, when the config has a LUT, (n, n, 2)."""
+        iw, ih = self.irradiance_size()
+        _require_shape(irr, "irradiance", (ih, iw, 4))
+        if len(mips) != self.cfg.mip_count:
+            raise IBLError(ERR_INVALID_ARGUMENT,
+                           f"{len(mips)} mip tensors; this context bakes {self.cfg.mip_count}")
+        for m, t in enumerate(mips):
+            w, h, _ = self.mip_info(m)
+            _require_shape(t, f"mip {m}", (h, w, 4))
+        if self.cfg.lut_size > 0:
+            n = self.cfg.lut_size
+            if lut is None:
+                raise IBLError(ERR_INVALID_ARGUMENT, f"this context bakes a {n}x{n} LUT: pass one")
+            _require_shape(lut, "lut", (n, n, 2))
         o = Outputs()
         _require_cuda(irr, "irradiance", 4)
         o.irradiance_dev = irr.data_ptr()
@@ -438,7 +494,7 @@ class BakeContext:
             _require_cuda(t, f"mip {m}", 4)
             o.mip_dev[m] = t.data_ptr()
             o.mip_pitch_bytes[m] = _pitch(t, 4)
-        if lut is not None:
+        if lut is not None and self.cfg.lut_size > 0:
             _require_cuda(lut, "lut", 2)
             o.lut_dev = lut.data_ptr()
             o.lut_pitch_bytes = _pitch(lut, 2)
@@ -621,6 +677,11 @@ def bake_tc(chain, w: int, h: int, outs: List, roughness: List[float], irradianc
     """Precision-path bake into CUDA tensors (mips and optional irradiance):
     float32 outputs are RGBA32F, float16 outputs RGBA16F (all of one type)."""
     torch = _torch()
+    _require_counts(outs, roughness)
+    if levels is not None and len(levels) != len(outs):
+        raise IBLError(ERR_INVALID_ARGUMENT,
+                       f"{len(levels)} source levels for {len(outs)} output mips")
+    _require_chain(chain, w, h)
     n = len(outs)
     arr = (MipTarget * max(n, 1))()
     all_out = list(outs) + ([irradiance] if irradiance is not None else [])
