@@ -78,7 +78,7 @@ struct althea_ibl_server {
   althea_ibl_server_config cfg{};
   std::vector<Slot*> slots;
   std::deque<Pending> queue;
-  std::vector<althea_ibl_completion> finished;  // retired, not yet returned
+  std::deque<althea_ibl_completion> finished;  // retired, not yet returned
   std::map<size_t, std::vector<void*>> free_blocks;
   size_t reserved = 0, in_use = 0, peak = 0;
   uint64_t completed = 0, rejected = 0;
@@ -328,14 +328,21 @@ extern "C" int althea_ibl_server_create(const althea_ibl_server_config* cfg,
 extern "C" size_t althea_ibl_server_request_bytes(const althea_ibl_server* s, int w, int h,
                                                   int mips) {
   if (!s || ibl::check_env(w, h) || mips < 1 || mips > ALTHEA_IBL_MAX_MIPS) return 0;
-  return layout_for(s, w, h, mips).total;
+  const size_t total = layout_for(s, w, h, mips).total;
+  return total == (size_t)-1 ? 0 : total;
 }
 
 extern "C" int althea_ibl_server_submit(althea_ibl_server* s, const althea_ibl_request* r) {
   if (!s) return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null server");
   int st = check_request(s, r);
   if (st) return st;
-  if (layout_for(s, r->env_width, r->env_height, r->mip_count).total > s->cfg.budget_bytes) {
+  const size_t total = layout_for(s, r->env_width, r->env_height, r->mip_count).total;
+  if (total == (size_t)-1) {
+    // the precision planner refused the shape; the last error holds its reason
+    s->rejected++;
+    return ALTHEA_IBL_ERR_UNSUPPORTED;
+  }
+  if (total > s->cfg.budget_bytes) {
     s->rejected++;
     return ibl::set_error(ALTHEA_IBL_ERR_BUDGET, "request needs more device memory than the "
                                                  "server budget of %zu bytes",
@@ -356,7 +363,7 @@ extern "C" int althea_ibl_server_poll(althea_ibl_server* s, althea_ibl_completio
   int k = 0;
   while (k < max && !s->finished.empty()) {
     out[k++] = s->finished.front();
-    s->finished.erase(s->finished.begin());
+    s->finished.pop_front();
   }
   *n = k;
   return ALTHEA_IBL_OK;

@@ -329,13 +329,16 @@ typedef struct althea_ibl_server althea_ibl_server;
 
 int althea_ibl_server_create(const althea_ibl_server_config* cfg, althea_ibl_server** out);
 /* Queues the request and admits what fits; never blocks on the GPU.  A request
- * whose memory alone exceeds the budget is refused with ALTHEA_IBL_ERR_BUDGET. */
+ * whose memory alone exceeds the budget is refused with ALTHEA_IBL_ERR_BUDGET;
+ * on the precision path, a shape the planner cannot run is refused with
+ * ALTHEA_IBL_ERR_UNSUPPORTED. */
 int althea_ibl_server_submit(althea_ibl_server* s, const althea_ibl_request* req);
 /* Retires finished requests (returning up to max completions), frees their
  * slots and memory, and admits queued requests that now fit. */
 int althea_ibl_server_poll(althea_ibl_server* s, althea_ibl_completion* out, int max, int* n);
 int althea_ibl_server_get_stats(const althea_ibl_server* s, althea_ibl_server_stats* st);
-/* Device memory a request of this size holds while in flight. */
+/* Device memory a request of this size holds while in flight; 0 for a size
+ * the server cannot run. */
 size_t althea_ibl_server_request_bytes(const althea_ibl_server* s, int env_width, int env_height,
                                        int mip_count);
 double althea_ibl_server_now(void);   /* the steady clock used in completions */
