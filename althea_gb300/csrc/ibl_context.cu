@@ -86,10 +86,14 @@ extern "C" int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_contex
     delete c;
     return st;
   }
-  cudaGetDevice(&c->device);
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_status(e, "cudaGetDevice");
+  }
   c->chain_texels = althea_ibl_chain_texels(w, h);
   c->irr_ws_bytes = irr_plan(w, h, c->irr_w, c->irr_h).workspace;
-  cudaError_t e = cudaMalloc(&c->chain, c->chain_texels * 16);
+  e = cudaMalloc(&c->chain, c->chain_texels * 16);
   if (e == cudaSuccess) e = cudaMalloc(&c->irr_ws, c->irr_ws_bytes);
   if (e != cudaSuccess) {
     if (c->chain) cudaFree(c->chain);
@@ -97,6 +101,18 @@ extern "C" int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_contex
     return cuda_status(e, "context allocation");
   }
   *out = c;
+  return ALTHEA_IBL_OK;
+}
+
+// The context's buffers live on the device that was current at create; a
+// launch from another device would touch memory it may not reach.
+static int check_device(const althea_ibl_context* c) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  if (dev != c->device)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
+                     "the context lives on device %d but device %d is current", c->device, dev);
   return ALTHEA_IBL_OK;
 }
 
@@ -131,13 +147,15 @@ extern "C" const float* althea_ibl_env_chain(const althea_ibl_context* c) {
 extern "C" int althea_ibl_upload_env(althea_ibl_context* c, const float* rgba, int src_is_device,
                                      void* stream) {
   if (!c || !rgba) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
+  int r = check_device(c);
+  if (r) return r;
   cudaStream_t st = (cudaStream_t)stream;
   size_t bytes = (size_t)c->cfg.env_width * c->cfg.env_height * 16;
   cudaError_t e = cudaMemcpyAsync(c->chain, rgba, bytes,
                                   src_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                   st);
   if (e != cudaSuccess) return cuda_status(e, "env upload");
-  int r = launch_build_chain(c->chain, c->cfg.env_width, c->cfg.env_height, c->chain, st);
+  r = launch_build_chain(c->chain, c->cfg.env_width, c->cfg.env_height, c->chain, st);
   if (r == ALTHEA_IBL_OK) c->env_ready = true;
   return r;
 }
@@ -146,9 +164,11 @@ extern "C" int althea_ibl_bake(althea_ibl_context* c, const althea_ibl_outputs* 
   if (!c || !o) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
   if (!c->env_ready)
     return set_error(ALTHEA_IBL_ERR_NOT_READY, "no environment map uploaded to this context");
+  int r = check_device(c);
+  if (r) return r;
   cudaStream_t st = (cudaStream_t)stream;
   const int w = c->cfg.env_width, h = c->cfg.env_height;
-  int r = check_image(o->irradiance_dev, c->irr_w, c->irr_h, o->irradiance_pitch_bytes, 16,
+  r = check_image(o->irradiance_dev, c->irr_w, c->irr_h, o->irradiance_pitch_bytes, 16,
                       "irradiance");
   if (r) return r;
   althea_ibl_mip_target mips[ALTHEA_IBL_MAX_MIPS];

@@ -155,6 +155,8 @@ typedef struct {
   size_t lut_pitch_bytes;
 } althea_ibl_outputs;
 
+/* The context's device memory lives on the device current at create;
+ * upload_env and bake refuse to run while another device is current. */
 int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_context** out);
 int althea_ibl_destroy(althea_ibl_context* ctx);
 /* Mip m size and roughness as the context bakes them. */
