@@ -1235,6 +1235,9 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
 int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int* levels,
               int irr_w, int irr_h, int irr_level, TcPlan& P) {
   size_t off = 256;  // error flag first
+  // A source level named by the caller must exist in the chain (the planner's
+  // own choices always do).
+  const int nlevels = chain_levels(w, h);
   for (int m = 0; m < n; ++m) {
     if (mips[m].roughness == 0.0f) {  // a delta: handled by the plain path
       P.jobs.push_back(JobPlan{});
@@ -1242,6 +1245,10 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
     }
     int lv = levels && levels[m] >= 0 ? levels[m]
                                       : planned_level(w, mips[m].width, mips[m].roughness, false);
+    if (lv >= nlevels)
+      return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
+                       "tensor path: mip %d source level %d; the chain has levels 0..%d", m, lv,
+                       nlevels - 1);
     int ws = level_dim(w, lv);
     if (ws < mips[m].width || ws % mips[m].width != 0 || mips[m].width > 4096 ||
         mips[m].height > 65536)
@@ -1253,6 +1260,10 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
   }
   if (irr_w > 0) {
     int lv = irr_level >= 0 ? irr_level : planned_level(w, irr_w, 1.0f, true);
+    if (lv >= nlevels)
+      return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
+                       "tensor path: irradiance source level %d; the chain has levels 0..%d", lv,
+                       nlevels - 1);
     int ws = level_dim(w, lv);
     if (ws < irr_w || ws % irr_w != 0 || irr_w > 4096)
       return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "tensor path: irradiance %dx%d vs level %d",
@@ -1303,6 +1314,9 @@ extern "C" size_t althea_ibl_tc_workspace_size(int w, int h, const althea_ibl_mi
 extern "C" int althea_ibl_tc_plan(int w, int h, const althea_ibl_mip_target* mips, int n,
                                   int irr_w, int* levels_out, int* irr_level_out) {
   if (check_env(w, h)) return ALTHEA_IBL_ERR_INVALID_ARGUMENT;
+  if (n < 0 || n > ALTHEA_IBL_MAX_MIPS || (n > 0 && (!mips || !levels_out)))
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "tensor plan: %d mips (0..%d, non-null)",
+                     n, ALTHEA_IBL_MAX_MIPS);
   for (int m = 0; m < n; ++m)
     levels_out[m] = mips[m].roughness == 0.0f
                         ? -1
@@ -1511,6 +1525,11 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
 size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n,
                           const int* levels, int irr_w, int irr_h, int irr_level) {
   if (check_env(w, h)) return 0;
+  if (n < 0 || n > ALTHEA_IBL_MAX_MIPS || (n > 0 && !mips)) {
+    set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "tensor path: %d mips (0..%d, non-null)", n,
+              ALTHEA_IBL_MAX_MIPS);
+    return 0;
+  }
   TcPlan P;
   if (make_plan(w, h, mips, n, levels, irr_w, irr_h, irr_level, P)) return 0;
   return P.total;

@@ -111,6 +111,34 @@ def test_precision_workspace_sizes_without_gpu():
     assert L.althea_ibl_tc_workspace_size(4096, 2048, bad, 1, None, 0, 0, -1) == 0
 
 
+def test_precision_source_levels_must_exist_in_the_chain():
+    """A caller-named source level past the chain's last level is refused
+    before any pointer into the chain is formed."""
+    L = ibl.load()
+    w, h = 64, 32  # levels 0..6
+    one = (ibl.MipTarget * 1)(ibl.MipTarget(0, 16, 1, 1, 0.5))
+    assert L.althea_ibl_tc_workspace_size(w, h, one, 1, (ctypes.c_int * 1)(6), 0, 0, -1) > 0
+    assert L.althea_ibl_tc_workspace_size(w, h, one, 1, (ctypes.c_int * 1)(7), 0, 0, -1) == 0
+    assert b"source level 7" in L.althea_ibl_last_error()
+    assert L.althea_ibl_tc_workspace_size(w, h, one, 1, (ctypes.c_int * 1)(40), 0, 0, -1) == 0
+    assert L.althea_ibl_tc_workspace_size(w, h, None, 0, None, 1, 1, 7) == 0
+    assert b"irradiance source level 7" in L.althea_ibl_last_error()
+    # counts outside 0..MAX_MIPS, or mips missing, are refused without touching them
+    assert L.althea_ibl_tc_workspace_size(w, h, None, 2, None, 0, 0, -1) == 0
+    assert L.althea_ibl_tc_workspace_size(w, h, one, ibl.MAX_MIPS + 1, None, 0, 0, -1) == 0
+    lv, il = (ctypes.c_int * 1)(), ctypes.c_int()
+    assert L.althea_ibl_tc_plan(w, h, None, 1, 0, lv, ctypes.byref(il)) == ibl.ERR_INVALID_ARGUMENT
+    assert L.althea_ibl_tc_plan(w, h, one, -1, 0, lv, ctypes.byref(il)) == ibl.ERR_INVALID_ARGUMENT
+    # the planner's own choices always name existing levels
+    for ew in (16, 256, 4096):
+        for mw in (1, 2, ew // 2):
+            lv1 = (ctypes.c_int * 1)()
+            t = (ibl.MipTarget * 1)(ibl.MipTarget(0, 16 * mw, mw, max(mw // 2, 1), 0.7))
+            assert L.althea_ibl_tc_plan(ew, ew // 2, t, 1, mw, lv1, ctypes.byref(il)) == ibl.OK
+            assert 0 <= lv1[0] < ibl.chain_levels(ew, ew // 2)
+            assert 0 <= il.value < ibl.chain_levels(ew, ew // 2)
+
+
 # ctypes mirror -> C type of include/althea_ibl.h
 _LAYOUTS = [
     (ibl.MipTarget, "althea_ibl_mip_target"), (ibl.Config, "althea_ibl_config"),
