@@ -62,11 +62,16 @@ void from_rgbe(const unsigned char* in, float* c) {
   c[3] = 1.0f;
 }
 
+// One header line without its terminator; "\r\n" endings (files written in
+// text mode on Windows) read like "\n" ones.
 bool read_line(FILE* f, std::string& line) {
   line.clear();
   int ch;
   while ((ch = fgetc(f)) != EOF) {
-    if (ch == '\n') return true;
+    if (ch == '\n') {
+      if (!line.empty() && line.back() == '\r') line.pop_back();
+      return true;
+    }
     line.push_back((char)ch);
     if (line.size() > 4096) return false;
   }

@@ -60,3 +60,59 @@ def test_rejects_non_radiance(tmp_path):
     from althea_gb300 import ibl
     with pytest.raises(ibl.IBLError):
         hdr.read_hdr(str(p))
+
+
+def test_reads_crlf_headers(tmp_path):
+    """Header lines ending in \\r\\n (text-mode writers on Windows) read the
+    same as \\n ones; the pixel data is binary either way."""
+    a = np.full((3, 16, 4), 0.75, np.float32)
+    a[..., 3] = 1.0
+    p = tmp_path / "lf.hdr"
+    hdr.write_hdr(str(p), a)
+    raw = p.read_bytes()
+    cut = raw.index(b"+X 16\n") + len(b"+X 16\n")
+    crlf = tmp_path / "crlf.hdr"
+    crlf.write_bytes(raw[:cut].replace(b"\n", b"\r\n") + raw[cut:])
+    assert np.array_equal(hdr.read_hdr(str(crlf)), hdr.read_hdr(str(p)))
+
+
+def _rle_file(w, h, body):
+    return b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y %d +X %d\n" % (h, w) + body
+
+
+@pytest.mark.parametrize("body", [
+    bytes([2, 2, 0, 16]) + bytes([128 + 17, 1]),            # a run past the row's end
+    bytes([2, 2, 0, 16]) + bytes([20]) + bytes(20),         # literals past the row's end
+    bytes([2, 2, 0, 16]) + bytes([0]),                      # a zero-length literal
+    bytes([2, 2, 0, 16]) + bytes([128 + 16, 1, 128 + 16]),  # stops inside a run
+    b"",                                                    # no pixels at all
+    bytes(16 * 4 - 1),                                      # a flat row one byte short
+])
+def test_corrupt_pixels_are_refused(tmp_path, body):
+    from althea_gb300 import ibl
+    p = tmp_path / "corrupt.hdr"
+    p.write_bytes(_rle_file(16, 1, body))
+    with pytest.raises(ibl.IBLError) as e:
+        hdr.read_hdr(str(p))
+    assert e.value.status == ibl.ERR_INVALID_ARGUMENT
+
+
+def test_hand_made_rle_row_decodes():
+    """One 16-pixel row written by hand: R a run of 16, G 16 literals, B two
+    runs of 8, E a run of 16 (exponent 129: mantissa m decodes to m / 128)."""
+    import tempfile
+    body = bytes([2, 2, 0, 16])
+    body += bytes([128 + 16, 64])
+    body += bytes([16]) + bytes(range(0, 160, 10))
+    body += bytes([128 + 8, 32, 128 + 8, 128])
+    body += bytes([128 + 16, 129])
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "row.hdr")
+        with open(p, "wb") as f:
+            f.write(_rle_file(16, 1, body))
+        img = hdr.read_hdr(p)
+    assert img.shape == (1, 16, 4)
+    assert np.all(img[0, :, 0] == 0.5)
+    assert np.array_equal(img[0, :, 1], np.arange(0, 160, 10, dtype=np.float32) / 128)
+    assert np.all(img[0, :8, 2] == 0.25) and np.all(img[0, 8:, 2] == 1.0)
+    assert np.all(img[0, :, 3] == 1.0)
