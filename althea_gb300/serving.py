@@ -11,7 +11,7 @@ from __future__ import annotations
 import ctypes
 import time
 from dataclasses import dataclass
-from typing import Dict, List, Optional
+from typing import Dict, List
 
 import numpy as np
 
@@ -41,7 +41,11 @@ class ProbeServer:
         self._s = ctypes.c_void_p()
         ibl._check(ibl.load().althea_ibl_server_create(ctypes.byref(self.cfg),
                                                        ctypes.byref(self._s)))
-        self._keep: Dict[int, RequestBuffers] = {}
+        # Each submission gets its own tag inside the native server, mapped back
+        # to the caller's tag on completion; its buffers are referenced here
+        # until then, so they stay alive while the device reads and writes them.
+        self._inflight: Dict[int, tuple] = {}
+        self._next = 0
         self._done = (ibl.Completion * 256)()
 
     def buffers(self, env_np: np.ndarray, mip_count: int) -> RequestBuffers:
@@ -56,11 +60,15 @@ class ProbeServer:
         return RequestBuffers(env, mips, irr, sizes)
 
     def submit(self, tag: int, buf: RequestBuffers) -> None:
+        """Queues a re-bake of buf.env into buf's outputs.  Its completion is
+        reported by poll() under `tag` (tags may repeat)."""
         h, w = buf.env.shape[:2]
+        key = self._next
         req = ibl.Request(buf.env.data_ptr(), w, h, len(buf.mip_sizes), buf.irradiance.data_ptr(),
-                          buf.mips.data_ptr(), tag)
-        self._keep[tag] = buf
+                          buf.mips.data_ptr(), key)
         ibl._check(ibl.load().althea_ibl_server_submit(self._s, ctypes.byref(req)))
+        self._next += 1
+        self._inflight[key] = (tag, buf)
 
     def poll(self) -> List[ibl.Completion]:
         n = ctypes.c_int()
@@ -70,7 +78,8 @@ class ProbeServer:
                                                          ctypes.byref(n)))
             for k in range(n.value):
                 c = self._done[k]
-                out.append(ibl.Completion(c.tag, c.status, c.submit_s, c.start_s, c.done_s))
+                tag, _ = self._inflight.pop(c.tag, (c.tag, None))  # buffers free again
+                out.append(ibl.Completion(tag, c.status, c.submit_s, c.start_s, c.done_s))
             if n.value < len(self._done):
                 return out
 
@@ -93,9 +102,6 @@ class ProbeServer:
             if time.monotonic() - t0 > timeout_s:
                 raise TimeoutError("server did not drain")
             time.sleep(0.0002)
-
-    def release(self, tag: int) -> Optional[RequestBuffers]:
-        return self._keep.pop(tag, None)
 
     def close(self) -> None:
         if self._s:
