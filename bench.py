@@ -105,6 +105,25 @@ def read_peaks():
     return 6800.0, "fallback"
 
 
+def smi_id(index):
+    """nvidia-smi's name for CUDA device `index`.  CUDA ordinals and nvidia-smi
+    indices differ when CUDA_VISIBLE_DEVICES hides or reorders GPUs, so the
+    device's UUID is used when nvidia-smi answers to it, else the
+    CUDA_VISIBLE_DEVICES entry, else the ordinal itself."""
+    try:
+        import torch
+        u = str(torch.cuda.get_device_properties(index).uuid)
+        cand = u if u.startswith("GPU-") else "GPU-" + u
+        r = subprocess.run(["nvidia-smi", f"--id={cand}", "--query-gpu=index",
+                            "--format=csv,noheader"], capture_output=True, text=True, timeout=10)
+        if r.returncode == 0 and r.stdout.strip():
+            return cand
+    except Exception:
+        pass
+    vis = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    return vis[index] if index < len(vis) else str(index)
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -112,7 +131,7 @@ class ClockSampler:
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index = index
+        self.index = smi_id(index)
         self.rows = []
         self._stop = threading.Event()
         self._t = None
@@ -146,7 +165,7 @@ class ClockSampler:
                           if len(r) > 4 + i and r[4 + i].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.rows)}
+                "samples": len(self.rows), "gpu": self.index}
 
 
 def dist_setup():
