@@ -1232,6 +1232,10 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   return ALTHEA_IBL_OK;
 }
 
+// Widest contracted output (mips with roughness > 0 and the irradiance): the
+// widths the kernels have been run and checked at.
+constexpr int kMaxTcWidth = 1024;
+
 int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int* levels,
               int irr_w, int irr_h, int irr_level, TcPlan& P) {
   size_t off = 256;  // error flag first
@@ -1250,7 +1254,7 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
                        "tensor path: mip %d source level %d; the chain has levels 0..%d", m, lv,
                        nlevels - 1);
     int ws = level_dim(w, lv);
-    if (ws < mips[m].width || ws % mips[m].width != 0 || mips[m].width > 4096 ||
+    if (ws < mips[m].width || ws % mips[m].width != 0 || mips[m].width > kMaxTcWidth ||
         mips[m].height > 65536)
       return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
                        "tensor path: mip %d (%dx%d) cannot contract against level %d", m,
@@ -1265,7 +1269,7 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
                        "tensor path: irradiance source level %d; the chain has levels 0..%d", lv,
                        nlevels - 1);
     int ws = level_dim(w, lv);
-    if (ws < irr_w || ws % irr_w != 0 || irr_w > 4096)
+    if (ws < irr_w || ws % irr_w != 0 || irr_w > kMaxTcWidth)
       return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "tensor path: irradiance %dx%d vs level %d",
                        irr_w, irr_h, lv);
     int st = add_job(P, w, h, irr_w, irr_h, 1.0f, 1, lv, off);

@@ -182,7 +182,10 @@ int althea_ibl_bake(althea_ibl_context* ctx, const althea_ibl_outputs* outs, voi
  * by althea_ibl_tc_plan so the result stays within 1e-3 of the same sum over
  * level 0; levels[m] = -1 selects the plan).  tcgen05 BF16 hi/lo MMAs with
  * FP32 accumulation in TMEM, FP64 weight normalisation.  Roughness-0 mips
- * (a delta) take the plain path.  Output mips must be at most 1024 wide.
+ * (a delta) take the plain path.  Contracted outputs (mips of roughness > 0,
+ * the irradiance) are at most 1024 wide, and their source level a whole
+ * multiple of their width; other shapes are refused with
+ * ALTHEA_IBL_ERR_UNSUPPORTED (althea_ibl_tc_workspace_size returns 0).
  * Workspace: althea_ibl_tc_workspace_size bytes, 256-byte aligned.
  * althea_ibl_tc_error synchronises the stream and reports a kernel that gave
  * up on a bounded wait. */

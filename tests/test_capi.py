@@ -123,6 +123,11 @@ def test_precision_source_levels_must_exist_in_the_chain():
     assert L.althea_ibl_tc_workspace_size(w, h, one, 1, (ctypes.c_int * 1)(40), 0, 0, -1) == 0
     assert L.althea_ibl_tc_workspace_size(w, h, None, 0, None, 1, 1, 7) == 0
     assert b"irradiance source level 7" in L.althea_ibl_last_error()
+    # contracted outputs are at most 1024 wide; roughness 0 (the delta path) is not contracted
+    for mw, r, ok in ((1024, 0.5, True), (2048, 0.5, False), (2048, 0.0, True)):
+        t = (ibl.MipTarget * 1)(ibl.MipTarget(0, 16 * mw, mw, mw // 2, r))
+        assert (L.althea_ibl_tc_workspace_size(4096, 2048, t, 1, None, 0, 0, -1) > 0) == ok
+    assert L.althea_ibl_tc_workspace_size(4096, 2048, None, 0, None, 2048, 1024, -1) == 0
     # counts outside 0..MAX_MIPS, or mips missing, are refused without touching them
     assert L.althea_ibl_tc_workspace_size(w, h, None, 2, None, 0, 0, -1) == 0
     assert L.althea_ibl_tc_workspace_size(w, h, one, ibl.MAX_MIPS + 1, None, 0, 0, -1) == 0
