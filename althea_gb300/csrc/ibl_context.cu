@@ -77,9 +77,12 @@ extern "C" int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_contex
     return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "samples/generator");
   }
   if (cfg->lut_size < 0 || cfg->lut_size > 16384 ||
-      (cfg->lut_size > 0 && (cfg->lut_samples < 1 || cfg->lut_samples > (1 << 24)))) {
+      (cfg->lut_size > 0 &&
+       (cfg->lut_samples < 1 || cfg->lut_samples > (1 << 24) ||
+        (cfg->lut_orientation != ALTHEA_IBL_LUT_ASSET &&
+         cfg->lut_orientation != ALTHEA_IBL_LUT_CORRECTED)))) {
     delete c;
-    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "lut_size/lut_samples");
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "lut_size/lut_samples/lut_orientation");
   }
   st = check_irradiance_args(w, h, c->irr_w, c->irr_h);
   if (st) {

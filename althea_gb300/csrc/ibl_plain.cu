@@ -428,7 +428,9 @@ int check_irradiance_args(int w, int h, int ow, int oh) {
     return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
                      "irradiance grid int(300*H/W) = %d for %dx%d; supported 1..%d", phi, w, h,
                      kMaxPhiSamples);
-  if (ow < 1 || oh < 1) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "irradiance size");
+  if (ow < 1 || oh < 1 || ow > 65536 || oh > 65536)
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "irradiance size %dx%d outside 1..65536",
+                     ow, oh);
   return ALTHEA_IBL_OK;
 }
 

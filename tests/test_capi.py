@@ -69,6 +69,16 @@ def test_argument_checks_without_gpu():
     ctx = ctypes.c_void_p()
     assert L.althea_ibl_create(ctypes.byref(bad), ctypes.byref(ctx)) == ibl.ERR_INVALID_ARGUMENT
     assert not ctx.value
+    # config checks come before any device work, so they answer without a GPU
+    for field, value, what in (("mip_count", 0, b"mip_count"), ("samples", 0, b"samples"),
+                               ("lut_orientation", 7, b"lut_orientation"),
+                               ("lut_samples", 0, b"lut_samples"),
+                               ("irradiance_width", 100000, b"irradiance size")):
+        cfg = ibl.make_config(64, 32, lut_size=16)
+        setattr(cfg, field, value)
+        assert L.althea_ibl_create(ctypes.byref(cfg), ctypes.byref(ctx)) == \
+            ibl.ERR_INVALID_ARGUMENT, field
+        assert what in L.althea_ibl_last_error() and not ctx.value
     assert L.althea_ibl_bake(None, None, None) == ibl.ERR_INVALID_ARGUMENT
 
 
