@@ -223,3 +223,25 @@ def test_header_compiles_as_cpp(tmp_path):
                    '          return c.mip_count + althea_ibl_abi_version(); }\n')
     subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
                            "-I", os.path.join(ROOT, "include"), str(src)])
+
+
+def test_cpp_consumer_links_and_runs(tmp_path):
+    """A C++ program (tests/capi_consumer.cpp) links the library through the
+    header alone and runs its device-free calls: planner, configs, RGBE files,
+    error reporting."""
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    lib = ibl.load()._name
+    exe = tmp_path / "consumer"
+    libdir = os.path.dirname(lib)
+    cudart = "/usr/local/cuda/lib64"
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-O1",
+                           "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "capi_consumer.cpp"), "-o", str(exe),
+                           "-L", libdir, "-lalthea_ibl", "-Wl,-rpath," + libdir,
+                           "-Wl,-rpath-link," + cudart, "-Wl,-rpath," + cudart])
+    out = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert "consumer ok" in out.stdout
