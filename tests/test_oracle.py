@@ -158,6 +158,29 @@ def test_single_bright_texel_gives_the_ggx_lobe():
         assert ref.max() > 1e-3 * L  # the lobe is actually sampled
 
 
+def test_single_bright_texel_irradiance():
+    """Known answer for the irradiance quadrature: an env that is 0 but for one
+    texel gives (1/pi) L max(0, n.w_t0) Omega_t0 at every output direction,
+    written here in numpy from the definition."""
+    w, h, L = 64, 32, 1000.0
+    x0, y0 = 40, 9
+    env = np.zeros((h, w, 4), dtype=np.float32)
+    env[y0, x0, :3] = L
+    ys, xs = np.mgrid[0:8, 0:16]
+    xy = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
+    got = oracle.quad_irradiance(env, 16, 8, xy)[:, 0]
+    yaw = np.pi * (2.0 * (x0 + 0.5) / w - 1.0)
+    pit = np.pi * ((y0 + 0.5) / h - 0.5)
+    d = np.array([np.cos(pit) * np.cos(yaw), np.sin(pit), np.cos(pit) * np.sin(yaw)])
+    omega = (2.0 * np.pi / w) * abs(np.sin(np.pi * ((y0 + 1) / h - 0.5)) -
+                                    np.sin(np.pi * (y0 / h - 0.5)))
+    ny, nx = np.pi * (xy[:, 1] / 8 - 0.5), np.pi * (2.0 * xy[:, 0] / 16 - 1.0)
+    n = np.stack([np.cos(ny) * np.cos(nx), np.sin(ny), np.cos(ny) * np.sin(nx)], 1)
+    ref = L * np.maximum(n @ d, 0.0) * omega / np.pi
+    assert np.allclose(got, ref, rtol=1e-9, atol=1e-12 * L)
+    assert (ref > 0).sum() > 20 and (ref == 0).sum() > 20  # both hemispheres are sampled
+
+
 def test_lut_known_answer_grazing_free_mirror():
     """At NoV -> 1 and roughness -> 0 the split-sum scale/bias tend to (1, 0)."""
     n = 64
