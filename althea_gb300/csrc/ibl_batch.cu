@@ -224,8 +224,12 @@ void load_tune_file_locked() {
   if (!f) return;
   char key[4096];
   int tx, ty, irr;
+  // Lines naming a tile shape or irradiance target this build does not have
+  // (an edited or stale file) are skipped.
   while (fscanf(f, "%4095s %d %d %d", key, &tx, &ty, &irr) == 4) {
-    for (int s = 0; s < kNumTileShapes; ++s)
+    bool known_irr = false;
+    for (int t = 0; t < kNumIrrTargets; ++t) known_irr = known_irr || kIrrTargets[t] == irr;
+    for (int s = 0; s < kNumTileShapes && known_irr; ++s)
       if (kTileShapes[s].tx == tx && kTileShapes[s].ty == ty) (*g_tune_cache)[key] = {s, irr};
   }
   fclose(f);
