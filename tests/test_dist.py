@@ -45,7 +45,7 @@ def test_two_gloo_ranks_agree_on_job_throughput():
     import torch.multiprocessing as mp
     world = 2
     sizes = [256, 512, 1024, 2048, 256, 512, 1024]
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of a process that runs threads
     out = mgr.dict()
     mp.spawn(_worker, args=(world, _free_port(), sizes, out), nprocs=world, join=True)
     r0, r1 = out[0], out[1]
