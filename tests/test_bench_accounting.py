@@ -1,0 +1,54 @@
+"""CPU checks of the numerators bench.py reports its rooflines against, for
+the 4096x2048 workloads, recomputed here from their definitions:
+
+* plain path: algorithmic gathered bytes, 128 B per sample (two levels x four
+  RGBA32F taps) for mips of roughness > 0, one 64 B bilinear tap per texel at
+  roughness 0, plus 16 B written per output texel;
+* precision path: 2 flops x 4 channels per (output texel, source texel) pair
+  of every contraction the planner emits, and the launches of one bake."""
+import bench
+from althea_gb300 import ibl
+
+
+def _plan():
+    return ibl.tc_plan(bench.ENV_W, bench.ENV_H, bench.mip_sizes(), bench.roughness(),
+                       bench.IRR_W)
+
+
+def test_workload_shape():
+    assert (bench.ENV_W, bench.ENV_H) == (4096, 2048)
+    assert bench.mip_sizes() == [(2048 >> m, 1024 >> m) for m in range(9)]
+    assert bench.roughness() == [m / 8 for m in range(9)]
+    assert (bench.IRR_W, bench.IRR_H) == (128, 64)
+
+
+def test_plain_algorithmic_bytes():
+    texels = [w * h for w, h in bench.mip_sizes()]
+    gathers = texels[0] * 64 + sum(texels[1:]) * bench.SAMPLES * 128
+    assert bench.prefilter_algorithmic_bytes() == gathers + 16 * sum(texels)
+    assert round(bench.prefilter_algorithmic_bytes() / 1e9, 2) == 91.80
+
+
+def test_precision_flops_and_jobs():
+    levels, irr_level = _plan()
+    assert levels == [-1, 2, 2, 2, 1, 1, 1, 1, 1] and irr_level == 1
+    pairs = 0
+    for (w, h), lv in list(zip(bench.mip_sizes(), levels)) + [((128, 64), irr_level)]:
+        if lv >= 0:
+            pairs += w * h * (4096 >> lv) * (2048 >> lv)
+    alg, executed = bench.tc_flops(levels, irr_level)
+    assert alg == 8 * pairs and executed == 18 * pairs
+    assert round(alg / 1e12, 2) == 3.21
+    # phase counts: s = source / output width; g = 1, s / 8 or s
+    for w, h, ws, hs, lv, g in bench.tc_jobs(levels, irr_level):
+        s = ws // w
+        assert ws % w == 0 and 8 * g == s * (8 // s if 8 % s == 0 else (1 if s % 8 == 0 else 8))
+
+
+def test_precision_launches_per_bake():
+    """12 chain blits, 2 split passes (levels 1 and 2), 1 tables pass,
+    6 contractions (mips 1-6 and the irradiance, mip 4 and the irradiance
+    paired in one launch), 1 finish, 2 x 2 for the 16x8 and 8x4 mips on the
+    CUDA cores, 1 delta mip, 1 LUT: 28."""
+    levels, irr_level = _plan()
+    assert bench.tc_launches(levels, irr_level) == 12 + 2 + 1 + 6 + 1 + 4 + 1 + 1 == 28
