@@ -269,3 +269,28 @@ def test_ref_library_agrees_on_random_case():
         a = oracle.prefilter(chain, w, h, 48, 24, r, 512, xy=xy)
         b = oracle.ref_prefilter(chain, w, h, 48, 24, r, 512, xy=xy)[xy[:, 1], xy[:, 0]]
         assert np.array_equal(a, b)
+
+
+@pytest.mark.skipif(oracle.ref_lib() is None, reason="oracle/_ref not built on this machine")
+@pytest.mark.parametrize("w,h,seed", [(37, 19, 1), (64, 33, 2), (100, 7, 3), (2, 1, 4), (1, 1, 5),
+                                      (200, 100, 6)])
+def test_ref_library_agrees_on_odd_sizes(w, h, seed):
+    """The C restatement against the reference shaders compiled as C++, bit
+    for bit, on env sizes with odd and degenerate levels (1-texel rows and
+    columns, non-power-of-two chains), both sample generators, every texel of
+    small outputs, and the irradiance at env size."""
+    env = synth.make_env(w, h, seed=seed, sun_max=1e4)
+    chain = oracle.build_chain(env)
+    assert np.array_equal(chain, oracle.ref_build_chain(env))
+    ow, oh = max(w // 2, 1), max(h // 2, 1)
+    for gen in (oracle.GEN_REF_HASH, oracle.GEN_HAMMERSLEY):
+        for r in (0.0, 0.2, 0.55, 1.0):
+            a = oracle.prefilter(chain, w, h, ow, oh, r, 256, gen)
+            b = oracle.ref_prefilter(chain, w, h, ow, oh, r, 256, gen)
+            assert np.array_equal(a, b, equal_nan=True), (gen, r)
+    if int(300 * h / w) >= 1:  # the reference's grid has at least one phi step
+        rng = np.random.default_rng(seed)
+        xy = np.stack([rng.integers(0, w, 6), rng.integers(0, h, 6)], 1).astype(np.int32)
+        a = oracle.irradiance(chain, w, h, w, h, xy=xy)
+        b = oracle.ref_irradiance_envsize(chain, w, h, xy)[xy[:, 1], xy[:, 0]]
+        assert np.array_equal(a, b)
