@@ -172,7 +172,7 @@ extern "C" int althea_ibl_bake(althea_ibl_context* c, const althea_ibl_outputs* 
   cudaStream_t st = (cudaStream_t)stream;
   const int w = c->cfg.env_width, h = c->cfg.env_height;
   r = check_image(o->irradiance_dev, c->irr_w, c->irr_h, o->irradiance_pitch_bytes, 16,
-                      "irradiance");
+                  "irradiance");
   if (r) return r;
   althea_ibl_mip_target mips[ALTHEA_IBL_MAX_MIPS];
   for (int m = 0; m < c->cfg.mip_count; ++m) {
