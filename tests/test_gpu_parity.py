@@ -158,10 +158,13 @@ def test_create_resources_interface():
     assert res.getHandles() == (0, 1, 2, 3)
 
 
-def test_production_size_sampled_texels():
+@pytest.mark.parametrize("gen", [ibl.GEN_REF_HASH, ibl.GEN_HAMMERSLEY])
+def test_production_size_sampled_texels(gen):
     # 4096x2048 map, 9 mips from 2048x1024 (roughness m/8), 128x64 irradiance,
     # N = 1024: sampled texels against the oracle (every texel is too slow for
-    # the oracle), plus seam, pole rows and corners.
+    # the oracle), plus seam, pole rows and corners; bit-identical.  The
+    # Hammersley generator takes its own code path in the kernel (the sample
+    # half-vectors tabulated once per block in shared memory).
     w, h = 4096, 2048
     env = synth.make_env(w, h, seed=0, sun_max=1e4)
     chain = oracle.build_chain(env)
@@ -171,8 +174,8 @@ def test_production_size_sampled_texels():
     assert torch.equal(got_chain, chain_d)
     sizes = [(2048 >> m, 1024 >> m) for m in range(9)]
     rough = [m / 8.0 for m in range(9)]
-    outs = run_prefilter(chain_d, w, h, sizes, rough, 1024, ibl.GEN_REF_HASH)
-    rng = np.random.default_rng(1)
+    outs = run_prefilter(chain_d, w, h, sizes, rough, 1024, gen)
+    rng = np.random.default_rng(1 + gen)
     for m, ((ow, oh), r) in enumerate(zip(sizes, rough)):
         n = 160
         xs = rng.integers(0, ow, n)
@@ -180,10 +183,11 @@ def test_production_size_sampled_texels():
         extra = np.array([[0, 0], [ow - 1, oh - 1], [0, oh - 1], [ow - 1, 0], [ow // 2, 0],
                           [0, oh // 2], [ow // 2, oh // 2]])
         xy = np.concatenate([np.stack([xs, ys], 1), extra]).astype(np.int32)
-        ref = oracle.prefilter(chain, w, h, ow, oh, r, 1024, oracle.GEN_REF_HASH, xy=xy)
+        ref = oracle.prefilter(chain, w, h, ow, oh, r, 1024, gen, xy=xy)
         got = outs[m][xy[:, 1], xy[:, 0]]
         err = rel_err(got, ref)
         assert err.max() <= TOL, (m, err.max())
+        assert np.array_equal(got, ref), f"mip {m} not bit-identical"
         assert np.isfinite(outs[m]).all() and (outs[m][..., :3] > 0).all()
     irr = torch.empty((64, 128, 4), dtype=torch.float32, device="cuda")
     ibl.irradiance(chain_d, w, h, irr)
