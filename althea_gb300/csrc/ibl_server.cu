@@ -12,6 +12,11 @@
 // would synchronise the device); free blocks of other sizes are released only
 // when a new size class would otherwise exceed the budget.
 //
+// Resident maps: althea_ibl_server_register_env uploads an env map once and
+// keeps it on the device (its bytes count against the budget); a request that
+// names it copies it on the device into its own chain, adds the request's sun
+// lobes (ibl_suns.cu) and bakes, so no env map crosses the host link.
+//
 // Host code only; the kernels are the single-probe ones (ibl_plain.cu, or
 // ibl_tc.cu when the server runs the precision path), whose results do not
 // depend on what else runs on the device.
@@ -65,6 +70,14 @@ struct Slot {
   size_t bytes = 0;
   int status = ALTHEA_IBL_OK;
   int env_width = 0, env_height = 0, mip_count = 0;  // shape of the request in flight
+  int env_id = 0;                                    // resident map it reads, or 0
+};
+
+struct ResidentEnv {
+  float* level0 = nullptr;  // RGBA32F, tightly packed
+  int width = 0, height = 0;
+  size_t bytes = 0;
+  int users = 0;            // queued and running requests that read it
 };
 
 struct Pending {
@@ -82,6 +95,9 @@ struct althea_ibl_server {
   std::map<size_t, std::vector<void*>> free_blocks;
   size_t reserved = 0, in_use = 0, peak = 0;
   uint64_t completed = 0, rejected = 0;
+  std::map<int, ResidentEnv> resident;
+  size_t resident_bytes = 0;
+  int next_env_id = 1;
 };
 
 namespace {
@@ -130,18 +146,10 @@ Layout layout_for(const althea_ibl_server* s, int w, int h, int mips) {
 }
 
 // Block of exactly `bytes` from the pool; false when it cannot fit now.
-bool pool_acquire(althea_ibl_server* s, size_t bytes, void** out) {
-  if (s->in_use + bytes > s->cfg.budget_bytes) return false;
-  auto it = s->free_blocks.find(bytes);
-  if (it != s->free_blocks.end() && !it->second.empty()) {
-    *out = it->second.back();
-    it->second.pop_back();
-    s->in_use += bytes;
-    if (s->in_use > s->peak) s->peak = s->in_use;
-    return true;
-  }
-  // A new block: release idle blocks of other sizes until it fits.
-  while (s->reserved + bytes > s->cfg.budget_bytes) {
+// Frees idle pool blocks until `extra` more bytes fit the budget beside the
+// reserved blocks and the resident maps; false when they cannot.
+bool make_room(althea_ibl_server* s, size_t extra) {
+  while (s->reserved + s->resident_bytes + extra > s->cfg.budget_bytes) {
     bool freed = false;
     for (auto& kv : s->free_blocks) {
       if (!kv.second.empty()) {
@@ -154,6 +162,21 @@ bool pool_acquire(althea_ibl_server* s, size_t bytes, void** out) {
     }
     if (!freed) return false;
   }
+  return true;
+}
+
+bool pool_acquire(althea_ibl_server* s, size_t bytes, void** out) {
+  if (s->in_use + s->resident_bytes + bytes > s->cfg.budget_bytes) return false;
+  auto it = s->free_blocks.find(bytes);
+  if (it != s->free_blocks.end() && !it->second.empty()) {
+    *out = it->second.back();
+    it->second.pop_back();
+    s->in_use += bytes;
+    if (s->in_use > s->peak) s->peak = s->in_use;
+    return true;
+  }
+  // A new block: release idle blocks of other sizes until it fits.
+  if (!make_room(s, bytes)) return false;
   void* p = nullptr;
   if (cudaMalloc(&p, bytes) != cudaSuccess) {
     cudaGetLastError();
@@ -177,9 +200,20 @@ int start(althea_ibl_server* s, Slot* slot, const Pending& pend, const Layout& L
   char* base = static_cast<char*>(slot->block);
   float* chain = reinterpret_cast<float*>(base + L.chain_off);
   int status = ALTHEA_IBL_OK;
-  cudaError_t e = cudaMemcpyAsync(chain, r.env_host, (size_t)r.env_width * r.env_height * 16,
-                                  cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) status = ibl::cuda_status(e, "server env upload");
+  cudaError_t e = cudaSuccess;
+  if (r.env_id) {
+    // the resident map plus this request's suns, written into the request's chain
+    const ResidentEnv& env = s->resident.at(r.env_id);
+    status = ibl::launch_apply_suns(env.level0, chain, r.env_width, r.env_height, r.suns,
+                                    r.sun_count, st);
+  } else {
+    e = cudaMemcpyAsync(chain, r.env_host, (size_t)r.env_width * r.env_height * 16,
+                        cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) status = ibl::cuda_status(e, "server env upload");
+    if (!status && r.sun_count > 0)
+      status = ibl::launch_apply_suns(chain, chain, r.env_width, r.env_height, r.suns,
+                                      r.sun_count, st);
+  }
   if (!status) status = ibl::launch_build_chain(chain, r.env_width, r.env_height, chain, st);
   althea_ibl_mip_target mips[ALTHEA_IBL_MAX_MIPS];
   mip_targets(L, base, r.mip_count, mips);
@@ -226,13 +260,14 @@ void admit(althea_ibl_server* s) {
   while (!s->queue.empty()) {
     const Pending& head = s->queue.front();
     Layout L = layout_for(s, head.req.env_width, head.req.env_height, head.req.mip_count);
-    if (L.total > s->cfg.budget_bytes) {  // can never fit
+    if (L.total + s->resident_bytes > s->cfg.budget_bytes) {  // cannot fit beside the maps
       althea_ibl_completion c{};
       c.tag = head.req.tag;
       c.status = ALTHEA_IBL_ERR_BUDGET;
       c.submit_s = c.start_s = c.done_s = head.submit_s;
       s->finished.push_back(c);
       s->rejected++;
+      if (head.req.env_id) s->resident[head.req.env_id].users--;
       s->queue.pop_front();
       continue;
     }
@@ -254,6 +289,7 @@ void admit(althea_ibl_server* s) {
     free_slot->env_width = head.req.env_width;
     free_slot->env_height = head.req.env_height;
     free_slot->mip_count = head.req.mip_count;
+    free_slot->env_id = head.req.env_id;
     start(s, free_slot, head, L);
     s->queue.pop_front();
   }
@@ -277,6 +313,8 @@ void retire(althea_ibl_server* s) {
     }
     s->finished.push_back(c);
     pool_release(s, sl->block, sl->bytes);
+    if (sl->env_id) s->resident[sl->env_id].users--;
+    sl->env_id = 0;
     sl->block = nullptr;
     sl->busy = false;
     s->completed++;
@@ -284,7 +322,22 @@ void retire(althea_ibl_server* s) {
 }
 
 int check_request(const althea_ibl_server* s, const althea_ibl_request* r) {
-  if (!r || !r->env_host) return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null request");
+  if (!r) return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null request");
+  if (r->env_id) {
+    auto it = s->resident.find(r->env_id);
+    if (it == s->resident.end())
+      return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "env_id %d is not registered",
+                            r->env_id);
+    if (it->second.width != r->env_width || it->second.height != r->env_height)
+      return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
+                            "request size %dx%d; resident map %d is %dx%d", r->env_width,
+                            r->env_height, r->env_id, it->second.width, it->second.height);
+  } else if (!r->env_host) {
+    return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "request: no env_host and no env_id");
+  }
+  if (r->sun_count < 0 || r->sun_count > ALTHEA_IBL_MAX_SUNS)
+    return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "request sun_count %d outside 0..%d",
+                          r->sun_count, ALTHEA_IBL_MAX_SUNS);
   int st = ibl::check_env(r->env_width, r->env_height);
   if (st) return st;
   if (r->mip_count < 1 || r->mip_count > ALTHEA_IBL_MAX_MIPS)
@@ -342,12 +395,14 @@ extern "C" int althea_ibl_server_submit(althea_ibl_server* s, const althea_ibl_r
     s->rejected++;
     return ALTHEA_IBL_ERR_UNSUPPORTED;
   }
-  if (total > s->cfg.budget_bytes) {
+  if (total + s->resident_bytes > s->cfg.budget_bytes) {
     s->rejected++;
     return ibl::set_error(ALTHEA_IBL_ERR_BUDGET, "request needs more device memory than the "
-                                                 "server budget of %zu bytes",
-                          s->cfg.budget_bytes);
+                                                 "server budget of %zu bytes leaves beside "
+                                                 "%zu bytes of resident maps",
+                          s->cfg.budget_bytes, s->resident_bytes);
   }
+  if (r->env_id) s->resident[r->env_id].users++;
   s->queue.push_back(Pending{*r, now_s()});
   retire(s);
   admit(s);
@@ -380,6 +435,57 @@ extern "C" int althea_ibl_server_get_stats(const althea_ibl_server* s, althea_ib
   st->peak_bytes_in_use = s->peak;
   st->completed = s->completed;
   st->rejected = s->rejected;
+  st->bytes_resident = s->resident_bytes;
+  st->resident_maps = (int)s->resident.size();
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_server_register_env(althea_ibl_server* s, const float* rgba, int w,
+                                              int h, int src_is_device, int* env_id_out) {
+  if (!s || !rgba || !env_id_out)
+    return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
+  *env_id_out = 0;
+  int st = ibl::check_env(w, h);
+  if (st) return st;
+  const size_t bytes = (size_t)w * h * 16;
+  if (!make_room(s, bytes))
+    return ibl::set_error(ALTHEA_IBL_ERR_BUDGET,
+                          "a %dx%d map (%zu bytes) does not fit the budget of %zu bytes beside "
+                          "%zu bytes in use and %zu resident",
+                          w, h, bytes, s->cfg.budget_bytes, s->in_use, s->resident_bytes);
+  ResidentEnv env;
+  env.width = w;
+  env.height = h;
+  env.bytes = bytes;
+  cudaError_t e = cudaMalloc(&env.level0, bytes);
+  if (e != cudaSuccess) return ibl::cuda_status(e, "resident map allocation");
+  e = cudaMemcpy(env.level0, rgba, bytes,
+                 src_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(env.level0);
+    return ibl::cuda_status(e, "resident map upload");
+  }
+  const int id = s->next_env_id++;
+  s->resident[id] = env;
+  s->resident_bytes += bytes;
+  *env_id_out = id;
+  return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_server_unregister_env(althea_ibl_server* s, int env_id) {
+  if (!s) return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null server");
+  retire(s);  // requests that finished no longer hold the map
+  auto it = s->resident.find(env_id);
+  if (it == s->resident.end())
+    return ibl::set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "env_id %d is not registered",
+                          env_id);
+  if (it->second.users > 0)
+    return ibl::set_error(ALTHEA_IBL_ERR_NOT_READY, "resident map %d is used by %d requests",
+                          env_id, it->second.users);
+  cudaFree(it->second.level0);
+  s->resident_bytes -= it->second.bytes;
+  s->resident.erase(it);
+  admit(s);  // memory freed: queued requests may fit now
   return ALTHEA_IBL_OK;
 }
 
@@ -396,6 +502,7 @@ extern "C" int althea_ibl_server_destroy(althea_ibl_server* s) {
   }
   for (auto& kv : s->free_blocks)
     for (void* p : kv.second) cudaFree(p);
+  for (auto& kv : s->resident) cudaFree(kv.second.level0);
   delete s;
   return ALTHEA_IBL_OK;
 }

@@ -1,10 +1,11 @@
 """Probe re-bake serving over the native server (althea_ibl_server_*).
 
-``ProbeServer`` owns one server: requests carry host (pinned) env maps and host
-output buffers; the server admits them by slot and HBM budget, overlaps their
-work on the device and reports completion times on its steady clock.
-``run_poisson`` replays a Poisson arrival stream against a server and returns
-latency percentiles and throughput.
+``ProbeServer`` owns one server: requests carry host (pinned) env maps, or
+name a map registered with the server (resident on the device) plus the sun
+lobes to add to it, and host output buffers; the server admits them by slot
+and HBM budget, overlaps their work on the device and reports completion
+times on its steady clock.  ``run_poisson`` replays a Poisson arrival stream
+against a server and returns latency percentiles and throughput.
 """
 from __future__ import annotations
 
@@ -20,10 +21,12 @@ from . import ibl
 
 @dataclass
 class RequestBuffers:
-    env: object            # pinned (H, W, 4) float32 host tensor
+    env: object            # pinned (H, W, 4) float32 host tensor, or None (resident map)
     mips: object           # pinned flat float32 host tensor (all mips back to back)
     irradiance: object     # pinned (ih, iw, 4) float32 host tensor
     mip_sizes: List[tuple]
+    env_id: int = 0        # a map registered with the server, or 0
+    env_size: tuple = (0, 0)   # (W, H) of the env map
 
 
 def mip_sizes_for(w: int, h: int, mip_count: int) -> List[tuple]:
@@ -45,6 +48,7 @@ class ProbeServer:
         # to the caller's tag on completion; its buffers are referenced here
         # until then, so they stay alive while the device reads and writes them.
         self._inflight: Dict[int, tuple] = {}
+        self._resident: Dict[int, tuple] = {}
         self._next = 0
         self._done = (ibl.Completion * 256)()
 
@@ -57,15 +61,58 @@ class ProbeServer:
         mips = torch.empty(sum(a * b * 4 for a, b in sizes), dtype=torch.float32).pin_memory()
         iw, ih = self.irradiance_size
         irr = torch.empty((ih, iw, 4), dtype=torch.float32).pin_memory()
-        return RequestBuffers(env, mips, irr, sizes)
+        return RequestBuffers(env, mips, irr, sizes, 0, (w, h))
 
-    def submit(self, tag: int, buf: RequestBuffers) -> None:
-        """Queues a re-bake of buf.env into buf's outputs.  Its completion is
-        reported by poll() under `tag` (tags may repeat)."""
-        h, w = buf.env.shape[:2]
+    def register_env(self, env) -> int:
+        """Uploads an (H, W, 4) float32 map (numpy, host or CUDA tensor) once;
+        it stays on the device, counted against the budget.  Returns its id."""
+        import torch
+        t = env if isinstance(env, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(env))
+        t = t.contiguous()
+        if t.dtype != torch.float32 or t.dim() != 3 or t.shape[2] != 4:
+            raise ibl.IBLError(ibl.ERR_INVALID_ARGUMENT, "env must be (H, W, 4) float32")
+        h, w = t.shape[:2]
+        out = ctypes.c_int()
+        ibl._check(ibl.load().althea_ibl_server_register_env(
+            self._s, t.data_ptr(), w, h, 1 if t.is_cuda else 0, ctypes.byref(out)))
+        self._resident[out.value] = (w, h)
+        return out.value
+
+    def unregister_env(self, env_id: int) -> None:
+        ibl._check(ibl.load().althea_ibl_server_unregister_env(self._s, env_id))
+        self._resident.pop(env_id, None)
+
+    def output_buffers(self, env_id: int, mip_count: int) -> RequestBuffers:
+        """Pinned host outputs for requests on a resident map (no env buffer)."""
+        import torch
+        w, h = self._resident[env_id]
+        sizes = mip_sizes_for(w, h, mip_count)
+        mips = torch.empty(sum(a * b * 4 for a, b in sizes), dtype=torch.float32).pin_memory()
+        iw, ih = self.irradiance_size
+        irr = torch.empty((ih, iw, 4), dtype=torch.float32).pin_memory()
+        return RequestBuffers(None, mips, irr, sizes, env_id, (w, h))
+
+    def submit(self, tag: int, buf: RequestBuffers, suns=()) -> None:
+        """Queues a re-bake into buf's outputs -- of buf.env, or of the resident
+        map buf.env_id -- with the given sun lobes [(direction, sigma rad,
+        radiance), ...] added on the device first.  Its completion is reported
+        by poll() under `tag` (tags may repeat)."""
+        if buf.env is not None:
+            h, w = buf.env.shape[:2]
+        else:
+            w, h = buf.env_size
         key = self._next
-        req = ibl.Request(buf.env.data_ptr(), w, h, len(buf.mip_sizes), buf.irradiance.data_ptr(),
-                          buf.mips.data_ptr(), key)
+        req = ibl.Request()
+        req.env_host = buf.env.data_ptr() if buf.env is not None else None
+        req.env_width, req.env_height = w, h
+        req.mip_count = len(buf.mip_sizes)
+        req.irradiance_host = buf.irradiance.data_ptr()
+        req.mips_host = buf.mips.data_ptr()
+        req.tag = key
+        req.env_id = buf.env_id
+        arr, n = ibl.make_suns(suns)
+        req.sun_count = n
+        req.suns = arr
         ibl._check(ibl.load().althea_ibl_server_submit(self._s, ctypes.byref(req)))
         self._next += 1
         self._inflight[key] = (tag, buf)
@@ -120,9 +167,10 @@ def now() -> float:
 
 
 def run_poisson(server: ProbeServer, pool: List[RequestBuffers], rate: float, n_requests: int,
-                seed: int = 0) -> dict:
+                seed: int = 0, suns_for=None) -> dict:
     """Submits n_requests at Poisson arrival times (rate per second), cycling
     through the prepared request buffers, and returns latency statistics.
+    suns_for(i): the sun lobes of request i (added on the device), or None.
     Latency = completion (host callback on the request's stream) - arrival."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, size=n_requests)
@@ -143,7 +191,7 @@ def run_poisson(server: ProbeServer, pool: List[RequestBuffers], rate: float, n_
             time.sleep(0.00005)
         arrival_abs[i] = target
         in_use[k] = i
-        server.submit(i, pool[k])
+        server.submit(i, pool[k], suns_for(i) if suns_for is not None else ())
     for c in server.drain():
         done[c.tag] = c
     t_end = max(c.done_s for c in done.values())

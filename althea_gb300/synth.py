@@ -75,6 +75,21 @@ def sun_params(w: int, h: int, seed: int = 0, sun_max: float = 1e4, n_suns: int 
     return suns
 
 
+def draw_suns(seed: int, sun_max: float = 1e4, n_suns: int = 8):
+    """n_suns suns drawn like make_env's (direction uniform on the sphere,
+    sigma ~ U[1, 3] degrees, radiance log-uniform in [1, sun_max]) from their
+    own PCG64 stream: the per-request suns of a re-bake of a resident sky."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    suns = []
+    for _ in range(n_suns):
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        sigma = np.deg2rad(rng.uniform(1.0, 3.0))
+        lum = float(np.exp(rng.uniform(0.0, np.log(sun_max))))
+        suns.append((d, sigma, lum))
+    return suns
+
+
 def make_tinted_env(w: int, h: int, seed: int = 0) -> np.ndarray:
     """A small map whose channels differ (tests that channels stay apart)."""
     rng = np.random.Generator(np.random.PCG64(seed))
