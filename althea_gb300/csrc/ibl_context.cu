@@ -9,6 +9,7 @@
 
 #include <cstring>
 #include <new>
+#include <string>
 
 #include "althea_ibl.h"
 #include "ibl_internal.h"
@@ -23,10 +24,45 @@ struct althea_ibl_context {
   float mip_r[ALTHEA_IBL_MAX_MIPS];
   float* chain;
   size_t chain_texels;
-  void* irr_ws;
+  void* irr_ws;          // plain path: irradiance partial sums
   size_t irr_ws_bytes;
+  void* tc_ws;           // precision path: the planned contraction's workspace
+  size_t tc_ws_bytes;
   bool env_ready;
+  // Side streams for work independent of the tensor-core contractions: the
+  // LUT (lut_side) and the outputs summed on the CUDA cores (narrow_side),
+  // forked from and joined back into the caller's stream inside each bake.
+  cudaStream_t lut_stream, narrow_stream;
+  cudaEvent_t lut_fork, lut_join, narrow_fork, narrow_join;
 };
+
+static void free_side_streams(althea_ibl_context* c) {
+  if (c->lut_stream) cudaStreamDestroy(c->lut_stream);
+  if (c->narrow_stream) cudaStreamDestroy(c->narrow_stream);
+  for (cudaEvent_t ev : {c->lut_fork, c->lut_join, c->narrow_fork, c->narrow_join})
+    if (ev) cudaEventDestroy(ev);
+}
+
+static cudaError_t make_side_streams(althea_ibl_context* c) {
+  cudaError_t e = cudaStreamCreateWithFlags(&c->lut_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->narrow_stream, cudaStreamNonBlocking);
+  for (cudaEvent_t* ev : {&c->lut_fork, &c->lut_join, &c->narrow_fork, &c->narrow_join})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  return e;
+}
+
+// The context's mips as planner targets (no output pointers: planning and
+// workspace sizing look at sizes and roughness only).
+static void mip_targets(const althea_ibl_context* c, althea_ibl_mip_target* t) {
+  const size_t texel = c->cfg.out_format == ALTHEA_IBL_FORMAT_RGBA16F ? 8 : 16;
+  for (int m = 0; m < c->cfg.mip_count; ++m) {
+    t[m].out_dev = nullptr;
+    t[m].pitch_bytes = (size_t)c->mip_w[m] * texel;
+    t[m].width = c->mip_w[m];
+    t[m].height = c->mip_h[m];
+    t[m].roughness = c->mip_r[m];
+  }
+}
 
 extern "C" void althea_ibl_config_reference(althea_ibl_config* c, int w, int h) {
   if (!c) return;
@@ -43,6 +79,8 @@ extern "C" void althea_ibl_config_reference(althea_ibl_config* c, int w, int h) 
   c->lut_size = 0;           // the reference loads brdf_lut.png instead
   c->lut_samples = 1024;
   c->lut_orientation = ALTHEA_IBL_LUT_ASSET;
+  c->path = ALTHEA_IBL_PATH_PLAIN;  // the reference's estimator
+  c->out_format = ALTHEA_IBL_FORMAT_RGBA32F;
 }
 
 extern "C" int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_context** out) {
@@ -84,10 +122,40 @@ extern "C" int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_contex
     delete c;
     return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "lut_size/lut_samples/lut_orientation");
   }
+  if (cfg->path != ALTHEA_IBL_PATH_PLAIN && cfg->path != ALTHEA_IBL_PATH_PRECISION) {
+    delete c;
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "path %d (plain 0, precision 1)",
+                     cfg->path);
+  }
+  if (cfg->out_format != ALTHEA_IBL_FORMAT_RGBA32F &&
+      cfg->out_format != ALTHEA_IBL_FORMAT_RGBA16F) {
+    delete c;
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "out_format %d (RGBA32F 0, RGBA16F 1)",
+                     cfg->out_format);
+  }
+  if (cfg->path == ALTHEA_IBL_PATH_PLAIN && cfg->out_format != ALTHEA_IBL_FORMAT_RGBA32F) {
+    delete c;
+    return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
+                     "out_format RGBA16F: the plain path writes RGBA32F (the reference's format)");
+  }
   st = check_irradiance_args(w, h, c->irr_w, c->irr_h);
   if (st) {
     delete c;
     return st;
+  }
+  const bool precision = cfg->path == ALTHEA_IBL_PATH_PRECISION;
+  if (precision) {
+    // Plan now, so that a shape the planner cannot run is refused at create
+    // and the workspace is sized once (the reference allocates its bake
+    // temporaries per bake, Src/ImageBasedLighting.cpp:137-412).
+    althea_ibl_mip_target t[ALTHEA_IBL_MAX_MIPS];
+    mip_targets(c, t);
+    c->tc_ws_bytes = tc_workspace_bytes(w, h, t, cfg->mip_count, nullptr, c->irr_w, c->irr_h, -1);
+    if (c->tc_ws_bytes == 0) {
+      delete c;
+      const std::string why = last_error();  // set_error writes the same buffer
+      return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "precision path: %s", why.c_str());
+    }
   }
   cudaError_t e = cudaGetDevice(&c->device);
   if (e != cudaSuccess) {
@@ -95,11 +163,16 @@ extern "C" int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_contex
     return cuda_status(e, "cudaGetDevice");
   }
   c->chain_texels = althea_ibl_chain_texels(w, h);
-  c->irr_ws_bytes = irr_plan(w, h, c->irr_w, c->irr_h).workspace;
+  if (!precision) c->irr_ws_bytes = irr_plan(w, h, c->irr_w, c->irr_h).workspace;
   e = cudaMalloc(&c->chain, c->chain_texels * 16);
-  if (e == cudaSuccess) e = cudaMalloc(&c->irr_ws, c->irr_ws_bytes);
+  if (e == cudaSuccess && c->irr_ws_bytes) e = cudaMalloc(&c->irr_ws, c->irr_ws_bytes);
+  if (e == cudaSuccess && c->tc_ws_bytes) e = cudaMalloc(&c->tc_ws, c->tc_ws_bytes);
+  if (e == cudaSuccess) e = make_side_streams(c);
   if (e != cudaSuccess) {
     if (c->chain) cudaFree(c->chain);
+    if (c->irr_ws) cudaFree(c->irr_ws);
+    if (c->tc_ws) cudaFree(c->tc_ws);
+    free_side_streams(c);
     delete c;
     return cuda_status(e, "context allocation");
   }
@@ -122,7 +195,9 @@ static int check_device(const althea_ibl_context* c) {
 extern "C" int althea_ibl_destroy(althea_ibl_context* c) {
   if (!c) return ALTHEA_IBL_OK;
   cudaFree(c->chain);
-  cudaFree(c->irr_ws);
+  if (c->irr_ws) cudaFree(c->irr_ws);
+  if (c->tc_ws) cudaFree(c->tc_ws);
+  free_side_streams(c);
   delete c;
   return ALTHEA_IBL_OK;
 }
@@ -171,17 +246,16 @@ extern "C" int althea_ibl_bake(althea_ibl_context* c, const althea_ibl_outputs* 
   if (r) return r;
   cudaStream_t st = (cudaStream_t)stream;
   const int w = c->cfg.env_width, h = c->cfg.env_height;
-  r = check_image(o->irradiance_dev, c->irr_w, c->irr_h, o->irradiance_pitch_bytes, 16,
+  const size_t texel = c->cfg.out_format == ALTHEA_IBL_FORMAT_RGBA16F ? 8 : 16;
+  r = check_image(o->irradiance_dev, c->irr_w, c->irr_h, o->irradiance_pitch_bytes, texel,
                   "irradiance");
   if (r) return r;
   althea_ibl_mip_target mips[ALTHEA_IBL_MAX_MIPS];
+  mip_targets(c, mips);
   for (int m = 0; m < c->cfg.mip_count; ++m) {
     mips[m].out_dev = o->mip_dev[m];
     mips[m].pitch_bytes = o->mip_pitch_bytes[m];
-    mips[m].width = c->mip_w[m];
-    mips[m].height = c->mip_h[m];
-    mips[m].roughness = c->mip_r[m];
-    r = check_image(mips[m].out_dev, mips[m].width, mips[m].height, mips[m].pitch_bytes, 16,
+    r = check_image(mips[m].out_dev, mips[m].width, mips[m].height, mips[m].pitch_bytes, texel,
                     "prefiltered mip");
     if (r) return r;
   }
@@ -189,16 +263,56 @@ extern "C" int althea_ibl_bake(althea_ibl_context* c, const althea_ibl_outputs* 
     r = check_image(o->lut_dev, c->cfg.lut_size, c->cfg.lut_size, o->lut_pitch_bytes, 8, "lut");
     if (r) return r;
   }
-  // Src/ImageBasedLighting.cpp:315-343: irradiance dispatch; :353-395: one
-  // prefilter dispatch per mip (here one launch for the whole chain).
-  r = launch_prefilter(c->chain, w, h, mips, c->cfg.mip_count, c->cfg.samples,
-                       c->cfg.generator, st);
-  if (r) return r;
-  r = launch_irradiance(c->chain, w, h, o->irradiance_dev, c->irr_w, c->irr_h,
-                        o->irradiance_pitch_bytes, c->irr_ws, st);
-  if (r) return r;
+  // The LUT does not depend on the env map: on the precision path it runs on
+  // a side stream, beside the tensor-bound contractions, and is joined below.
+  const bool precision = c->cfg.path == ALTHEA_IBL_PATH_PRECISION;
+  const bool lut_side = precision && c->cfg.lut_size > 0;
+  if (lut_side) {
+    cudaError_t e = cudaEventRecord(c->lut_fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->lut_stream, c->lut_fork, 0);
+    if (e != cudaSuccess) return cuda_status(e, "LUT side-stream fork");
+    r = launch_brdf_lut(o->lut_dev, c->cfg.lut_size, o->lut_pitch_bytes, c->cfg.lut_samples,
+                        c->cfg.lut_orientation, c->lut_stream);
+    if (r) return r;
+    e = cudaEventRecord(c->lut_join, c->lut_stream);
+    if (e != cudaSuccess) return cuda_status(e, "LUT side-stream record");
+  }
+  if (precision) {
+    // the planner's source levels (-1), the workspace sized at create
+    const SideStream side{c->narrow_stream, c->narrow_fork, c->narrow_join};
+    r = tc_bake(c->chain, w, h, mips, c->cfg.mip_count, nullptr, o->irradiance_dev, c->irr_w,
+                c->irr_h, o->irradiance_pitch_bytes, -1, c->tc_ws, c->tc_ws_bytes,
+                c->cfg.out_format, st, &side);
+    if (lut_side) {  // join even when the bake failed, so no fork is left open
+      const cudaError_t e = cudaStreamWaitEvent(st, c->lut_join, 0);
+      if (!r && e != cudaSuccess) r = cuda_status(e, "LUT side-stream join");
+    }
+    return r;
+  } else {
+    // Src/ImageBasedLighting.cpp:315-343: irradiance dispatch; :353-395: one
+    // prefilter dispatch per mip (here one launch for the whole chain).
+    r = launch_prefilter(c->chain, w, h, mips, c->cfg.mip_count, c->cfg.samples,
+                         c->cfg.generator, st);
+    if (r) return r;
+    r = launch_irradiance(c->chain, w, h, o->irradiance_dev, c->irr_w, c->irr_h,
+                          o->irradiance_pitch_bytes, c->irr_ws, st);
+    if (r) return r;
+  }
   if (c->cfg.lut_size > 0)
     r = launch_brdf_lut(o->lut_dev, c->cfg.lut_size, o->lut_pitch_bytes, c->cfg.lut_samples,
                         c->cfg.lut_orientation, st);
   return r;
+}
+
+extern "C" int althea_ibl_bake_status(const althea_ibl_context* c, void* stream) {
+  if (!c) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null context");
+  int r = check_device(c);
+  if (r) return r;
+  if (c->cfg.path == ALTHEA_IBL_PATH_PRECISION) return althea_ibl_tc_error(c->tc_ws, stream);
+  return cuda_status(cudaStreamSynchronize((cudaStream_t)stream), "bake status");
+}
+
+extern "C" size_t althea_ibl_context_device_bytes(const althea_ibl_context* c) {
+  if (!c) return 0;
+  return c->chain_texels * 16 + c->irr_ws_bytes + c->tc_ws_bytes;
 }

@@ -38,15 +38,29 @@ int launch_irradiance(const float* chain, int w, int h, float* out, int ow, int 
 int launch_delta_mip(const float* chain, int w, int h, const althea_ibl_mip_target* mip,
                      int out_half, cudaStream_t st);
 
+// A second stream for work that does not feed the tensor-core contractions
+// (the outputs summed on the CUDA cores): forked from the bake's stream after
+// the direction tables with `fork`, joined back with `join` before the bake
+// returns, so the CUDA-core kernels can share SMs with the tensor-bound ones.
+struct SideStream {
+  cudaStream_t stream;
+  cudaEvent_t fork, join;
+};
+
 // Precision path (ibl_tc.cu): the bake behind althea_ibl_bake_tc_ex, and its
-// workspace size (0 when the plan is unsupported).
+// workspace size (0 when the plan is unsupported).  side may be null (one
+// stream).
 int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
             const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
-            int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream);
+            int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream,
+            const SideStream* side = nullptr);
 size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n,
                           const int* levels, int irr_w, int irr_h, int irr_level);
 int launch_brdf_lut(float* out, int n, size_t pitch_bytes, int samples, int orientation,
                     cudaStream_t st);
+// Sun lobes added to an env level 0 (ibl_suns.cu); out may equal base.
+int launch_apply_suns(const float* base, float* out, int w, int h, const althea_ibl_sun* suns,
+                      int n, cudaStream_t st);
 // Reflection-buffer convolution (ibl_ssr.cu): levels 1..mips-1 from level 0.
 int ssr_convolve(void* const* levels, const size_t* pitch_bytes, int w, int h, int mips,
                  cudaStream_t st);

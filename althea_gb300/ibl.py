@@ -53,7 +53,7 @@ class Config(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in (
         "env_width", "env_height", "irradiance_width", "irradiance_height", "mip_count",
         "first_mip_width", "first_mip_height", "samples", "generator", "lut_size", "lut_samples",
-        "lut_orientation")]
+        "lut_orientation", "path", "out_format")]
 
 
 class Outputs(ctypes.Structure):
@@ -104,11 +104,20 @@ class ServerConfig(ctypes.Structure):
                 ("path", ctypes.c_int)]
 
 
+MAX_SUNS = 16
+
+
+class Sun(ctypes.Structure):
+    _fields_ = [("dir", ctypes.c_float * 3), ("sigma", ctypes.c_float),
+                ("radiance", ctypes.c_float)]
+
+
 class Request(ctypes.Structure):
     _fields_ = [("env_host", ctypes.c_void_p), ("env_width", ctypes.c_int),
                 ("env_height", ctypes.c_int), ("mip_count", ctypes.c_int),
                 ("irradiance_host", ctypes.c_void_p), ("mips_host", ctypes.c_void_p),
-                ("tag", ctypes.c_uint64)]
+                ("tag", ctypes.c_uint64), ("env_id", ctypes.c_int), ("sun_count", ctypes.c_int),
+                ("suns", Sun * MAX_SUNS)]
 
 
 class Completion(ctypes.Structure):
@@ -120,7 +129,8 @@ class ServerStats(ctypes.Structure):
     _fields_ = [("inflight", ctypes.c_int), ("queued", ctypes.c_int),
                 ("bytes_in_use", ctypes.c_size_t), ("bytes_reserved", ctypes.c_size_t),
                 ("peak_bytes_in_use", ctypes.c_size_t), ("completed", ctypes.c_uint64),
-                ("rejected", ctypes.c_uint64)]
+                ("rejected", ctypes.c_uint64), ("bytes_resident", ctypes.c_size_t),
+                ("resident_maps", ctypes.c_int)]
 
 _lib = None
 
@@ -161,6 +171,9 @@ def load(build_if_missing: bool = True):
         "althea_ibl_upload_env": (i, [vp, vp, i, vp]),
         "althea_ibl_env_chain": (vp, [vp]),
         "althea_ibl_bake": (i, [vp, ctypes.POINTER(Outputs), vp]),
+        "althea_ibl_bake_status": (i, [vp, vp]),
+        "althea_ibl_context_device_bytes": (sz, [vp]),
+        "althea_ibl_irradiance_noalloc": (i, [vp, i, i, vp, i, i, sz, vp]),
         "althea_ibl_batch_create": (i, [ctypes.POINTER(Probe), i, ctypes.POINTER(BatchParams), vp,
                                         ctypes.POINTER(vp)]),
         "althea_ibl_batch_run": (i, [vp, vp]),
@@ -172,6 +185,9 @@ def load(build_if_missing: bool = True):
         "althea_ibl_server_get_stats": (i, [vp, ctypes.POINTER(ServerStats)]),
         "althea_ibl_server_request_bytes": (sz, [vp, i, i, i]),
         "althea_ibl_server_now": (ctypes.c_double, []),
+        "althea_ibl_server_register_env": (i, [vp, vp, i, i, i, ctypes.POINTER(i)]),
+        "althea_ibl_server_unregister_env": (i, [vp, i]),
+        "althea_ibl_apply_suns": (i, [vp, vp, i, i, ctypes.POINTER(Sun), i, vp]),
         "althea_ibl_server_destroy": (i, [vp]),
         "althea_ibl_tc_workspace_size": (sz, [i, i, ctypes.POINTER(MipTarget), i,
                                               ctypes.POINTER(i), i, i, i]),
@@ -357,8 +373,14 @@ def reference_config(env_width: int, env_height: int) -> Config:
 
 def make_config(env_width, env_height, irradiance_size=None, mip_count=5, first_mip=None,
                 samples=10000, generator=GEN_REF_HASH, lut_size=0, lut_samples=1024,
-                lut_orientation=LUT_ASSET) -> Config:
+                lut_orientation=LUT_ASSET, path=PATH_PLAIN, out_format=FORMAT_RGBA32F) -> Config:
+    """The reference's settings for this env size with the given overrides.
+    path: PATH_PLAIN (the reference estimator) or PATH_PRECISION (the
+    tensor-core contraction within 1e-3 of FP64); out_format: FORMAT_RGBA32F
+    or, on the precision path, FORMAT_RGBA16F for the mips and irradiance."""
     cfg = reference_config(env_width, env_height)
+    cfg.path = path
+    cfg.out_format = out_format
     if irradiance_size is not None:
         cfg.irradiance_width, cfg.irradiance_height = irradiance_size
     cfg.mip_count = mip_count
@@ -455,24 +477,41 @@ class BakeContext:
         n = chain_texels(self.cfg.env_width, self.cfg.env_height)
         return _device_view(ptr, n * 4).view(n, 4)
 
+    def _out_dtype(self):
+        torch = _torch()
+        return torch.float16 if self.cfg.out_format == FORMAT_RGBA16F else torch.float32
+
+    def device_bytes(self) -> int:
+        """Device memory the context holds: the resident chain and its workspaces."""
+        return load().althea_ibl_context_device_bytes(self._ctx)
+
     def allocate_outputs(self, device="cuda"):
         torch = _torch()
+        dt = self._out_dtype()
         iw, ih = self.irradiance_size()
-        irr = torch.empty((ih, iw, 4), dtype=torch.float32, device=device)
+        irr = torch.empty((ih, iw, 4), dtype=dt, device=device)
         mips = []
         for m in range(self.cfg.mip_count):
             w, h, _ = self.mip_info(m)
-            mips.append(torch.empty((h, w, 4), dtype=torch.float32, device=device))
+            mips.append(torch.empty((h, w, 4), dtype=dt, device=device))
         lut = None
         if self.cfg.lut_size > 0:
             n = self.cfg.lut_size
             lut = torch.empty((n, n, 2), dtype=torch.float32, device=device)
         return irr, mips, lut
 
-    def bake(self, irr, mips, lut=None, stream=None):
-        """Bakes into caller tensors of exactly the context's sizes (as
-        allocate_outputs makes them): irradiance (ih, iw, 4), one (h_m, w_m, 4)
-        tensor per mip and, when the config has a LUT, (n, n, 2)."""
+    def bake(self, irr, mips, lut=None, stream=None, check: bool = False):
+        """Bakes into caller tensors of exactly the context's sizes and format
+        (as allocate_outputs makes them): irradiance (ih, iw, 4), one
+        (h_m, w_m, 4) tensor per mip -- float32, or float16 for an RGBA16F
+        config -- and, when the config has a LUT, (n, n, 2) float32.
+        check: synchronise and raise if a precision bake's bounded waits gave up."""
+        torch = _torch()
+        dt = self._out_dtype()
+        for k, t in enumerate([irr] + list(mips)):
+            if isinstance(t, torch.Tensor) and t.dtype != dt:
+                raise IBLError(ERR_INVALID_ARGUMENT,
+                               f"output {k} is {t.dtype}; this context writes {dt}")
         iw, ih = self.irradiance_size()
         _require_shape(irr, "irradiance", (ih, iw, 4))
         if len(mips) != self.cfg.mip_count:
@@ -487,18 +526,27 @@ class BakeContext:
                 raise IBLError(ERR_INVALID_ARGUMENT, f"this context bakes a {n}x{n} LUT: pass one")
             _require_shape(lut, "lut", (n, n, 2))
         o = Outputs()
-        _require_cuda(irr, "irradiance", 4)
+        half = dt == torch.float16
+        _require_cuda(irr, "irradiance", 4, allow_half=half)
         o.irradiance_dev = irr.data_ptr()
         o.irradiance_pitch_bytes = _pitch(irr, 4)
         for m, t in enumerate(mips):
-            _require_cuda(t, f"mip {m}", 4)
+            _require_cuda(t, f"mip {m}", 4, allow_half=half)
             o.mip_dev[m] = t.data_ptr()
             o.mip_pitch_bytes[m] = _pitch(t, 4)
         if lut is not None and self.cfg.lut_size > 0:
             _require_cuda(lut, "lut", 2)
             o.lut_dev = lut.data_ptr()
             o.lut_pitch_bytes = _pitch(lut, 2)
-        _check(load().althea_ibl_bake(self._ctx, ctypes.byref(o), _stream_ptr(stream)))
+        sp = _stream_ptr(stream)
+        _check(load().althea_ibl_bake(self._ctx, ctypes.byref(o), sp))
+        if check:
+            self.status(stream)
+
+    def status(self, stream=None) -> None:
+        """Synchronises the stream; raises IBLError if a precision bake's
+        kernels gave up on a bounded wait."""
+        _check(load().althea_ibl_bake_status(self._ctx, _stream_ptr(stream)))
 
 
 def _device_view(ptr: int, nfloats: int):
@@ -517,14 +565,18 @@ class ImageBasedLighting:
     @staticmethod
     def createResources(env, cfg: Optional[Config] = None, stream=None) -> IBLResources:
         """env: (H, W, 4) float32 (host or CUDA).  Bakes irradiance, the
-        prefiltered chain and (when cfg.lut_size > 0) the BRDF LUT."""
+        prefiltered chain and (when cfg.lut_size > 0) the BRDF LUT, on the
+        path and in the output format cfg names (default: the reference's
+        estimator, RGBA32F)."""
         h, w = int(env.shape[0]), int(env.shape[1])
         cfg = cfg or reference_config(w, h)
         ctx = BakeContext(cfg)
         try:
             ctx.upload_env(env, stream)
             irr, mips, lut = ctx.allocate_outputs()
-            ctx.bake(irr, mips, lut, stream)
+            # synchronous like the reference's bake (vkQueueWaitIdle), and
+            # checked: a precision bake that gave up raises here
+            ctx.bake(irr, mips, lut, stream, check=True)
             env_dev = chain_level(ctx.chain(), w, h, 0).clone()
         finally:
             ctx.close()
@@ -535,6 +587,40 @@ class ImageBasedLighting:
     def buildLayout() -> List[str]:
         # Src/ImageBasedLighting.cpp:607-619: four texture bindings.
         return ["environmentMap", "prefilteredMap", "irradianceMap", "brdfLut"]
+
+
+# ---- analytic sun lobes ---------------------------------------------------------
+
+def make_suns(suns) -> tuple:
+    """[(direction (3,), sigma rad, radiance), ...] -> (ctypes Sun array, count)."""
+    n = len(suns)
+    if n > MAX_SUNS:
+        raise IBLError(ERR_INVALID_ARGUMENT, f"{n} suns; at most {MAX_SUNS}")
+    arr = (Sun * MAX_SUNS)()
+    for k, (d, sigma, lum) in enumerate(suns):
+        arr[k].dir[0], arr[k].dir[1], arr[k].dir[2] = (float(d[0]), float(d[1]), float(d[2]))
+        arr[k].sigma, arr[k].radiance = float(sigma), float(lum)
+    return arr, n
+
+
+def apply_suns(base, suns, out=None, stream=None):
+    """out = base + the suns' Gaussian lobes on R, G, B (CUDA (H, W, 4) float32;
+    out may be base).  suns: [(direction, sigma in radians, radiance), ...]."""
+    torch = _torch()
+    _require_cuda(base, "base", 4)
+    if not base.is_contiguous():
+        raise IBLError(ERR_INVALID_ARGUMENT, "base must be contiguous")
+    if out is None:
+        out = torch.empty_like(base)
+    _require_cuda(out, "out", 4)
+    _require_shape(out, "out", tuple(base.shape))
+    if not out.is_contiguous():
+        raise IBLError(ERR_INVALID_ARGUMENT, "out must be contiguous")
+    arr, n = make_suns(suns)
+    h, w = base.shape[:2]
+    _check(load().althea_ibl_apply_suns(base.data_ptr(), out.data_ptr(), w, h, arr, n,
+                                        _stream_ptr(stream)))
+    return out
 
 
 # ---- batches -------------------------------------------------------------------

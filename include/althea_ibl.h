@@ -31,9 +31,22 @@
 extern "C" {
 #endif
 
-#define ALTHEA_IBL_ABI_VERSION 1
+#define ALTHEA_IBL_ABI_VERSION 2   /* 2: config path/out_format, resident server maps, suns */
 #define ALTHEA_IBL_MAX_LEVELS 16   /* env maps up to 32768 wide */
 #define ALTHEA_IBL_MAX_MIPS 16     /* prefiltered chain length */
+
+/* Bake path: the reference estimator (PreFilterEnvMap.comp /
+ * GenIrradianceMap.comp, bit for bit) or the quadrature it estimates as a
+ * tensor-core contraction within 1e-3 of FP64 (the precision path below). */
+#define ALTHEA_IBL_PATH_PLAIN 0       /* the reference estimator */
+#define ALTHEA_IBL_PATH_PRECISION 1   /* tensor-core contraction, <= 1e-3 vs FP64 */
+
+/* Output formats of the prefiltered mips and the irradiance (the precision
+ * path writes either; the plain path writes RGBA32F, the reference's format,
+ * Src/ImageBasedLighting.cpp:156-166,192-221). */
+#define ALTHEA_IBL_FORMAT_RGBA32F 0   /* 16-byte texels (VK_FORMAT_R32G32B32A32_SFLOAT) */
+#define ALTHEA_IBL_FORMAT_RGBA16F 1   /* 8-byte texels (IEEE half), alpha 1
+                                         (VK_FORMAT_R16G16B16A16_SFLOAT) */
 
 typedef enum {
   ALTHEA_IBL_OK = 0,
@@ -107,14 +120,18 @@ int althea_ibl_irradiance(const float* chain_dev, int env_width, int env_height,
  * frame or real-time callback where an allocation may stall the device).
  * Same kernels and results as althea_ibl_irradiance, but the partial sums
  * live in a fixed array of ALTHEA_IBL_NOALLOC_SCRATCH_BYTES inside the
- * library, held on every device that loads the library until exit; the call
- * allocates nothing.  Outputs whose partial sums do not fit (above about
- * 260,000 texels: 512 x 256 fits, 1024 x 512 does not) are rejected with
- * ALTHEA_IBL_ERR_UNSUPPORTED.
- * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  All calls share the array: calls whose kernels overlap on the GPU
- * race and must be serialised by the caller. */
+ * library; the call allocates nothing.  Outputs whose partial sums do not fit
+ * are rejected with ALTHEA_IBL_ERR_UNSUPPORTED: up to 262,144 output texels
+ * (512 x 512, or 512 x 256) fit, 262,145 and more (1024 x 512) do not.
+ * The array is device memory of the CUDA context current at the call, held
+ * until that context is destroyed or the process exits.  With lazy module
+ * loading (the CUDA default) it is committed by the first call in each
+ * context, and that first call also looks up the array's device address
+ * (once per context, cached under the context's id): make one warm-up call
+ * outside any frame loop and before any stream capture.  All calls in a
+ * context share the array: calls whose kernels overlap on the GPU (other
+ * streams, other host threads) race on it and must be serialised by the
+ * caller; the batch and server calls never use it. */
 #define ALTHEA_IBL_NOALLOC_SCRATCH_BYTES (4 * 1024 * 1024)
 int althea_ibl_irradiance_noalloc(const float* chain_dev, int env_width, int env_height,
                                   float* out_dev, int out_width, int out_height,
@@ -141,6 +158,9 @@ typedef struct {
   int lut_size;                   /* 0 = no LUT */
   int lut_samples;
   int lut_orientation;            /* althea_ibl_lut_orientation */
+  int path;                       /* ALTHEA_IBL_PATH_* (reference: PLAIN) */
+  int out_format;                 /* ALTHEA_IBL_FORMAT_* of the mips and the irradiance
+                                     (reference: RGBA32F; RGBA16F needs PATH_PRECISION) */
 } althea_ibl_config;
 
 /* Fills the reference's own settings for an env map of the given size. */
@@ -156,7 +176,9 @@ typedef struct {
 } althea_ibl_outputs;
 
 /* The context's device memory lives on the device current at create;
- * upload_env and bake refuse to run while another device is current. */
+ * upload_env and bake refuse to run while another device is current.
+ * create refuses (ALTHEA_IBL_ERR_UNSUPPORTED) a precision config the planner
+ * cannot run and RGBA16F outputs on the plain path. */
 int althea_ibl_create(const althea_ibl_config* cfg, althea_ibl_context** out);
 int althea_ibl_destroy(althea_ibl_context* ctx);
 /* Mip m size and roughness as the context bakes them. */
@@ -170,8 +192,21 @@ int althea_ibl_upload_env(althea_ibl_context* ctx, const float* rgba, int src_is
 /* Resident chain (device), for callers that bind the env map itself. */
 const float* althea_ibl_env_chain(const althea_ibl_context* ctx);
 /* Irradiance + every prefiltered mip (+ LUT when configured) into caller
- * buffers: the dispatch sequence of Src/ImageBasedLighting.cpp:315-402. */
+ * buffers: the dispatch sequence of Src/ImageBasedLighting.cpp:315-402.
+ * With path = ALTHEA_IBL_PATH_PRECISION the context plans the contraction
+ * (althea_ibl_tc_plan's source levels) and holds its workspace, sized at
+ * create; the mips and the irradiance are then written in cfg.out_format
+ * (the althea_ibl_outputs pointers point to texels of that format, pitches
+ * in bytes).  The LUT is RG32F on both paths. */
 int althea_ibl_bake(althea_ibl_context* ctx, const althea_ibl_outputs* outs, void* stream);
+/* Synchronises the stream, then reports a precision bake whose kernels gave
+ * up on a bounded wait (ALTHEA_IBL_ERR_CUDA); ALTHEA_IBL_OK otherwise and on
+ * the plain path.  Replaces the reference's blocking vkQueueWaitIdle
+ * (Src/SingleTimeCommandBuffer.cpp:28-54) for callers that want the result
+ * checked. */
+int althea_ibl_bake_status(const althea_ibl_context* ctx, void* stream);
+/* Device bytes the context holds (chain + workspaces), as allocated at create. */
+size_t althea_ibl_context_device_bytes(const althea_ibl_context* ctx);
 
 /* ---- precision path: dense contraction on the tensor cores -------------------
  * Replaces the two estimators of Shaders/IBL_Precompute (GenIrradianceMap.comp,
@@ -209,12 +244,10 @@ int althea_ibl_tc_error(const void* workspace_dev, void* stream);
  * Synchronises the stream. */
 int althea_ibl_tc_wait_selftest(unsigned long long limit_ns, int* waited_ms, void* stream);
 
-/* Output formats of althea_ibl_bake_tc_ex (every mip and the irradiance). */
-#define ALTHEA_IBL_FORMAT_RGBA32F 0   /* 16-byte texels, as althea_ibl_bake_tc */
-#define ALTHEA_IBL_FORMAT_RGBA16F 1   /* 8-byte texels (IEEE half), alpha 1 */
-/* althea_ibl_bake_tc with the output format chosen: the images the renderer
- * binds as VK_FORMAT_R16G16B16A16_SFLOAT (the mips' out_dev and
- * irradiance_dev then point to RGBA16F texels; pitches in bytes). */
+/* althea_ibl_bake_tc with the output format chosen (ALTHEA_IBL_FORMAT_*):
+ * with RGBA16F, the images the renderer binds as
+ * VK_FORMAT_R16G16B16A16_SFLOAT (the mips' out_dev and irradiance_dev then
+ * point to RGBA16F texels; pitches in bytes). */
 int althea_ibl_bake_tc_ex(const float* chain_dev, int env_width, int env_height,
                           const althea_ibl_mip_target* mips, int mip_count, const int* levels,
                           void* irradiance_dev, int irradiance_width, int irradiance_height,
@@ -287,6 +320,25 @@ int althea_ibl_batch_run(althea_ibl_batch* batch, void* stream);
 int althea_ibl_batch_describe(const althea_ibl_batch* batch, althea_ibl_batch_info* info);
 int althea_ibl_batch_destroy(althea_ibl_batch* batch);
 
+/* ---- analytic sun lobes ---------------------------------------------------------
+ * No counterpart in the reference, whose env maps are fixed files
+ * (Src/ImageBasedLighting.cpp:429-446).  A probe is usually re-baked because
+ * its lights changed (the sun moved with the time of day), not its whole sky:
+ * these calls add Gaussian sun lobes to a sky map on the device,
+ *   out = base + sum_s radiance_s exp(-theta_s^2 / (2 sigma_s^2))  on R, G, B,
+ * theta_s = angle between a texel centre's direction and dir_s, with the
+ * texel directions of sampleEnvMap (PreFilterEnvMap.comp:98-122); alpha is
+ * copied.  The server applies a request's suns to a resident map before its
+ * bake.  out_dev may equal base_dev (RGBA32F, width x height, tightly packed). */
+#define ALTHEA_IBL_MAX_SUNS 16
+typedef struct {
+  float dir[3];              /* direction (x, y, z); normalised by the call */
+  float sigma;               /* angular width in radians, 0 < sigma < 4 */
+  float radiance;            /* peak radiance added to R, G and B, >= 0 */
+} althea_ibl_sun;
+int althea_ibl_apply_suns(const float* base_dev, float* out_dev, int width, int height,
+                          const althea_ibl_sun* suns, int sun_count, void* stream);
+
 /* ---- serving: continuous re-bakes under an HBM budget -------------------------
  * No counterpart in the reference (one synchronous bake at start-up,
  * Src/GlobalResources.cpp:18-22).  A server admits probe re-bake requests as
@@ -297,9 +349,6 @@ int althea_ibl_batch_destroy(althea_ibl_batch* batch);
  * cudaFree on the request path).  Results are identical whether a request runs
  * alone or among others (the kernels are deterministic and independent of
  * concurrency).  The API is single-threaded: call submit/poll from one thread. */
-#define ALTHEA_IBL_PATH_PLAIN 0       /* the reference estimator */
-#define ALTHEA_IBL_PATH_PRECISION 1   /* tensor-core contraction, <= 1e-3 vs FP64 */
-
 typedef struct {
   size_t budget_bytes;       /* device memory the server may hold */
   int max_inflight;          /* requests on the GPU at once (streams) */
@@ -310,12 +359,17 @@ typedef struct {
 } althea_ibl_server_config;
 
 typedef struct {
-  const float* env_host;     /* RGBA32F level 0, host memory (pinned for overlap) */
-  int env_width, env_height;
+  const float* env_host;     /* RGBA32F level 0, host memory (pinned for overlap);
+                                unused (may be NULL) when env_id names a resident map */
+  int env_width, env_height; /* with env_id: the registered map's size */
   int mip_count;             /* mips from W/2 x H/2, roughness m/(M-1) */
   float* irradiance_host;    /* irradiance_width*height*4 floats, or NULL */
   float* mips_host;          /* every mip back to back (sum of w*h*4 floats) */
   uint64_t tag;
+  int env_id;                /* 0: upload env_host; else an id from
+                                althea_ibl_server_register_env (the map stays on the device) */
+  int sun_count;             /* suns added to the map before the bake, 0..ALTHEA_IBL_MAX_SUNS */
+  althea_ibl_sun suns[ALTHEA_IBL_MAX_SUNS];
 } althea_ibl_request;
 
 typedef struct {
@@ -328,6 +382,8 @@ typedef struct {
   int inflight, queued;
   size_t bytes_in_use, bytes_reserved, peak_bytes_in_use;
   uint64_t completed, rejected;
+  size_t bytes_resident;     /* registered env maps */
+  int resident_maps;
 } althea_ibl_server_stats;
 
 typedef struct althea_ibl_server althea_ibl_server;
@@ -342,6 +398,17 @@ int althea_ibl_server_submit(althea_ibl_server* s, const althea_ibl_request* req
  * slots and memory, and admits queued requests that now fit. */
 int althea_ibl_server_poll(althea_ibl_server* s, althea_ibl_completion* out, int max, int* n);
 int althea_ibl_server_get_stats(const althea_ibl_server* s, althea_ibl_server_stats* st);
+/* Resident env maps.  register uploads an RGBA32F level 0 (host memory, or
+ * device memory when src_is_device) once and keeps it on the device, counted
+ * against the budget, until unregister; requests then name it by env_id and
+ * move no env map across the host link (a re-bake of a known sky, with the
+ * request's suns added on the device).  register refuses a map that does not
+ * fit the budget beside what the server already holds (ALTHEA_IBL_ERR_BUDGET);
+ * unregister refuses while queued or running requests use the map
+ * (ALTHEA_IBL_ERR_NOT_READY).  Synchronous (not on the request path). */
+int althea_ibl_server_register_env(althea_ibl_server* s, const float* rgba, int env_width,
+                                   int env_height, int src_is_device, int* env_id_out);
+int althea_ibl_server_unregister_env(althea_ibl_server* s, int env_id);
 /* Device memory a request of this size holds while in flight; 0 for a size
  * the server cannot run. */
 size_t althea_ibl_server_request_bytes(const althea_ibl_server* s, int env_width, int env_height,

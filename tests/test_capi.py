@@ -35,7 +35,7 @@ def test_chain_geometry():
                                                for l in range(13))
     assert ibl.chain_level_offset(4096, 2048, 1) == 4096 * 2048
     assert ibl.chain_levels(37, 19) == 6
-    assert ibl.load().althea_ibl_abi_version() == 1
+    assert ibl.load().althea_ibl_abi_version() == 2
 
 
 def test_reference_config_matches_reference_bake():
@@ -80,6 +80,44 @@ def test_argument_checks_without_gpu():
             ibl.ERR_INVALID_ARGUMENT, field
         assert what in L.althea_ibl_last_error() and not ctx.value
     assert L.althea_ibl_bake(None, None, None) == ibl.ERR_INVALID_ARGUMENT
+    assert L.althea_ibl_bake_status(None, None) == ibl.ERR_INVALID_ARGUMENT
+    assert L.althea_ibl_context_device_bytes(None) == 0
+
+
+def test_context_path_and_format_checks_without_gpu():
+    """The bake context's path and output format: values outside the enums
+    are invalid, RGBA16F is refused on the plain path, and a precision config
+    the planner cannot run is refused at create -- all before any device work."""
+    L = ibl.load()
+    ctx = ctypes.c_void_p()
+    ref = ibl.reference_config(4096, 2048)
+    assert (ref.path, ref.out_format) == (ibl.PATH_PLAIN, ibl.FORMAT_RGBA32F)
+    for field, value, status, what in (
+            ("path", 2, ibl.ERR_INVALID_ARGUMENT, b"path 2"),
+            ("out_format", 5, ibl.ERR_INVALID_ARGUMENT, b"out_format 5"),
+            ("out_format", ibl.FORMAT_RGBA16F, ibl.ERR_UNSUPPORTED, b"plain path")):
+        cfg = ibl.make_config(64, 32)
+        setattr(cfg, field, value)
+        assert L.althea_ibl_create(ctypes.byref(cfg), ctypes.byref(ctx)) == status, field
+        assert what in L.althea_ibl_last_error() and not ctx.value
+    # irradiance 100 wide does not divide its 2048-wide source level
+    cfg = ibl.make_config(4096, 2048, irradiance_size=(100, 50), mip_count=9,
+                          path=ibl.PATH_PRECISION, out_format=ibl.FORMAT_RGBA16F)
+    assert L.althea_ibl_create(ctypes.byref(cfg), ctypes.byref(ctx)) == ibl.ERR_UNSUPPORTED
+    assert b"precision path" in L.althea_ibl_last_error() and not ctx.value
+
+
+def test_noalloc_size_limit_without_gpu():
+    """The no-allocation irradiance holds 4 MiB of partial sums: 512 x 512
+    output texels (one 16-byte partial each) fit exactly, one texel more is
+    refused before any device work."""
+    L = ibl.load()
+    assert L.althea_ibl_irradiance_workspace_size(1024, 512, 512, 512) == 4 * 1024 * 1024
+    assert L.althea_ibl_irradiance_workspace_size(1024, 512, 545, 481) > 4 * 1024 * 1024
+    fake = 1 << 20  # aligned, never dereferenced: the size check answers first
+    assert L.althea_ibl_irradiance_noalloc(fake, 1024, 512, fake, 545, 481, 545 * 16, None) == \
+        ibl.ERR_UNSUPPORTED
+    assert b"no-allocation" in L.althea_ibl_last_error()
 
 
 def test_python_errors_carry_status():
@@ -161,6 +199,7 @@ _LAYOUTS = [
     (ibl.BatchParams, "althea_ibl_batch_params"), (ibl.BatchInfo, "althea_ibl_batch_info"),
     (ibl.ServerConfig, "althea_ibl_server_config"), (ibl.Request, "althea_ibl_request"),
     (ibl.Completion, "althea_ibl_completion"), (ibl.ServerStats, "althea_ibl_server_stats"),
+    (ibl.Sun, "althea_ibl_sun"),
 ]
 # Python constant -> C enum constant or macro
 _CONSTANTS = {
@@ -174,6 +213,7 @@ _CONSTANTS = {
     "BATCH_PRECISION": "ALTHEA_IBL_BATCH_PRECISION", "BATCH_HALF": "ALTHEA_IBL_BATCH_HALF",
     "PATH_PLAIN": "ALTHEA_IBL_PATH_PLAIN", "PATH_PRECISION": "ALTHEA_IBL_PATH_PRECISION",
     "FORMAT_RGBA32F": "ALTHEA_IBL_FORMAT_RGBA32F", "FORMAT_RGBA16F": "ALTHEA_IBL_FORMAT_RGBA16F",
+    "MAX_SUNS": "ALTHEA_IBL_MAX_SUNS",
 }
 
 

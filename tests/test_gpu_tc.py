@@ -203,3 +203,82 @@ def test_bounded_wait_gives_up_and_reports():
     assert 20 <= waited < 1000
     test_half_outputs_are_the_float_outputs_rounded()
 
+
+
+@pytest.mark.parametrize("fmt", [ibl.FORMAT_RGBA32F, ibl.FORMAT_RGBA16F])
+def test_context_precision_bake_equals_stateless_bake(fmt):
+    """The createResources mirror on the precision path: the bake context plans
+    the contraction and holds its workspace itself, and writes what the
+    stateless bake_tc writes with the planner's levels, bit for bit, in either
+    output format (RGBA16F = the RGBA32F result rounded)."""
+    w, h = 1024, 512
+    env = synth.make_env(w, h, seed=4, sun_max=1e6)
+    env_d = torch.from_numpy(env).cuda()
+    cfg = ibl.make_config(w, h, irradiance_size=(32, 16), mip_count=7, lut_size=64,
+                          lut_samples=64, path=ibl.PATH_PRECISION, out_format=fmt)
+    ctx = ibl.BakeContext(cfg)
+    assert ctx.device_bytes() > ibl.chain_texels(w, h) * 16
+    ctx.upload_env(env_d)
+    irr, mips, lut = ctx.allocate_outputs()
+    want = torch.float16 if fmt == ibl.FORMAT_RGBA16F else torch.float32
+    assert irr.dtype == want and all(m.dtype == want for m in mips)
+    ctx.bake(irr, mips, lut, check=True)
+    rough = [ctx.mip_info(m)[2] for m in range(7)]
+    chain = ibl.build_env_chain(env_d)
+    ref_mips = [torch.empty(m.shape, dtype=torch.float32, device="cuda") for m in mips]
+    ref_irr = torch.empty(irr.shape, dtype=torch.float32, device="cuda")
+    ibl.bake_tc(chain, w, h, ref_mips, rough, irradiance=ref_irr)
+    torch.cuda.synchronize()
+    assert torch.equal(ctx.chain(), chain)
+    for a, b in zip(mips, ref_mips):
+        assert torch.equal(a, b.to(want))
+    assert torch.equal(irr, ref_irr.to(want))
+    assert torch.equal(lut, ibl.brdf_lut(64, 64, ibl.LUT_ASSET))
+    with pytest.raises(ibl.IBLError):  # the other format is refused
+        other = torch.float32 if want == torch.float16 else torch.float16
+        ctx.bake(irr.to(other), [m.to(other) for m in mips], lut)
+    ctx.close()
+    res = ibl.ImageBasedLighting.createResources(env_d, cfg)
+    assert torch.equal(res.prefilteredMap[3], ref_mips[3].to(want))
+    assert torch.equal(res.irradianceMap, ref_irr.to(want))
+
+
+def test_two_product_split_on_low_roughness_planned_mips():
+    """With planner-chosen levels, GGX mips of roughness <= 0.2 take the
+    two-product split (BF16 hi weights, normalised by the sum of the rounded
+    weights); the same levels named by the caller take three products.  On a
+    2048x1024 probe with 1e6 suns: mip 1 (roughness 1/7) differs between the
+    two by the weight rounding only, both stay within 1e-3 of the FP64
+    quadrature over level 0, and every other output is bit-identical."""
+    spec = ibl.spec_for(2048, 1024)
+    w, h = 2048, 1024
+    env = synth.make_env(w, h, seed=3, sun_max=1e6)
+    chain = ibl.build_env_chain(torch.from_numpy(env).cuda())
+    levels, il = ibl.tc_plan(w, h, spec.mip_sizes, spec.roughness, 32)
+
+    def bake(lv, ilv):
+        outs = [torch.empty((mh, mw, 4), dtype=torch.float32, device="cuda")
+                for mw, mh in spec.mip_sizes]
+        irr = torch.empty((16, 32, 4), dtype=torch.float32, device="cuda")
+        ibl.bake_tc(chain, w, h, outs, spec.roughness, irradiance=irr, levels=lv,
+                    irradiance_level=ilv)
+        torch.cuda.synchronize()
+        return [o.cpu().numpy() for o in outs], irr.cpu().numpy()
+
+    two, irr_a = bake(None, -1)
+    three, irr_b = bake(levels, il)
+    assert np.array_equal(irr_a, irr_b)
+    rng = np.random.default_rng(5)
+    for m, r in enumerate(spec.roughness):
+        if r == 0.0 or r > 0.2:
+            assert np.array_equal(two[m], three[m]), m
+            continue
+        assert not np.array_equal(two[m], three[m])
+        d = np.abs(two[m][..., :3] - three[m][..., :3]) / np.abs(three[m][..., :3])
+        assert d.max() <= 1e-3, d.max()
+        mw, mh = spec.mip_sizes[m]
+        idx = rng.choice(mw * mh, size=192, replace=False)
+        xy = np.stack([idx % mw, idx // mw], 1).astype(np.int32)
+        ref = oracle.quad_prefilter(env, mw, mh, r, xy)[:, :3]
+        for img in (two[m], three[m]):
+            assert _rel(img[xy[:, 1], xy[:, 0], :3], ref).max() <= 1e-3
