@@ -237,6 +237,27 @@ __device__ __forceinline__ void mma_stage_ts(uint32_t d, uint32_t a, uint64_t bh
       : "memory");
 }
 
+// The same stage with the weights as BF16 hi only (two products per K = 16):
+//   D += Ahi*Bhi + Ahi*Blo  for K = 0..15 and 16..31.
+// The weight sum is then taken over the same rounded weights, so the
+// normalised result is an exact weighted average with BF16 weights.
+__device__ __forceinline__ void mma_stage_ts2(uint32_t d, uint32_t a, uint64_t bh, uint64_t bl,
+                                              uint64_t bh2, uint64_t bl2, uint32_t idesc,
+                                              uint32_t accumulate, uint64_t* bar) {
+  asm volatile(
+      "{\n .reg .pred p, t;\n .reg .b32 a8;\n"
+      " setp.ne.b32 p, %7, 0;\n setp.eq.b32 t, %7, %7;\n"
+      " add.u32 a8, %1, 8;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %6, p;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %3, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a8], %4, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a8], %5, %6, t;\n"
+      " tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%8];\n}\n" ::"r"(d),
+      "r"(a), "l"(bh), "l"(bl), "l"(bh2), "l"(bl2), "r"(idesc), "r"(accumulate),
+      "r"((uint32_t)__cvta_generic_to_shared(bar))
+      : "memory");
+}
+
 // Hardware reciprocal approximation (one MUFU operation, ~1 ulp).
 __device__ __forceinline__ float rcp_approx(float x) {
   float r;
@@ -307,6 +328,8 @@ struct Job {
   double* wsum_part;         // [ksplit][ho]  (kind 0)
   int* error;                // set when a bounded wait gave up
   int out_half;              // 1: outputs are RGBA16F (8-byte texels), else RGBA32F
+  int two_prod;              // 1: BF16 hi weights only (two products per channel), weight
+                             // sum over the rounded weights; 0: hi/lo weights (three)
   // A second output of the same geometry (same source level, phase count,
   // columns) in TMEM lanes 64-127, so that two outputs of <= 64 rows fill one
   // M = 128 tile: they share every radiance operand, only the weights differ.
@@ -338,7 +361,7 @@ __host__ __device__ inline SmemPlan smem_plan(const Job& J) {
 
 // The contraction kernel.  Grid: (ceil(ho/128), m * nblk, ksplit); each CTA
 // sums at most kMaxK of K in one TMEM accumulation chain per channel.
-template <int KIND>
+template <int KIND, bool TWO>
 __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t a_full[kStages], a_empty[kStages];
@@ -516,10 +539,14 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
               const __nv_bfloat162 h2 = __floats2bfloat162_rn(w[e].x, w[e].y);
-              const float2 lo = __ffma2_rn(__bfloat1622float2(h2), minus1, w[e]);
-              const __nv_bfloat162 l2 = __floats2bfloat162_rn(lo.x, lo.y);
               hw[e] = *reinterpret_cast<const uint32_t*>(&h2);
-              lw[e] = *reinterpret_cast<const uint32_t*>(&l2);
+              if (TWO) {
+                w[e] = __bfloat1622float2(h2);  // the weight the MMAs use
+              } else {
+                const float2 lo = __ffma2_rn(__bfloat1622float2(h2), minus1, w[e]);
+                const __nv_bfloat162 l2 = __floats2bfloat162_rn(lo.x, lo.y);
+                lw[e] = *reinterpret_cast<const uint32_t*>(&l2);
+              }
             }
             if (want)
               rowsum2 = __fadd2_rn(__fadd2_rn(rowsum2, w[0]), __fadd2_rn(__fadd2_rn(w[1], w[2]), w[3]));
@@ -540,7 +567,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
           if (live) {
             const uint32_t col = (uint32_t)(kACol + st * kKS + 4 * h);
             tmem_st4(lane_base + col, hw);
-            tmem_st4(lane_base + col + 16, lw);
+            if (!TWO) tmem_st4(lane_base + col + 16, lw);
           }
           if (kint) {
             // publish at once: the next stage this quarter owns is four away
@@ -595,8 +622,12 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
             }
             tc_fence_after();
             const uint32_t a_hi = tmem + (uint32_t)kACol + st * kKS;
-            mma_stage_ts(d, a_hi, dbh, dbh + r8, dbh + 2, dbh + 2 + r8, idesc, gidx != 0,
-                         &a_empty[st]);
+            if (TWO)
+              mma_stage_ts2(d, a_hi, dbh, dbh + r8, dbh + 2, dbh + 2 + r8, idesc, gidx != 0,
+                            &a_empty[st]);
+            else
+              mma_stage_ts(d, a_hi, dbh, dbh + r8, dbh + 2, dbh + 2 + r8, idesc, gidx != 0,
+                           &a_empty[st]);
             if (kc == kchunks - 1) mma_commit(&slot_empty[slot]);
           }
         }
@@ -1129,9 +1160,20 @@ int level_index(TcPlan& P, int w, int h, int level, int g, size_t& off) {
   return (int)P.levels.size() - 1;
 }
 
+// Glossy mips at most this rough, on a source level the planner chose, take
+// the two-product split (BF16 hi weights, the weight sum over the rounded
+// weights).  The rounding of the weights is then an error of its own, up to
+// 2^-9 per weight, correlated over a sun's texels: measured against the FP64
+// quadrature over level 0 on the 4096x2048 map with 1e6 suns (seeds 0-2,
+// every texel within 5 degrees of a sun, seams, poles and 512 random texels),
+// mip 1 (roughness 1/8 from a 1024-wide level) reaches 5.4e-4 with it against
+// 1.8e-4 without; the rougher mips already carry up to 7.6e-4 from their
+// source level and keep three products.
+constexpr float kTwoProdMaxRoughness = 0.2f;
+
 // Adds a contraction job (mip or irradiance) to the plan.
 int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, int level,
-            size_t& off) {
+            bool planned, size_t& off) {
   JobPlan jp;
   Job& J = jp.J;
   memset(&J, 0, sizeof(J));
@@ -1152,6 +1194,7 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   }
   J.kind = kind;
   J.a2 = roughness * roughness;
+  J.two_prod = planned && kind == 0 && roughness <= kTwoProdMaxRoughness ? 1 : 0;
   if (ow * oh <= kNarrowMax && ow <= kNarrowMaxW && 32 % ow == 0) {
     // CUDA-core job: one block per (output row, band of source rows), about
     // four blocks per SM
@@ -1247,8 +1290,8 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
       P.jobs.push_back(JobPlan{});
       continue;
     }
-    int lv = levels && levels[m] >= 0 ? levels[m]
-                                      : planned_level(w, mips[m].width, mips[m].roughness, false);
+    const bool planned = !(levels && levels[m] >= 0);
+    int lv = planned ? planned_level(w, mips[m].width, mips[m].roughness, false) : levels[m];
     if (lv >= nlevels)
       return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
                        "tensor path: mip %d source level %d; the chain has levels 0..%d", m, lv,
@@ -1259,7 +1302,8 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
       return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
                        "tensor path: mip %d (%dx%d) cannot contract against level %d", m,
                        mips[m].width, mips[m].height, lv);
-    int st = add_job(P, w, h, mips[m].width, mips[m].height, mips[m].roughness, 0, lv, off);
+    int st = add_job(P, w, h, mips[m].width, mips[m].height, mips[m].roughness, 0, lv, planned,
+                     off);
     if (st) return st;
   }
   if (irr_w > 0) {
@@ -1272,7 +1316,7 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
     if (ws < irr_w || ws % irr_w != 0 || irr_w > kMaxTcWidth)
       return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "tensor path: irradiance %dx%d vs level %d",
                        irr_w, irr_h, lv);
-    int st = add_job(P, w, h, irr_w, irr_h, 1.0f, 1, lv, off);
+    int st = add_job(P, w, h, irr_w, irr_h, 1.0f, 1, lv, irr_level < 0, off);
     if (st) return st;
   }
   // Pair tensor jobs of at most 64 rows that share every radiance operand
@@ -1289,7 +1333,7 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
       if (x.ws != y.ws || x.hs != y.hs || x.wo != y.wo || x.g != y.g || x.m != y.m ||
           x.krow != y.krow || x.kpad != y.kpad || x.nres != y.nres || x.nb != y.nb ||
           x.nblk != y.nblk || x.rlen != y.rlen || x.nslots != y.nslots ||
-          x.nsplit != y.nsplit || x.ksplit != y.ksplit)
+          x.nsplit != y.nsplit || x.ksplit != y.ksplit || x.two_prod != y.two_prod)
         continue;
       A.pair_with = (int)b;
       B.paired = true;
@@ -1333,7 +1377,8 @@ namespace ibl {
 
 int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
             const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
-            int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream) {
+            int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream,
+            const SideStream* side) {
   int st = check_env(w, h);
   if (st) return st;
   if (out_format != ALTHEA_IBL_FORMAT_RGBA32F && out_format != ALTHEA_IBL_FORMAT_RGBA16F)
@@ -1413,6 +1458,17 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     }
     if (nt > 0) tables_kernel<<<dim3((nmax + 31) / 32, nt), 32, 0, s>>>(ta);
   }
+  // The outputs summed on the CUDA cores go to the side stream when there is
+  // one (they need the tables, nothing else of the tensor path).
+  bool any_narrow = false;
+  for (const JobPlan& jp : P.jobs) any_narrow |= jp.narrow;
+  cudaStream_t ns = s;
+  if (side && any_narrow) {
+    e = cudaEventRecord(side->fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side->stream, side->fork, 0);
+    if (e != cudaSuccess) return cuda_status(e, "tc side-stream fork");
+    ns = side->stream;
+  }
   static_assert(sizeof(FinishArgs) <= 32000, "finish arguments fit the kernel parameter space");
   FinishArgs fa;
   memset(&fa, 0, sizeof(fa));
@@ -1451,16 +1507,16 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
         e = cudaFuncSetAttribute(narrow_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem);
         if (e != cudaSuccess) return cuda_status(e, "tc narrow smem attribute");
-        narrow_kernel<0><<<grid, kNarrowThreads, smem, s>>>(nj);
+        narrow_kernel<0><<<grid, kNarrowThreads, smem, ns>>>(nj);
       } else {
         e = cudaFuncSetAttribute(narrow_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem);
         if (e != cudaSuccess) return cuda_status(e, "tc narrow smem attribute");
-        narrow_kernel<1><<<grid, kNarrowThreads, smem, s>>>(nj);
+        narrow_kernel<1><<<grid, kNarrowThreads, smem, ns>>>(nj);
       }
       e = cudaGetLastError();
       if (e != cudaSuccess) return cuda_status(e, "tc narrow launch");
-      narrow_finish_kernel<<<J.wo * J.ho, 32, 0, s>>>(nj, J.kind, out, pitch, out_half);
+      narrow_finish_kernel<<<J.wo * J.ho, 32, 0, ns>>>(nj, J.kind, out, pitch, out_half);
       e = cudaGetLastError();
       if (e != cudaSuccess) return cuda_status(e, "tc narrow finish launch");
       continue;
@@ -1497,17 +1553,11 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     int smem = (int)smem_plan(J).total;
     if (smem < 120 * 1024) smem = 120 * 1024;
     dim3 grid((J.ho + kM - 1) / kM, J.m * J.nblk, J.ksplit);
-    if (J.kind == 0) {
-      e = cudaFuncSetAttribute(contract_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               smem);
-      if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
-      contract_kernel<0><<<grid, kThreads, smem, s>>>(J);
-    } else {
-      e = cudaFuncSetAttribute(contract_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               smem);
-      if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
-      contract_kernel<1><<<grid, kThreads, smem, s>>>(J);
-    }
+    auto kern = J.kind == 1 ? contract_kernel<1, false>
+                            : (J.two_prod ? contract_kernel<0, true> : contract_kernel<0, false>);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
+    kern<<<grid, kThreads, smem, s>>>(J);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "tc contraction launch");
   }
@@ -1522,6 +1572,11 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     if (P.jobs[m].level >= 0 || P.jobs[m].narrow) continue;
     st = launch_delta_mip(chain, w, h, &mips[m], out_half, s);
     if (st) return st;
+  }
+  if (ns != s) {  // join the side stream
+    e = cudaEventRecord(side->join, ns);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, side->join, 0);
+    if (e != cudaSuccess) return cuda_status(e, "tc side-stream join");
   }
   return cuda_status(cudaGetLastError(), "tensor path launch");
 }
