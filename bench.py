@@ -19,7 +19,7 @@ Hammersley) is timed on the same map in the same run.
             pair; the executed split-precision flops (2 x 9 per pair) beside.
 * cpu_baseline: the reference shaders compiled as C++ (oracle/_ref) -- or the
             C restatement when that library is absent -- on every host core,
-            over a bounded sample of texels per mip, extrapolated to a probe.
+            one whole probe (every texel, baked in row strata), timed.
 
 ``--path plain``: the plain production configuration (suns up to 1e4, the
 reference estimator bit-for-bit) with its HBM roofline.  ``--impl reference``
@@ -178,84 +178,157 @@ def dist_setup():
 # ----------------------------------------------------------------------------
 # CPU baseline (oracle/_ref = reference shaders as C++, else the C port)
 # ----------------------------------------------------------------------------
-def cpu_sample_probe_time(env, kind_pref="reference", scale=1.0):
-    """Times a bounded sample of a probe on all host cores; returns
-    (seconds per whole probe, kind, cores, sample description, seconds spent)."""
-    import oracle
-    use_ref = kind_pref == "reference" and oracle.ref_lib() is not None
-    kind = "reference" if use_ref else "port"
-    cores = os.cpu_count()
-    chain = oracle.ref_build_chain(env) if use_ref else oracle.build_chain(env)
-    rng = np.random.default_rng(123)
-    per_probe = 0.0
-    spent = 0.0
-    parts = []
-    for (ow, oh), r in zip(mip_sizes(), roughness()):
-        texels = ow * oh
-        k = min(texels, int((4096 if r > 0 else 8192) * scale))
-        idx = rng.choice(texels, size=k, replace=False)
-        xy = np.stack([idx % ow, idx // ow], 1).astype(np.int32)
+# A CPU step bakes one stratum of a probe: rows y = k, k + S, k + 2S, ... of
+# every prefilter mip and of the irradiance (stratum 0 also bakes the LUT), so
+# S consecutive strata bake every texel of the probe exactly once.  A probe's
+# CPU time is the sum of its S strata's measured times: nothing extrapolated.
+CPU_STRATA = 8
+
+
+class CpuProbe:
+    """The reference's CPU implementation of one probe bake on every host
+    core: the reference shaders compiled as C++ (oracle/_ref, kind
+    "reference"), or the C restatement when that library is absent ("port").
+    The LUT has no reference code; the C restatement (FP32) bakes it."""
+
+    def __init__(self, env, kind_pref="reference"):
+        import oracle
+        self.oracle = oracle
+        self.use_ref = kind_pref == "reference" and oracle.ref_lib() is not None
+        self.kind = "reference" if self.use_ref else "port"
+        self.cores = os.cpu_count()
+        self.chain = oracle.ref_build_chain(env) if self.use_ref else oracle.build_chain(env)
+
+    @staticmethod
+    def rows_xy(ow, oh, k, strata):
+        ys = np.arange(k, oh, strata)
+        if ys.size == 0:
+            return None
+        yy, xx = np.meshgrid(ys, np.arange(ow), indexing="ij")
+        return np.stack([xx.ravel(), yy.ravel()], 1).astype(np.int32)
+
+    def prefilter(self, ow, oh, r, xy):
+        """The listed texels of one mip, (n, 4)."""
+        o = self.oracle
+        if self.use_ref:
+            out = o.ref_prefilter(self.chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, GENERATOR,
+                                  xy=xy, nthreads=self.cores)
+            return out[xy[:, 1], xy[:, 0]]
+        return o.prefilter(self.chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, GENERATOR, xy=xy,
+                           nthreads=self.cores)
+
+    def irradiance(self, xy):
+        """The listed texels of the irradiance output, (n, 4)."""
+        o = self.oracle
+        if self.use_ref:
+            s = ENV_W // IRR_W  # the reference dispatches at env size: strided texels
+            out = o.ref_irradiance_envsize(self.chain, ENV_W, ENV_H, xy * s, nthreads=self.cores)
+            return out[xy[:, 1] * s, xy[:, 0] * s]
+        return o.irradiance(self.chain, ENV_W, ENV_H, IRR_W, IRR_H, xy=xy, nthreads=self.cores)
+
+    def stratum(self, k, strata):
+        """Bakes stratum k of `strata`; returns the seconds it took."""
         t0 = time.perf_counter()
-        if use_ref:
-            oracle.ref_prefilter(chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, GENERATOR,
-                                 xy=xy, nthreads=cores)
-        else:
-            oracle.prefilter(chain, ENV_W, ENV_H, ow, oh, r, SAMPLES, GENERATOR, xy=xy,
-                             nthreads=cores)
-        dt = time.perf_counter() - t0
-        spent += dt
-        per_probe += dt * texels / k
-        parts.append(f"mip{ow}x{oh}:{k}")
-    k = max(8, int(64 * scale))
-    idx = rng.choice(IRR_W * IRR_H, size=k, replace=False)
-    xy = np.stack([idx % IRR_W, idx // IRR_W], 1).astype(np.int32)
-    t0 = time.perf_counter()
-    if use_ref:
-        s = ENV_W // IRR_W  # env-size dispatch of the reference, strided texels
-        oracle.ref_irradiance_envsize(chain, ENV_W, ENV_H, xy * s, nthreads=cores)
-    else:
-        oracle.irradiance(chain, ENV_W, ENV_H, IRR_W, IRR_H, xy=xy, nthreads=cores)
-    dt = time.perf_counter() - t0
-    spent += dt
-    per_probe += dt * IRR_W * IRR_H / k
-    parts.append(f"irradiance:{k}")
-    # LUT: the reference has no generator; the C restatement times it.
-    t0 = time.perf_counter()
-    n_small = 64
-    oracle.brdf_lut_f32(n_small, LUT_SAMPLES, oracle.LUT_ASSET, nthreads=cores)
-    dt = time.perf_counter() - t0
-    spent += dt
-    per_probe += dt * (LUT_N * LUT_N) / (n_small * n_small)
-    parts.append(f"lut:{n_small}x{n_small}")
-    return per_probe, kind, cores, "texels per stage " + ",".join(parts), spent
+        for (ow, oh), r in zip(mip_sizes(), roughness()):
+            xy = self.rows_xy(ow, oh, k, strata)
+            if xy is not None:
+                self.prefilter(ow, oh, r, xy)
+        xy = self.rows_xy(IRR_W, IRR_H, k, strata)
+        if xy is not None:
+            self.irradiance(xy)
+        if k == 0:
+            self.oracle.brdf_lut_f32(LUT_N, LUT_SAMPLES, self.oracle.LUT_ASSET,
+                                     nthreads=self.cores)
+        return time.perf_counter() - t0
+
+    def whole_probe(self, strata=CPU_STRATA):
+        """Every texel of one probe, stratum by stratum: seconds per probe.  One
+        stratum runs first, untimed (thread pool, page faults), as the
+        reference arm's warm-up steps do."""
+        self.stratum(strata - 1, strata)
+        return sum(self.stratum(k, strata) for k in range(strata))
+
+    def max_err_vs_fp64(self, env, per_mip=128, seed=7):
+        """The estimator's max relative error against the FP64 quadrature over
+        level 0 on sampled texels of every mip with roughness > 0 and of the
+        irradiance (the contract the precision path is held to)."""
+        o = self.oracle
+        rng = np.random.default_rng(seed)
+        worst = 0.0
+        for (w, h), r in zip(mip_sizes(), roughness()):
+            if r == 0.0:
+                continue
+            idx = rng.choice(w * h, size=min(per_mip, w * h), replace=False)
+            xy = np.stack([idx % w, idx // w], 1).astype(np.int32)
+            ref = o.quad_prefilter(env, w, h, r, xy, nthreads=self.cores)[:, :3]
+            got = self.prefilter(w, h, r, xy)[:, :3]
+            worst = max(worst, float((np.abs(got - ref) / np.abs(ref)).max()))
+        idx = rng.choice(IRR_W * IRR_H, size=per_mip, replace=False)
+        xy = np.stack([idx % IRR_W, idx // IRR_W], 1).astype(np.int32)
+        ref = o.quad_irradiance(env, IRR_W, IRR_H, xy, nthreads=self.cores)[:, :3]
+        got = self.irradiance(xy)[:, :3]
+        return max(worst, float((np.abs(got - ref) / np.abs(ref)).max()))
+
+
+def cpu_baseline_line(env):
+    """cpu_baseline of the GPU arm's line: one whole probe (every texel) on
+    every host core."""
+    cp = CpuProbe(env, "reference")
+    sec = cp.whole_probe()
+    return {"value": 1.0 / sec, "unit": "probes/s", "cores": cp.cores, "kind": cp.kind,
+            "sample": f"one whole probe: every texel of the 9 mips and the irradiance, and "
+                      f"the {LUT_N}x{LUT_N} LUT, baked in {CPU_STRATA} row strata after one "
+                      f"untimed stratum ({sec:.1f} s of CPU work, nothing extrapolated)"}
 
 
 def run_reference(args):
+    """The reference's own CPU implementation of the path (the reference
+    shaders compiled as C++) on every host core.  Step i bakes stratum
+    i mod S of the probe (S = min(8, steps)), so the timed steps bake every
+    texel at least once; value = 1 / (sum over the S strata of each stratum's
+    mean time), ms_per_step = the mean measured step time."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
     from althea_gb300 import synth
-    env = synth.make_env(ENV_W, ENV_H, seed=0, sun_max=args.sun_max if args.path == "tc" else 1e4)
-    for _ in range(args.warmup):
-        cpu_sample_probe_time(env, "reference", scale=8.0)
-    times = []
-    info = None
-    for _ in range(args.steps):
-        per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference", scale=8.0)
-        times.append(per_probe)
-        info = (kind, cores, sample)
-    sec = float(np.mean(times))
-    value = 1.0 / sec
+    sun_max = args.sun_max if args.path == "tc" else 1e4
+    env = synth.make_env(ENV_W, ENV_H, seed=0, sun_max=sun_max)
+    cp = CpuProbe(env, "reference")
+    strata = max(1, min(CPU_STRATA, args.steps))
+    for i in range(args.warmup):
+        cp.stratum(i % strata, strata)
+    per_stratum = [[] for _ in range(strata)]
+    steps_s = []
+    t_all = time.perf_counter()
+    for i in range(args.steps):
+        dt = cp.stratum(i % strata, strata)
+        per_stratum[i % strata].append(dt)
+        steps_s.append(dt)
+    elapsed = time.perf_counter() - t_all
+    sec_per_probe = float(sum(np.mean(t) for t in per_stratum))
+    value = 1.0 / sec_per_probe
+    err = cp.max_err_vs_fp64(env)
+    sample = (f"step i = row stratum i mod {strata} of every output (rows k, k+{strata}, ...; "
+              f"the {LUT_N}x{LUT_N} LUT in stratum 0): {strata} consecutive steps bake every "
+              f"texel of the probe once; {args.steps} timed steps, {elapsed:.1f} s")
     line = {"metric": METRIC, "value": value, "unit": "probes/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(steps_s)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "impl": "reference",
+            "data": f"synthetic (seeded sky x log-normal noise + 8 suns <= {sun_max:g})",
+            "impl": "reference",
             "config": {"workload": TC_WORKLOAD if args.path == "tc" else workload(),
                        "path": "reference compute shaders compiled as C++ (CPU, all host "
-                       "threads, N = 1024 samples per texel), extrapolated from a bounded "
-                       "texel sample"},
-            "cpu_baseline": {"value": value, "unit": "probes/s", "cores": info[1],
-                             "kind": info[0], "sample": info[2]},
+                               f"threads, N = {SAMPLES} samples per texel), every texel timed",
+                       "ms_per_probe": sec_per_probe * 1e3,
+                       "strata": strata,
+                       "max_rel_err_vs_fp64": err,
+                       "contract": "the reference estimator (Monte Carlo, N = 1024) is not "
+                                   "within 1e-3 of the FP64 quadrature (max_rel_err_vs_fp64); "
+                                   "the precision path is, the plain path matches this "
+                                   "estimator bit for bit"},
+            "cpu_baseline": {"value": value, "unit": "probes/s", "cores": cp.cores,
+                             "kind": cp.kind, "sample": sample},
             "e2e": {"value": value, "unit": "probes/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -383,9 +456,7 @@ def run_ours(args):
         achieved = prefilter_algorithmic_bytes() / (pf_ms / 1e3) / 1e9
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
-            per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference", scale=100.0)
-            cpu = {"value": 1.0 / per_probe, "unit": "probes/s", "cores": cores, "kind": kind,
-                   "sample": sample + f" ({spent:.1f} s of CPU work)"}
+            cpu = cpu_baseline_line(env)
         line = {
             "metric": METRIC, "value": value, "unit": "probes/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -430,14 +501,32 @@ def tc_jobs(levels, irr_level):
     return jobs
 
 
+# Glossy mips at most this rough take the library's two-product split (BF16
+# hi weights: hi*hi + hi*lo per channel) when the planner chose their level.
+TC_TWO_PRODUCT_MAX_ROUGHNESS = 0.2
+
+
+def tc_products(w, h, lv):
+    """BF16 products per channel and pair of one output of the default bake:
+    2 for a planned GGX mip of roughness <= 0.2, else 3 (hi*hi, hi*lo, lo*hi)."""
+    for (mw, mh), r in zip(mip_sizes(), roughness()):
+        if (mw, mh) == (w, h) and r > 0.0:
+            return 2 if r <= TC_TWO_PRODUCT_MAX_ROUGHNESS else 3
+    return 3  # the irradiance
+
+
 def tc_flops(levels, irr_level):
     """Per bake: (algorithmic flops, executed split-precision flops).  Every
     output texel is a sum over every texel of its source level (a pair).
     Algorithmic: 2 flops x 4 channels (RGBA, counted once) per pair -- hi/lo
     split terms, padding and weight generation not counted.  Executed: the
-    3 colour channels x 3 BF16 products (hi*hi, hi*lo, lo*hi) issued per pair."""
-    pairs = sum(w * h * ws * hs for w, h, ws, hs, _, _ in tc_jobs(levels, irr_level))
-    return 2 * 4 * pairs, 2 * 9 * pairs
+    3 colour channels x the BF16 products issued per pair (3, or 2 for the
+    two-product mips)."""
+    jobs = tc_jobs(levels, irr_level)
+    pairs = sum(w * h * ws * hs for w, h, ws, hs, _, _ in jobs)
+    executed = sum(2 * 3 * tc_products(w, h, lv) * w * h * ws * hs
+                   for w, h, ws, hs, lv, _ in jobs)
+    return 2 * 4 * pairs, executed
 
 
 # Outputs of at most this many texels are summed on the CUDA cores instead of
@@ -570,40 +659,100 @@ def run_tc(args):
         barrier()
         return evs
 
+    # value: the product path, the bake context (the createResources mirror)
+    # on the precision path with the env already in HBM: level 0 copied into
+    # the context's resident chain and the chain rebuilt (upload_env from
+    # device memory), then the bake -- contractions on the caller's stream, the
+    # LUT and the outputs summed on the CUDA cores on the context's side
+    # streams, joined before the bake returns.
+    cfg = ibl.make_config(ENV_W, ENV_H, irradiance_size=(IRR_W, IRR_H), mip_count=MIPS,
+                          first_mip=(FIRST_W, FIRST_H), lut_size=LUT_N,
+                          lut_samples=LUT_SAMPLES, path=ibl.PATH_PRECISION)
+    vctx = ibl.BakeContext(cfg)
+    v_irr, v_mips, v_lut = vctx.allocate_outputs(device=dev)
+
+    def product_step(ev):
+        ev[0].record(stream)
+        vctx.upload_env(env_d, stream)
+        vctx.bake(v_irr, v_mips, v_lut, stream)
+        ev[1].record(stream)
+
     with ClockSampler(local) as clk:
-        evs = timed(step, 4)
-    ibl._check(ibl.load().althea_ibl_tc_error(ws.data_ptr(), stream.cuda_stream))
-    total_ms = adist.allreduce_max(float(np.sum([e[0].elapsed_time(e[3]) for e in evs])), dev)
+        vevs = timed(product_step, 2)
+    vctx.status(stream)
+    total_ms = adist.allreduce_max(float(np.sum([e[0].elapsed_time(e[1]) for e in vevs])), dev)
     value = args.steps * world / (total_ms / 1e3)
+    # stage times (for the roofline): the same kernels through the stateless
+    # calls on one stream, chain | contractions | LUT between events
+    evs = timed(step, 4)
+    ibl._check(ibl.load().althea_ibl_tc_error(ws.data_ptr(), stream.cuda_stream))
+    serial_ms = float(np.mean([e[0].elapsed_time(e[3]) for e in evs]))
     tc_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
     chain_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
     lut_ms = float(np.mean([e[2].elapsed_time(e[3]) for e in evs]))
     tc_outs = [t.cpu().numpy() for t in mips]
     tc_irr = irr.cpu().numpy()
+    product_same = all(np.array_equal(v_mips[m].cpu().numpy(), tc_outs[m]) for m in range(MIPS))
+    product_same = product_same and np.array_equal(v_irr.cpu().numpy(), tc_irr)
+    product_same = product_same and torch.equal(v_lut, lut)
+    vctx.close()
 
-    # e2e: pinned host env in, every output out, through the public calls
+    # e2e through the public bake context (the createResources mirror, precision
+    # path): every step uploads the env from pinned host memory, bakes (chain,
+    # contractions, LUT) and reads every output back to pinned host memory.
+    # Two contexts on two streams take alternate steps, so one step's copies
+    # overlap the other's bake (a renderer re-baking probes back to back).
+    cfg = ibl.make_config(ENV_W, ENV_H, irradiance_size=(IRR_W, IRR_H), mip_count=MIPS,
+                          first_mip=(FIRST_W, FIRST_H), lut_size=LUT_N,
+                          lut_samples=LUT_SAMPLES, path=ibl.PATH_PRECISION)
     host_env = torch.from_numpy(env).pin_memory()
-    h_outs = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in mips + [irr, lut]]
+    lanes = []
+    for _ in range(2):
+        ctx = ibl.BakeContext(cfg)
+        e_irr, e_mips, e_lut = ctx.allocate_outputs(device=dev)
+        dev_outs = e_mips + [e_irr, e_lut]
+        host_outs = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in dev_outs]
+        lanes.append((ctx, e_irr, e_mips, e_lut, dev_outs, host_outs,
+                      torch.cuda.Stream(device=dev)))
 
-    def e2e_step():
-        env_d.copy_(host_env, non_blocking=True)
-        step([torch.cuda.Event(enable_timing=True) for _ in range(4)])
-        for hdst, dsrc in zip(h_outs, mips + [irr, lut]):
-            hdst.copy_(dsrc, non_blocking=True)
+    def e2e_step(i):
+        ctx, e_irr, e_mips, e_lut, dev_outs, host_outs, st = lanes[i % 2]
+        ctx.upload_env(host_env, st)
+        ctx.bake(e_irr, e_mips, e_lut, st)
+        for hdst, dsrc in zip(host_outs, dev_outs):
+            with torch.cuda.stream(st):
+                hdst.copy_(dsrc, non_blocking=True)
 
-    with torch.cuda.stream(stream):
-        e2e_step()
-    stream.synchronize()
+    def e2e_run(nsteps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0, s1 = lanes[0][6], lanes[1][6]
+        a.record(s0)
+        s1.wait_event(a)
+        for i in range(nsteps):
+            e2e_step(i)
+        done1 = torch.cuda.Event()
+        done1.record(s1)
+        s0.wait_event(done1)
+        b.record(s0)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    e2e_run(max(2, args.warmup))
+    for ln in lanes:
+        ln[0].status(ln[6])  # no bounded wait gave up
+    # the context's bake is the stateless bake above: same kernels, same bits
+    e2e_same = True
+    for ln in lanes:
+        e_irr_, e_mips_ = ln[1], ln[2]
+        e2e_same &= all(np.array_equal(e_mips_[m].cpu().numpy(), tc_outs[m])
+                        for m in range(MIPS))
+        e2e_same &= np.array_equal(e_irr_.cpu().numpy(), tc_irr)
     barrier()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        a.record(stream)
-        for _ in range(args.steps):
-            e2e_step()
-        b.record(stream)
-    stream.synchronize()
-    barrier()
-    e2e_ms = adist.allreduce_max(a.elapsed_time(b), dev) / args.steps
+    e2e_ms = adist.allreduce_max(e2e_run(args.steps), dev) / args.steps
+    h2d = host_env.numel() * 4
+    d2h = sum(t.numel() * t.element_size() for t in lanes[0][5])
+    for ln in lanes:
+        ln[0].close()
 
     # the plain path (reference estimator, N = 1024 Hammersley) on the same map
     p_mips = [torch.empty_like(t) for t in mips]
@@ -624,19 +773,25 @@ def run_tc(args):
                                    dev) / args.steps
     errs = error_table(env, {"tensor": tc_outs, "plain": [t.cpu().numpy() for t in p_mips]},
                        {"tensor": tc_irr, "plain": p_irr.cpu().numpy()})
+    # Batching and serving configurations, measured in the same run (one GPU):
+    # a 256-probe precision batch as one graph launch, and one Poisson arrival
+    # rate of resident-map re-bake requests.
+    sub_batch = sub_serve = None
+    if world == 1 and not args.no_sub:
+        sub_batch = measure_batch(256, True, args.sun_max, steps=5, warmup=2)
+        rows, sinfo = measure_serving(True, [1000.0], 2000, args.sun_max)
+        sub_serve = {"rows": rows, **sinfo,
+                     "workload": "Poisson re-bake requests at 1000/s, 2000 requests, sizes "
+                                 "uniform over 256..2048 wide, resident skies, 8 suns "
+                                 "re-seeded per request on the device, precision path"}
     if rank == 0:
         peak, peak_kind = read_tensor_peak()
         alg_flops, split_flops = tc_flops(levels, irr_level)
         achieved = alg_flops / (tc_ms / 1e3) / 1e12
         executed = split_flops / (tc_ms / 1e3) / 1e12
-        h2d = host_env.numel() * 4
-        d2h = sum(t.numel() * 4 for t in h_outs)
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
-            per_probe, kind, cores, sample, spent = cpu_sample_probe_time(env, "reference",
-                                                                         scale=100.0)
-            cpu = {"value": 1.0 / per_probe, "unit": "probes/s", "cores": cores, "kind": kind,
-                   "sample": sample + f" ({spent:.1f} s of CPU work)"}
+            cpu = cpu_baseline_line(env)
         line = {"metric": METRIC, "value": value, "unit": "probes/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -646,15 +801,25 @@ def run_tc(args):
                            "path": "tensor", "global_batch": world,
                            "parallelism": f"replicas x{world}",
                            "source_levels": levels, "irradiance_level": irr_level,
-                           "stage_ms": {"chain": chain_ms, "contraction": tc_ms, "lut": lut_ms},
+                           "api": "BakeContext (althea_ibl_create / upload_env / bake, "
+                                  "path = precision): contractions on the caller's stream, "
+                                  "LUT and CUDA-core outputs on the context's side streams",
+                           "outputs_equal_stateless_calls": bool(product_same),
+                           "stage_ms": {"chain": chain_ms, "contraction": tc_ms, "lut": lut_ms,
+                                        "serial_step": serial_ms},
                            "plain_same_map": {"value": 1e3 / plain_ms, "unit": "probes/s",
                                               "ms_per_step": plain_ms,
                                               "max_rel_err_vs_fp64": errs["plain"]["max"]},
                            "max_rel_err_vs_fp64": errs["tensor"]["max"],
                            "errors_per_mip_max_mean": errs,
-                           "l2": "flushed (256 MB write) between timed steps"},
+                           "l2": "flushed (256 MB write) between timed steps",
+                           "batch_256": sub_batch, "serving": sub_serve},
                 "e2e": {"value": world * 1e3 / e2e_ms, "unit": "probes/s",
-                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "api": "BakeContext (althea_ibl_create / upload_env / bake, "
+                               "path = precision), two contexts on two streams taking "
+                               "alternate steps",
+                        "outputs_equal_device_path": bool(e2e_same)},
                 "gpu_launches": tc_launches(levels, irr_level) * args.steps,
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
                              "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
@@ -712,120 +877,180 @@ def batch_algorithmic_bytes(specs):
     return total
 
 
-def run_batch(args):
-    """Many probes of uneven size per step: one CUDA-graph launch per batch."""
+def batch_envs(specs, seed0, sun_max, dev):
+    """Level-0 maps of a batch on the device: one seeded sky per width (numpy),
+    plus each probe's own 8 suns (seed0 + probe index) added on the device."""
     import torch
     from althea_gb300 import ibl, synth
-    world, rank, local = dist_setup()
-    torch.cuda.set_device(local)
-    precision = args.path == "tc"
-    specs = batch_specs(args.batch, seed=rank)
-    envs = [torch.from_numpy(synth.make_env(s.env_width, s.env_height, seed=1000 * rank + i,
-                                            sun_max=args.sun_max if precision else 1e4))
-            .cuda() for i, s in enumerate(specs)]
+    skies = {}
+    envs = []
+    for i, s in enumerate(specs):
+        if s.env_width not in skies:
+            skies[s.env_width] = torch.from_numpy(synth.make_env(
+                s.env_width, s.env_height, seed=seed0 + s.env_width, with_suns=False)).to(dev)
+        envs.append(ibl.apply_suns(skies[s.env_width],
+                                   synth.draw_suns(seed0 + i, sun_max=sun_max)))
+    torch.cuda.synchronize()
+    return envs
+
+
+def measure_batch(n, precision, sun_max, steps, warmup, seed=0, clocks=None):
+    """A batch of n probes of the batching configuration (widths uniform over
+    256..2048, log2(W)-3 mips, 32x16 irradiance, one shared 256x256 LUT) as
+    one CUDA-graph launch per step; returns the figures of the line."""
+    import torch
+    from althea_gb300 import ibl
+    dev = torch.device("cuda", torch.cuda.current_device())
+    specs = batch_specs(n, seed=seed)
+    envs = batch_envs(specs, 1000 * seed, sun_max if precision else 1e4, dev)
     stream = torch.cuda.Stream()
     batch = ibl.ProbeBatch(specs, envs, samples=SAMPLES, generator=GENERATOR, lut_size=256,
                            lut_samples=LUT_SAMPLES, autotune=True, graph=True, stream=stream,
                            precision=precision, half=precision)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             batch.run(stream)
     stream.synchronize()
     evs = []
-    with ClockSampler(local) as clk:
-        with torch.cuda.stream(stream):
-            for _ in range(args.steps):
-                flush.fill_(1)
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                batch.run(stream)
-                b.record(stream)
-                evs.append((a, b))
-        torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            flush.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            batch.run(stream)
+            b.record(stream)
+            evs.append((a, b))
+    torch.cuda.synchronize()
     ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
     info = batch.info()
-    peak, peak_kind = read_peaks()
-    algo = batch_algorithmic_bytes(specs)
-    achieved = algo / (ms / 1e3) / 1e9
     widths = {}
-    for s in specs:
-        widths[s.env_width] = widths.get(s.env_width, 0) + 1
-    tc_roofline = None
+    for sp in specs:
+        widths[sp.env_width] = widths.get(sp.env_width, 0) + 1
+    out = {"value": n / (ms / 1e3), "unit": "probes/s", "ms_per_step": ms, "probes": n,
+           "widths": dict(sorted(widths.items())), "path": "tensor" if precision else "plain",
+           "graph_kernels": info.graph_kernels, "tile": [info.tile_x, info.tile_y],
+           "persistent_blocks": info.persistent_blocks,
+           "irradiance_target_blocks": info.irradiance_target_blocks}
     if precision:
         tpeak, tkind = read_tensor_peak()
         tflops = batch_tc_flops(specs) / (ms / 1e3) / 1e12
-        tc_roofline = {"bound": "tensor", "achieved": tflops, "peak": tpeak, "unit": "TFLOP/s",
-                       "frac": tflops / tpeak, "traffic": None,
-                       "kernel": "whole batch graph (algorithmic flops of every contraction)",
-                       "peak_source": tkind}
+        out["roofline"] = {"bound": "tensor", "achieved": tflops, "peak": tpeak,
+                           "unit": "TFLOP/s", "frac": tflops / tpeak, "traffic": None,
+                           "kernel": "whole batch graph (algorithmic flops of every "
+                                     "contraction)", "peak_source": tkind}
+    else:
+        peak, peak_kind = read_peaks()
+        achieved = batch_algorithmic_bytes(specs) / (ms / 1e3) / 1e9
+        out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                           "frac": achieved / peak, "traffic": None,
+                           "kernel": "whole batch graph", "peak_source": peak_kind}
+    batch.close()
+    return out
+
+
+def run_batch(args):
+    """Many probes of uneven size per step: one CUDA-graph launch per batch."""
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    precision = args.path == "tc"
+    with ClockSampler(local) as clk:
+        r = measure_batch(args.batch, precision, args.sun_max, args.steps, args.warmup,
+                          seed=rank)
     path_desc = ("precision path (BF16 hi/lo tcgen05 contractions, RGBA16F outputs)" if precision
                  else f"plain path FP32, N=1024 {'Hammersley' if GENERATOR else 'reference-hash'}")
-    line = {"metric": METRIC, "value": args.batch / (ms / 1e3), "unit": "probes/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    line = {"metric": METRIC, "value": r["value"] * world, "unit": "probes/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
             "dtype": "bf16 hi/lo (fp32 accumulate)" if precision else "f32",
-            "data": "synthetic", "config": {
-                "workload": f"batch of {args.batch} probes (widths {dict(sorted(widths.items()))}"
+            "data": "synthetic (one seeded sky per width + each probe's own 8 suns)",
+            "config": {
+                "workload": f"batch of {args.batch} probes (widths {r['widths']}"
                             f", 2:1, log2(W)-3 mips from W/2, 32x16 irradiance, shared 256x256 "
                             f"LUT), {path_desc}, one CUDA-graph launch per step",
-                "path": "tensor" if precision else "plain",
-                "tile": [info.tile_x, info.tile_y], "persistent_blocks": info.persistent_blocks,
-                "irradiance_target_blocks": info.irradiance_target_blocks,
+                "path": r["path"], "tile": r["tile"],
+                "persistent_blocks": r["persistent_blocks"],
+                "irradiance_target_blocks": r["irradiance_target_blocks"],
                 "l2": "flushed (256 MB write) between timed steps"},
-            "gpu_launches": (info.graph_kernels * args.steps if info.graph_kernels >= 0
+            "gpu_launches": (r["graph_kernels"] * args.steps if r["graph_kernels"] >= 0
                              else None),
-            "roofline": tc_roofline if precision else {
-                "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "kernel": "whole batch graph",
-                "peak_source": peak_kind},
+            "roofline": r["roofline"],
             "clocks": clk.summary()}
     if rank == 0:
         print(json.dumps(line))
-    batch.close()
     return 0
 
 
-def run_serve(args):
-    """Poisson stream of re-bake requests (sizes as in the batch workload, suns
-    re-seeded per request from a pool of prepared maps) against the native
-    server under an HBM budget; p50/p99 latency and throughput per rate."""
-    from althea_gb300 import serving, synth
-    world, rank, local = dist_setup()
-    import torch
-    torch.cuda.set_device(local)
-    from althea_gb300 import ibl
-    precision = args.path == "tc"
-    server = serving.ProbeServer(budget_bytes=int(args.budget_gb * (1 << 30)),
-                                 max_inflight=args.inflight, samples=SAMPLES,
+def serve_maps(server, n, seed, precision):
+    """n resident skies (widths uniform over 256..2048, 2:1) registered with the
+    server, each with a pinned output buffer set per request in flight; the
+    requests add their own 8 suns on the device."""
+    from althea_gb300 import synth
+    rng = np.random.default_rng(seed)
+    pool = []
+    for k in range(n):
+        w = int(rng.choice([256, 512, 1024, 2048]))
+        sky = synth.make_env(w, w // 2, seed=5000 + 100 * seed + k, with_suns=False)
+        env_id = server.register_env(sky)
+        pool.append(server.output_buffers(env_id, max(1, w.bit_length() - 1 - 3)))
+    return pool
+
+
+def measure_serving(precision, rates, requests, sun_max, seed=0, pool_size=64, inflight=16,
+                    budget_gb=40.0, warm=64):
+    """Poisson streams of re-bake requests against the native server: resident
+    skies, each request with its own 8 suns (seeded by the request index);
+    p50/p99 latency and throughput per arrival rate."""
+    from althea_gb300 import ibl, serving, synth
+    server = serving.ProbeServer(budget_bytes=int(budget_gb * (1 << 30)),
+                                 max_inflight=inflight, samples=SAMPLES,
                                  generator=GENERATOR, irradiance_size=(32, 16),
                                  path=ibl.PATH_PRECISION if precision else ibl.PATH_PLAIN)
-    rng = np.random.default_rng(rank)
-    pool = []
-    for k in range(args.pool):
-        w = int(rng.choice([256, 512, 1024, 2048]))
-        env = synth.make_env(w, w // 2, seed=5000 + 100 * rank + k,
-                             sun_max=args.sun_max if precision else 1e4)
-        pool.append(server.buffers(env, max(1, w.bit_length() - 1 - 3)))
-    serving.run_poisson(server, pool, rate=200.0, n_requests=min(64, 4 * len(pool)), seed=1)
-    rows = []
-    for rate in args.rates:
-        n = int(min(args.requests, max(64, rate * args.seconds)))
-        rows.append(serving.run_poisson(server, pool, rate=rate, n_requests=n, seed=int(rate)))
+    pool = serve_maps(server, pool_size, seed, precision)
+    sm = sun_max if precision else 1e4
+
+    def suns_for(i):
+        return synth.draw_suns(1_000_003 * (seed + 1) + i, sun_max=sm)
+
+    serving.run_poisson(server, pool, rate=200.0, n_requests=warm, seed=1, suns_for=suns_for)
+    rows = [serving.run_poisson(server, pool, rate=rate, n_requests=requests, seed=int(rate),
+                                suns_for=suns_for) for rate in rates]
+    st = server.stats()
     server.close()
+    return rows, {"resident_maps": pool_size, "resident_bytes": int(st.bytes_resident),
+                  "slots": inflight, "budget_gb": budget_gb}
+
+
+def run_serve(args):
+    """Poisson stream of re-bake requests (sizes as in the batch workload) against
+    the native server under an HBM budget, maps resident on the device, each
+    request's 8 suns re-seeded and added on the device; p50/p99 latency and
+    throughput per rate."""
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    precision = args.path == "tc"
+    with ClockSampler(local) as clk:
+        rows, info = measure_serving(precision, args.rates, args.requests, args.sun_max,
+                                     seed=rank, pool_size=args.pool, inflight=args.inflight,
+                                     budget_gb=args.budget_gb)
     best = max(r["throughput"] for r in rows)
     line = {"metric": METRIC, "value": best, "unit": "probes/s", "n_gpus": world,
             "steps": len(rows), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16 hi/lo (fp32 accumulate)" if precision else "f32", "data": "synthetic",
-            "config": {"workload": f"serving: Poisson re-bake requests, sizes uniform over "
-                                   f"256..2048 wide (2:1), log2(W)-3 mips, 32x16 irradiance, "
+            "config": {"workload": f"serving: Poisson re-bake requests, {args.requests} per "
+                                   f"rate, sizes uniform over 256..2048 wide (2:1), log2(W)-3 "
+                                   f"mips, 32x16 irradiance, "
                                    f"{'precision path' if precision else 'N=1024'}, "
                                    f"{args.inflight} slots, {args.budget_gb} GB budget, "
-                                   f"{args.pool} pre-generated maps (suns re-seeded per map), "
-                                   "latency = completion callback - arrival, host pinned I/O",
-                       "path": "tensor" if precision else "plain"},
-            "serving": rows}
+                                   f"{args.pool} resident skies, each request's 8 suns "
+                                   "re-seeded and added on the device, latency = completion "
+                                   "callback - arrival, outputs read back to pinned host memory",
+                       "path": "tensor" if precision else "plain", **info},
+            "serving": rows, "clocks": clk.summary()}
     if rank == 0:
         print(json.dumps(line))
     return 0
@@ -1063,11 +1288,12 @@ def main():
                          "or the plain estimator (suns <= 1e4)")
     ap.add_argument("--sun-max", type=float, default=1e6, help="precision path sun radiance")
     ap.add_argument("--rates", type=float, nargs="+", default=[50, 200, 500, 1000, 2000])
-    ap.add_argument("--requests", type=int, default=10000)
-    ap.add_argument("--seconds", type=float, default=4.0, help="per-rate cap on arrival time")
+    ap.add_argument("--requests", type=int, default=10000, help="serving: requests per rate")
     ap.add_argument("--budget-gb", type=float, default=40.0)
     ap.add_argument("--inflight", type=int, default=16)
-    ap.add_argument("--pool", type=int, default=32)
+    ap.add_argument("--pool", type=int, default=64, help="serving: resident skies")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="default line: skip the batch and serving sub-measurements")
     args = ap.parse_args()
     global GENERATOR
     GENERATOR = 1 if args.generator == "hammersley" else 0
