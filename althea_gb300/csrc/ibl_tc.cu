@@ -237,23 +237,33 @@ __device__ __forceinline__ void mma_stage_ts(uint32_t d, uint32_t a, uint64_t bh
       : "memory");
 }
 
-// The same stage with the weights as BF16 hi only (two products per K = 16):
-//   D += Ahi*Bhi + Ahi*Blo  for K = 0..15 and 16..31.
-// The weight sum is then taken over the same rounded weights, so the
-// normalised result is an exact weighted average with BF16 weights.
-__device__ __forceinline__ void mma_stage_ts2(uint32_t d, uint32_t a, uint64_t bh, uint64_t bl,
-                                              uint64_t bh2, uint64_t bl2, uint32_t idesc,
-                                              uint32_t accumulate, uint64_t* bar) {
+// A K = 64 stage with the weights as BF16 hi only (two products per K = 16):
+//   D += Ahi*Bhi + Ahi*Blo  for K = 16t .. 16t + 15, t = 0..3,
+// A at TMEM columns a + 8t (hi only: 64 K in 32 columns), B descriptors
+// bh + 2t / bl + 2t (16-byte units).  Without the lo half of the weights a
+// stage of 64 K fits the TMEM of a 32 K hi/lo stage, which halves the
+// producers' per-stage hand-off work per weight.  The weight sum is taken
+// over the same rounded weights, so the normalised result is an exact
+// weighted average with BF16 weights.
+__device__ __forceinline__ void mma_stage64_ts2(uint32_t d, uint32_t a, uint64_t bh, uint64_t bl,
+                                                uint32_t idesc, uint32_t accumulate,
+                                                uint64_t* bar) {
   asm volatile(
-      "{\n .reg .pred p, t;\n .reg .b32 a8;\n"
-      " setp.ne.b32 p, %7, 0;\n setp.eq.b32 t, %7, %7;\n"
-      " add.u32 a8, %1, 8;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %6, p;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %3, %6, t;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a8], %4, %6, t;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a8], %5, %6, t;\n"
-      " tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%8];\n}\n" ::"r"(d),
-      "r"(a), "l"(bh), "l"(bl), "l"(bh2), "l"(bl2), "r"(idesc), "r"(accumulate),
+      "{\n .reg .pred p, t;\n .reg .b32 a8, a16, a24;\n .reg .b64 h2, l2, h4, l4, h6, l6;\n"
+      " setp.ne.b32 p, %5, 0;\n setp.eq.b32 t, %5, %5;\n"
+      " add.u32 a8, %1, 8;\n add.u32 a16, %1, 16;\n add.u32 a24, %1, 24;\n"
+      " add.u64 h2, %2, 2;\n add.u64 l2, %3, 2;\n add.u64 h4, %2, 4;\n"
+      " add.u64 l4, %3, 4;\n add.u64 h6, %2, 6;\n add.u64 l6, %3, 6;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %4, p;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %3, %4, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a8], h2, %4, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a8], l2, %4, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a16], h4, %4, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a16], l4, %4, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a24], h6, %4, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [a24], l6, %4, t;\n"
+      " tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%6];\n}\n" ::"r"(d),
+      "r"(a), "l"(bh), "l"(bl), "r"(idesc), "r"(accumulate),
       "r"((uint32_t)__cvta_generic_to_shared(bar))
       : "memory");
 }
@@ -286,6 +296,13 @@ __device__ __forceinline__ void tmem_st4(uint32_t taddr, const uint32_t* v) {
   asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr),
                "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3])
                : "memory");
+}
+
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+      : "memory");
 }
 
 __device__ __forceinline__ void tmem_wait_st() {
@@ -453,7 +470,11 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   const int j0 = split * j_per;
   const int j1 = min(job.hs, j0 + j_per);
   const int nrows = j1 > j0 ? j1 - j0 : 0;
-  const int kchunks = job.kpad / kKS;
+  // K per pipeline stage: 64 with hi-only weights (two products), else 32
+  constexpr int KS = TWO ? 64 : kKS;
+  constexpr int KW = KS / 4;   // K per producer warp and stage
+  constexpr int NG = KW / 8;   // groups of 8 K per producer warp and stage
+  const int kchunks = job.kpad / KS;
   const long long total = (long long)nrows * job.g * kchunks;
   const bool want_wsum = KIND == 0 && blockIdx.y == 0;
   const bool want_wsum_b = job.pair && job.kind_b == 0 && blockIdx.y == 0;
@@ -481,7 +502,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     const float2 minus1 = make_float2(-1.0f, -1.0f);
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
     double wacc = 0.0;
-    long long gidx = 0;
+    uint32_t gidx = 0;
     int pending = -1;  // stage whose stores are issued but not yet published
     bool ok = true;
     for (int j = j0; live && j < j1 && ok; ++j) {
@@ -496,11 +517,13 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
         float2 rowsum2 = make_float2(0.0f, 0.0f);
         for (int kc = 0; kc < kchunks; ++kc, ++gidx) {
           const int st = (int)(gidx & (kStages - 1));
-          const long long use = gidx / kStages;
+          const uint32_t use = gidx / kStages;
           if (kint && st != q) continue;  // another quarter's stage
-          uint32_t hw[4], lw[4];
+          uint32_t hw[4 * NG], lw[4];
           if (live) {
-            const int kb = kc * kKS + 8 * h;
+#pragma unroll
+           for (int gq = 0; gq < NG; ++gq) {
+            const int kb = kc * KS + KW * h + 8 * gq;
             // four pairs of weights with packed FP32x2 arithmetic
             float2 w[4];
 #pragma unroll
@@ -539,7 +562,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
               const __nv_bfloat162 h2 = __floats2bfloat162_rn(w[e].x, w[e].y);
-              hw[e] = *reinterpret_cast<const uint32_t*>(&h2);
+              hw[4 * gq + e] = *reinterpret_cast<const uint32_t*>(&h2);
               if (TWO) {
                 w[e] = __bfloat1622float2(h2);  // the weight the MMAs use
               } else {
@@ -550,6 +573,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
             }
             if (want)
               rowsum2 = __fadd2_rn(__fadd2_rn(rowsum2, w[0]), __fadd2_rn(__fadd2_rn(w[1], w[2]), w[3]));
+           }
           }
           // Software pipeline: the previous stage's TMEM stores landed while
           // this stage's weights were computed; publish that stage now.
@@ -565,9 +589,14 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
             break;
           }
           if (live) {
-            const uint32_t col = (uint32_t)(kACol + st * kKS + 4 * h);
-            tmem_st4(lane_base + col, hw);
-            if (!TWO) tmem_st4(lane_base + col + 16, lw);
+            if (TWO) {
+              // hi only, K 16t .. 16t + 15 at stage column 8t: this warp's 16 K
+              tmem_st8(lane_base + (uint32_t)(kACol + st * kKS + 8 * h), hw);
+            } else {
+              const uint32_t col = (uint32_t)(kACol + st * kKS + 4 * h);
+              tmem_st4(lane_base + col, hw);
+              tmem_st4(lane_base + col + 16, lw);
+            }
           }
           if (kint) {
             // publish at once: the next stage this quarter owns is four away
@@ -614,7 +643,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
             break;
           }
           uint64_t dbh = bdesc0 + (uint64_t)(slot * slot16 + plane16);
-          for (int kc = 0; kc < kchunks; ++kc, ++gidx, dbh += kKS * 2 / 16) {
+          for (int kc = 0; kc < kchunks; ++kc, ++gidx, dbh += KS * 2 / 16) {
             const uint32_t st = gidx & (kStages - 1);
             if (!wait_bar(&a_full[st], (gidx / kStages) & 1u, abort_flag)) {
               ok = false;
@@ -623,8 +652,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
             tc_fence_after();
             const uint32_t a_hi = tmem + (uint32_t)kACol + st * kKS;
             if (TWO)
-              mma_stage_ts2(d, a_hi, dbh, dbh + r8, dbh + 2, dbh + 2 + r8, idesc, gidx != 0,
-                            &a_empty[st]);
+              mma_stage64_ts2(d, a_hi, dbh, dbh + r8, idesc, gidx != 0, &a_empty[st]);
             else
               mma_stage_ts(d, a_hi, dbh, dbh + r8, dbh + 2, dbh + 2 + r8, idesc, gidx != 0,
                            &a_empty[st]);
@@ -1217,7 +1245,10 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   }
   const int li = level_index(P, w, h, level, J.g, off);
   J.krow = J.ws / J.g;
-  J.kpad = ((J.krow + kKS - 1) / kKS) * kKS;
+  {
+    const int ks = J.two_prod ? 2 * kKS : kKS;  // K per pipeline stage of the kernel variant
+    J.kpad = ((J.krow + ks - 1) / ks) * ks;
+  }
   J.nres = (ow + J.m - 1) / J.m;
   J.nb = ((J.nres + 15) / 16) * 16;
   if (J.nb > kNBMax) J.nb = kNBMax;
@@ -1342,10 +1373,14 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
   }
   // Unpaired tensor outputs of at most 32 rows: K interleave over the four
   // lane quarters.
+  // (The K interleave runs the 32 K hi/lo stages: such an output keeps three
+  // products; its kpad, a multiple of 64 if it had two, is still a multiple
+  // of 32.)
   for (auto& jp : P.jobs)
     if (jp.level >= 0 && !jp.narrow && !jp.paired && jp.pair_with < 0 && jp.J.ho <= 32) {
       jp.J.kinter = 4;
       jp.J.nparts = 4 * jp.J.ksplit;
+      jp.J.two_prod = 0;
     }
   P.total = off;
   return ALTHEA_IBL_OK;
