@@ -354,6 +354,13 @@ struct Job {
   // rows and owns every fourth K stage (stage slot q), so the weight work of
   // one quarter spreads over the four SM sub-partitions; each quarter's
   // partial sums are a split of their own (nparts = ksplit * kinter).
+  // Visible offsets: vis[tile * hs + j] = half-width (in phase-row units) of
+  // the window of column offsets around 0 where some output row of row tile
+  // `tile` sees source row j above its horizon (max(0, n.w) > 0); -1 when no
+  // row of the tile sees row j at all; >= krow when all offsets are needed.
+  // Outside the window every weight of the tile is exactly 0, so those K
+  // stages are skipped.  A margin of two texels covers the FP32 evaluation.
+  const int* vis;
   int kinter;                // 1 or 4
   int nparts;                // partial sums the finish adds: ksplit * kinter
   int pair;                  // 1: lanes 64-127 hold the second output
@@ -374,6 +381,23 @@ __host__ __device__ inline SmemPlan smem_plan(const Job& J) {
   p.cosd = p.slots + (size_t)J.nslots * 6 * J.rlen * 2;
   p.total = p.cosd + (size_t)J.g * J.kpad * 4;
   return p;
+}
+
+// K chunks (of ks) of a source row that hold visible offsets: [0, ca) and
+// [cb, kchunks), from the window half-width uh (see Job::vis).  The window is
+// |u| <= uh around the CTA's column shift sh < 8, i.e. k in [-uh, uh + 8)
+// modulo krow.
+__device__ __forceinline__ void visible_chunks(int uh, int krow, int ks, int kchunks, int& ca,
+                                               int& cb) {
+  if (uh < 0) {  // no row of the tile sees this source row
+    ca = 0;
+    cb = kchunks;
+  } else if (uh >= krow) {
+    ca = cb = kchunks;
+  } else {
+    ca = min(kchunks, (uh + 8 + ks - 1) / ks);
+    cb = max(ca, (krow - uh) / ks);
+  }
 }
 
 // The contraction kernel.  Grid: (ceil(ho/128), m * nblk, ksplit); each CTA
@@ -475,7 +499,14 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   constexpr int KW = KS / 4;   // K per producer warp and stage
   constexpr int NG = KW / 8;   // groups of 8 K per producer warp and stage
   const int kchunks = job.kpad / KS;
-  const long long total = (long long)nrows * job.g * kchunks;
+  // stages this CTA runs: the visible chunks of each of its source rows
+  const int* vis_row = job.vis + (size_t)blockIdx.x * job.hs;
+  long long total = 0;
+  for (int j = j0; j < j1; ++j) {
+    int ca, cb;
+    visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
+    total += (long long)job.g * (ca + kchunks - cb);
+  }
   const bool want_wsum = KIND == 0 && blockIdx.y == 0;
   const bool want_wsum_b = job.pair && job.kind_b == 0 && blockIdx.y == 0;
 
@@ -506,6 +537,9 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     int pending = -1;  // stage whose stores are issued but not yet published
     bool ok = true;
     for (int j = j0; live && j < j1 && ok; ++j) {
+      int ca, cb;
+      visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
+      const int nvis = ca + kchunks - cb;
       const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
       const float om = job.src_rows[3 * j + 2];
       const float ccq = cp * cq, ssq = sp_ * sq;
@@ -515,7 +549,8 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
       for (int ph = 0; ph < job.g && ok; ++ph) {
         const float* cdrow = cosd_sm + ph * job.kpad;
         float2 rowsum2 = make_float2(0.0f, 0.0f);
-        for (int kc = 0; kc < kchunks; ++kc, ++gidx) {
+        for (int v = 0; v < nvis; ++v, ++gidx) {
+          const int kc = v < ca ? v : cb + (v - ca);
           const int st = (int)(gidx & (kStages - 1));
           const uint32_t use = gidx / kStages;
           if (kint && st != q) continue;  // another quarter's stage
@@ -636,14 +671,20 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
       uint32_t gidx = 0, row_id = 0;
       bool ok = true;
       for (int j = j0; j < j1 && ok; ++j) {
+        int ca, cb;
+        visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
+        const int nvis = ca + kchunks - cb;
+        if (nvis == 0) continue;  // not staged by the loader either
         for (int ph = 0; ph < job.g && ok; ++ph, ++row_id) {
           const uint32_t slot = row_id % (uint32_t)job.nslots;
           if (!wait_bar(&slot_full[slot], (row_id / (uint32_t)job.nslots) & 1u, abort_flag)) {
             ok = false;
             break;
           }
-          uint64_t dbh = bdesc0 + (uint64_t)(slot * slot16 + plane16);
-          for (int kc = 0; kc < kchunks; ++kc, ++gidx, dbh += KS * 2 / 16) {
+          const uint64_t dbh_row = bdesc0 + (uint64_t)(slot * slot16 + plane16);
+          for (int v = 0; v < nvis; ++v, ++gidx) {
+            const int kc = v < ca ? v : cb + (v - ca);
+            const uint64_t dbh = dbh_row + (uint64_t)(kc * (KS * 2 / 16));
             const uint32_t st = gidx & (kStages - 1);
             if (!wait_bar(&a_full[st], (gidx / kStages) & 1u, abort_flag)) {
               ok = false;
@@ -656,8 +697,9 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
             else
               mma_stage_ts(d, a_hi, dbh, dbh + r8, dbh + 2, dbh + 2 + r8, idesc, gidx != 0,
                            &a_empty[st]);
-            if (kc == kchunks - 1) mma_commit(&slot_empty[slot]);
           }
+          // the row's slot is free once its MMAs are done
+          if (ok) mma_commit(&slot_empty[slot]);
         }
       }
       // every MMA issued by all issuers has completed before the accumulators
@@ -676,6 +718,9 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     long long row_id = 0;
     bool ok = true;
     for (int j = j0; j < j1 && ok; ++j) {
+      int ca, cb;
+      visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
+      if (ca + kchunks - cb == 0) continue;  // no visible offset: the row is not staged
       for (int ph = 0; ph < job.g && ok; ++ph, ++row_id) {
         const int slot = (int)(row_id % job.nslots);
         const long long use = row_id / job.nslots;
@@ -941,7 +986,39 @@ struct TableArgs {
   float* cosd[kMaxTcJobs];
   float* srows[kMaxTcJobs];
   float* orows[kMaxTcJobs];
+  // visible-offset windows (tensor jobs only; vis null otherwise): row tiles of
+  // kM rows, or one tile holding rows 0..ho-1 and a paired second output's
+  // rows 0..ho_b-1
+  int* vis[kMaxTcJobs];
+  int ntiles[kMaxTcJobs], ho_b[kMaxTcJobs], g[kMaxTcJobs], krow[kMaxTcJobs];
 };
+
+// Half-width of the visible offset window for output rows [ia, ib] (texel
+// corners of an ho-row output) against source row q.  c = cos p cos q cos D +
+// sin p sin q > 0 needs cos D > X = -tan p tan q.  The kernels evaluate c in
+// FP32 from FP32 tables, within about 4 2^-24 (cos p cos q + |sin p sin q|)
+// of its value, so a weight can come out positive wherever cos D >
+// X' = X - 1e-6 (1 + |X|).  X' grows with X and X is monotonic in p, so the
+// tile's end rows bound it.  The window |t + 0.5| <= T = acos(X') ws / 2 pi
+// (+ 2 texels) in phase-row units u (t = g u + ph).  -1: X' > 1 for every
+// row (every weight of the tile for this source row is exactly 0); >= krow:
+// every offset.
+__device__ int visible_halfwidth(double q, int ia, int ib, int ho, int ws, int g, int krow) {
+  const double pi = 3.14159265358979323846;
+  double xmin = 1e300;
+  for (int e = 0; e < 2; ++e) {
+    const int i = e ? ib : ia;
+    const double p = pi * ((double)i / ho - 0.5);
+    const double den = cos(p) * cos(q);  // > 0 (cos p = 6e-17 at a pole corner)
+    xmin = fmin(xmin, -(sin(p) * sin(q)) / den);
+  }
+  xmin -= 1e-6 * (1.0 + fabs(xmin));
+  if (xmin > 1.0) return -1;
+  const double a = acos(fmax(-1.0, xmin));
+  const double T = a * ws / (2.0 * pi) + 2.0;  // texels, two-texel margin
+  const double uh = ceil((T + 0.5 + g) / g) + 1.0;
+  return uh * 2.0 + 8.0 >= (double)krow ? krow : (int)uh;
+}
 
 __global__ void tables_kernel(const TableArgs a) {
   const double pi = 3.14159265358979323846;
@@ -960,6 +1037,19 @@ __global__ void tables_kernel(const TableArgs a) {
     double p = pi * ((double)t / ho - 0.5);
     a.orows[jb][2 * t] = (float)cos(p);
     a.orows[jb][2 * t + 1] = (float)sin(p);
+  }
+  if (t < hs && a.vis[jb]) {
+    const double q = pi * ((t + 0.5) / hs - 0.5);
+    for (int tile = 0; tile < a.ntiles[jb]; ++tile) {
+      const int ia = tile * kM, ib = min(ho, ia + kM) - 1;
+      int uh = visible_halfwidth(q, ia, ib, ho, ws, a.g[jb], a.krow[jb]);
+      if (a.ho_b[jb] > 0) {  // a pair: the union with the second output's rows
+        const int ub = visible_halfwidth(q, 0, a.ho_b[jb] - 1, a.ho_b[jb], ws, a.g[jb],
+                                         a.krow[jb]);
+        uh = max(uh, ub);
+      }
+      a.vis[jb][(size_t)tile * hs + t] = uh;
+    }
   }
 }
 
@@ -1018,97 +1108,128 @@ __global__ void rows_kernel(const RowsArgs a) {
   }
 }
 
-// Sum the K splits (FP32, fixed order), normalise by the FP64 weight sum,
-// write RGBA32F.  Block per (32 output rows, one column); warp w sums the
-// splits k = w mod 8 with the lanes on consecutive rows (the partial layout),
-// then warp 0 combines the eight in order.  FP64 is used only for the weight
-// sums and the final normalisation.
-__device__ __forceinline__ void finish_block(const Job& job, void* __restrict__ out,
-                                             long long pitch, int bx, int by) {
-  __shared__ float red[8][3][32];
-  __shared__ double redw[8][32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = bx * 32 + lane, x = by;
-  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
-  double sw = 0.0;
-  if (i < job.ho) {
-    // Four splits' loads in flight at a time; the sums keep the order k = w,
-    // w + 8, w + 16, ...
-    const size_t plane = (size_t)job.wo * job.ho;
-    constexpr int kU = 4;
-    for (int k0 = w; k0 < job.nparts; k0 += 8 * kU) {
-      float v0[kU], v1[kU], v2[kU];
-      double vw[kU];
-#pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        const int k = k0 + 8 * u;
-        v0[u] = v1[u] = v2[u] = 0.0f;
-        vw[u] = 0.0;
-        if (k < job.nparts) {
-          const float* p = job.partial + (((size_t)k * 3) * job.wo + x) * job.ho + i;
-          v0[u] = p[0];
-          v1[u] = p[plane];
-          v2[u] = p[2 * plane];
-          if (job.kind == 0) vw[u] = job.wsum_part[(size_t)k * job.ho + i];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        if (k0 + 8 * u < job.nparts) {
-          s0 += v0[u];
-          s1 += v1[u];
-          s2 += v2[u];
-          sw += vw[u];
-        }
-      }
-    }
-  }
-  red[w][0][lane] = s0;
-  red[w][1][lane] = s1;
-  red[w][2][lane] = s2;
-  redw[w][lane] = sw;
-  __syncthreads();
-  if (w == 0 && i < job.ho) {
-    float t0 = 0.0f, t1 = 0.0f, t2 = 0.0f;
-    double tw = 0.0;
-    for (int ww = 0; ww < 8; ++ww) {
-      t0 += red[ww][0][lane];
-      t1 += red[ww][1][lane];
-      t2 += red[ww][2][lane];
-      tw += redw[ww][lane];
-    }
-    const double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / tw);
-    const float r = (float)(t0 * norm), g = (float)(t1 * norm), b = (float)(t2 * norm);
-    if (job.out_half) {
-      const __half2 rg = __floats2half2_rn(r, g), ba = __floats2half2_rn(b, 1.0f);
-      uint2 v;
-      v.x = *reinterpret_cast<const uint32_t*>(&rg);
-      v.y = *reinterpret_cast<const uint32_t*>(&ba);
-      reinterpret_cast<uint2*>(out)[(long long)i * pitch + x] = v;
-    } else {
-      reinterpret_cast<float4*>(out)[(long long)i * pitch + x] = make_float4(r, g, b, 1.0f);
-    }
+// Sum the K splits (FP32, in ascending split order), normalise by the FP64
+// weight sum, write RGBA32F or RGBA16F.  One thread per (four consecutive
+// output rows, one column): the partial sums are [split][channel][x][row],
+// rows fastest, so a warp reads 32 x 16 contiguous bytes per (split,
+// channel) with float4 loads, and each thread keeps the loads of four splits
+// (12 x 16 bytes, plus the weight sums) in flight.  Rows of outputs whose
+// height is not a multiple of 4 are read one by one.  FP64 is used only for
+// the weight sums and the final normalisation.
+constexpr int kFinishRows = 4;   // output rows per thread
+constexpr int kFinishThreads = 256;
+
+__device__ __forceinline__ void store_texel(void* out, long long pitch, int i, int x, int half,
+                                            float r, float g, float b) {
+  if (half) {
+    const __half2 rg = __floats2half2_rn(r, g), ba = __floats2half2_rn(b, 1.0f);
+    uint2 v;
+    v.x = *reinterpret_cast<const uint32_t*>(&rg);
+    v.y = *reinterpret_cast<const uint32_t*>(&ba);
+    reinterpret_cast<uint2*>(out)[(long long)i * pitch + x] = v;
+  } else {
+    reinterpret_cast<float4*>(out)[(long long)i * pitch + x] = make_float4(r, g, b, 1.0f);
   }
 }
 
-// Every tensor job's finish in one launch: block b belongs to the job k with
-// begin[k] <= b < begin[k + 1] and covers (32 rows, one column) of it.
+__device__ __forceinline__ void finish_quad(const Job& job, void* __restrict__ out,
+                                            long long pitch, int quad, int x) {
+  const int i0 = quad * kFinishRows;
+  const size_t plane = (size_t)job.wo * job.ho;
+  const bool vec = (job.ho % kFinishRows) == 0;
+  float s[3][kFinishRows];
+  double sw[kFinishRows];
+#pragma unroll
+  for (int r = 0; r < kFinishRows; ++r) {
+    s[0][r] = s[1][r] = s[2][r] = 0.0f;
+    sw[r] = 0.0;
+  }
+  const float* base = job.partial + (size_t)x * job.ho + i0;
+  if (vec) {
+    constexpr int kU = 4;
+    for (int k0 = 0; k0 < job.nparts; k0 += kU) {
+      float4 v[kU][3];
+      double2 wv[kU][2];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int k = k0 + u;
+        if (k < job.nparts) {
+          const float* p = base + (size_t)k * 3 * plane;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) v[u][c] = *reinterpret_cast<const float4*>(p + c * plane);
+          if (job.kind == 0) {
+            const double* wp = job.wsum_part + (size_t)k * job.ho + i0;
+            wv[u][0] = *reinterpret_cast<const double2*>(wp);
+            wv[u][1] = *reinterpret_cast<const double2*>(wp + 2);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (k0 + u < job.nparts) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            s[c][0] += v[u][c].x;
+            s[c][1] += v[u][c].y;
+            s[c][2] += v[u][c].z;
+            s[c][3] += v[u][c].w;
+          }
+          if (job.kind == 0) {
+            sw[0] += wv[u][0].x;
+            sw[1] += wv[u][0].y;
+            sw[2] += wv[u][1].x;
+            sw[3] += wv[u][1].y;
+          }
+        }
+      }
+    }
+  } else {
+    for (int k = 0; k < job.nparts; ++k) {
+      const float* p = base + (size_t)k * 3 * plane;
+#pragma unroll
+      for (int r = 0; r < kFinishRows; ++r) {
+        if (i0 + r < job.ho) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) s[c][r] += p[c * plane + r];
+          if (job.kind == 0) sw[r] += job.wsum_part[(size_t)k * job.ho + i0 + r];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < kFinishRows; ++r) {
+    if (i0 + r >= job.ho) break;
+    const double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / sw[r]);
+    store_texel(out, pitch, i0 + r, x, job.out_half, (float)(s[0][r] * norm),
+                (float)(s[1][r] * norm), (float)(s[2][r] * norm));
+  }
+}
+
+// Every tensor job's finish in one launch: thread t belongs to the job k with
+// begin[k] <= t < begin[k + 1] and covers (four rows, one column) of it.
 constexpr int kMaxFinishJobs = ALTHEA_IBL_MAX_MIPS + 1;
 struct FinishArgs {
   Job job[kMaxFinishJobs];
   void* out[kMaxFinishJobs];
   long long pitch[kMaxFinishJobs];
-  int begin[kMaxFinishJobs + 1];
+  long long begin[kMaxFinishJobs + 1];
   int n;
 };
 
-__global__ void __launch_bounds__(256) finish_all_kernel(const __grid_constant__ FinishArgs a) {
-  const int b = blockIdx.x;
+__device__ __forceinline__ long long finish_threads(const Job& J) {
+  return (long long)((J.ho + kFinishRows - 1) / kFinishRows) * J.wo;
+}
+
+__global__ void __launch_bounds__(kFinishThreads) finish_all_kernel(
+    const __grid_constant__ FinishArgs a) {
+  const long long t = (long long)blockIdx.x * kFinishThreads + threadIdx.x;
+  if (t >= a.begin[a.n]) return;
   int k = 0;
-  while (k + 1 < a.n && b >= a.begin[k + 1]) ++k;
+  while (k + 1 < a.n && t >= a.begin[k + 1]) ++k;
   const Job& J = a.job[k];
-  const int local = b - a.begin[k], nbx = (J.ho + 31) / 32;
-  finish_block(J, a.out[k], a.pitch[k], local % nbx, local / nbx);
+  const long long local = t - a.begin[k];
+  const int quads = (J.ho + kFinishRows - 1) / kFinishRows;
+  finish_quad(J, a.out[k], a.pitch[k], (int)(local % quads), (int)(local / quads));
 }
 
 }  // namespace tc
@@ -1163,7 +1284,7 @@ struct JobPlan {
   int pair_with = -1;   // a second job run in this job's lanes 64-127
   bool paired = false;  // this job runs inside another's launch (finish only)
   size_t cosd_off = 0, rows_off = 0, orows_off = 0, partial_off = 0,
-         wsum_off = 0;
+         wsum_off = 0, vis_off = 0;
 };
 
 struct TcPlan {
@@ -1302,6 +1423,8 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   off = al256(off + (size_t)parts * 3 * ow * oh * 4);
   jp.wsum_off = off;
   off = al256(off + (size_t)parts * oh * 8);
+  jp.vis_off = off;  // one window per (row tile, source row)
+  off = al256(off + (size_t)((oh + kM - 1) / kM) * J.hs * 4);
   P.jobs.push_back(jp);
   return ALTHEA_IBL_OK;
 }
@@ -1488,6 +1611,14 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
       ta.cosd[nt] = const_cast<float*>(J.cos_d);
       ta.srows[nt] = const_cast<float*>(J.src_rows);
       ta.orows[nt] = const_cast<float*>(J.out_rows);
+      if (!jp.narrow && !jp.paired) {  // a tensor launch: its visible-offset windows
+        J.vis = reinterpret_cast<const int*>(base + jp.vis_off);
+        ta.vis[nt] = const_cast<int*>(J.vis);
+        ta.ntiles[nt] = (J.ho + kM - 1) / kM;
+        ta.ho_b[nt] = jp.pair_with >= 0 ? P.jobs[jp.pair_with].J.ho : 0;
+        ta.g[nt] = J.g;
+        ta.krow[nt] = J.krow;
+      }
       nmax = std::max(nmax, std::max(J.ws, std::max(J.hs, J.ho)));
       ++nt;
     }
@@ -1507,7 +1638,7 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
   static_assert(sizeof(FinishArgs) <= 32000, "finish arguments fit the kernel parameter space");
   FinishArgs fa;
   memset(&fa, 0, sizeof(fa));
-  int finish_blocks = 0;
+  long long finish_threads_total = 0;
   for (size_t k = 0; k < P.jobs.size(); ++k) {
     JobPlan& jp = P.jobs[k];
     void* out = nullptr;
@@ -1569,8 +1700,8 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     fa.job[fa.n] = J;
     fa.out[fa.n] = out;
     fa.pitch[fa.n] = pitch;
-    fa.begin[fa.n] = finish_blocks;
-    finish_blocks += ((J.ho + 31) / 32) * J.wo;
+    fa.begin[fa.n] = finish_threads_total;
+    finish_threads_total += (long long)((J.ho + kFinishRows - 1) / kFinishRows) * J.wo;
     ++fa.n;
     if (jp.paired) continue;  // contracted inside its partner's launch
     J.pair = 0;
@@ -1597,8 +1728,10 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     if (e != cudaSuccess) return cuda_status(e, "tc contraction launch");
   }
   if (fa.n > 0) {
-    fa.begin[fa.n] = finish_blocks;
-    finish_all_kernel<<<finish_blocks, 256, 0, s>>>(fa);
+    fa.begin[fa.n] = finish_threads_total;
+    const unsigned blocks =
+        (unsigned)((finish_threads_total + kFinishThreads - 1) / kFinishThreads);
+    finish_all_kernel<<<blocks, kFinishThreads, 0, s>>>(fa);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "tc finish launch");
   }
