@@ -352,8 +352,8 @@ struct Job {
   // M = 128 tile: they share every radiance operand, only the weights differ.
   // K interleave (outputs of <= 32 rows): every lane quarter holds the same
   // rows and owns every fourth K stage (stage slot q), so the weight work of
-  // one quarter spreads over the four SM sub-partitions; each quarter's
-  // partial sums are a split of their own (nparts = ksplit * kinter).
+  // one quarter spreads over the four SM sub-partitions; the CTA adds the
+  // quarters' sums before writing one partial per split.
   // Visible offsets: vis[tile * hs + j] = half-width (in phase-row units) of
   // the window of column offsets around 0 where some output row of row tile
   // `tile` sees source row j above its horizon (max(0, n.w) > 0); -1 when no
@@ -362,7 +362,7 @@ struct Job {
   // stages are skipped.  A margin of two texels covers the FP32 evaluation.
   const int* vis;
   int kinter;                // 1 or 4
-  int nparts;                // partial sums the finish adds: ksplit * kinter
+  int nparts;                // partial sums the finish adds: ksplit
   int pair;                  // 1: lanes 64-127 hold the second output
   int ho_b, kind_b;
   float a2_b;
@@ -387,16 +387,17 @@ __host__ __device__ inline SmemPlan smem_plan(const Job& J) {
 // [cb, kchunks), from the window half-width uh (see Job::vis).  The window is
 // |u| <= uh around the CTA's column shift sh < 8, i.e. k in [-uh, uh + 8)
 // modulo krow.
-__device__ __forceinline__ void visible_chunks(int uh, int krow, int ks, int kchunks, int& ca,
-                                               int& cb) {
+__host__ __device__ __forceinline__ void visible_chunks(int uh, int krow, int ks, int kchunks,
+                                                        int& ca, int& cb) {
   if (uh < 0) {  // no row of the tile sees this source row
     ca = 0;
     cb = kchunks;
   } else if (uh >= krow) {
     ca = cb = kchunks;
   } else {
-    ca = min(kchunks, (uh + 8 + ks - 1) / ks);
-    cb = max(ca, (krow - uh) / ks);
+    const int a = (uh + 8 + ks - 1) / ks, b = (krow - uh) / ks;
+    ca = a < kchunks ? a : kchunks;
+    cb = b > ca ? b : ca;
   }
 }
 
@@ -490,10 +491,10 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     tc_fence_after();
   }
 
-  const int j_per = (job.hs + job.ksplit - 1) / job.ksplit;
-  const int j0 = split * j_per;
-  const int j1 = min(job.hs, j0 + j_per);
-  const int nrows = j1 > j0 ? j1 - j0 : 0;
+  // This CTA's source rows: j = split, split + ksplit, ... (round robin, so
+  // every split holds the same mix of latitudes and the visible-offset
+  // windows cost every CTA about the same).
+  const int jstep = job.ksplit;
   // K per pipeline stage: 64 with hi-only weights (two products), else 32
   constexpr int KS = TWO ? 64 : kKS;
   constexpr int KW = KS / 4;   // K per producer warp and stage
@@ -502,7 +503,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   // stages this CTA runs: the visible chunks of each of its source rows
   const int* vis_row = job.vis + (size_t)blockIdx.x * job.hs;
   long long total = 0;
-  for (int j = j0; j < j1; ++j) {
+  for (int j = split; j < job.hs; j += jstep) {
     int ca, cb;
     visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
     total += (long long)job.g * (ca + kchunks - cb);
@@ -536,7 +537,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     uint32_t gidx = 0;
     int pending = -1;  // stage whose stores are issued but not yet published
     bool ok = true;
-    for (int j = j0; live && j < j1 && ok; ++j) {
+    for (int j = split; live && j < job.hs && ok; j += jstep) {
       int ca, cb;
       visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
       const int nvis = ca + kchunks - cb;
@@ -670,7 +671,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
       const uint32_t slot16 = 6u * r8;
       uint32_t gidx = 0, row_id = 0;
       bool ok = true;
-      for (int j = j0; j < j1 && ok; ++j) {
+      for (int j = split; j < job.hs && ok; j += jstep) {
         int ca, cb;
         visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
         const int nvis = ca + kchunks - cb;
@@ -717,7 +718,7 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     const int u0 = (8 * n0) % job.krow;
     long long row_id = 0;
     bool ok = true;
-    for (int j = j0; j < j1 && ok; ++j) {
+    for (int j = split; j < job.hs && ok; j += jstep) {
       int ca, cb;
       visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
       if (ca + kchunks - cb == 0) continue;  // no visible offset: the row is not staged
@@ -760,16 +761,49 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   const bool failed = abort_sh != 0;
   if (failed) {
     if (tid == 0) atomicExch(job.error, 1);
+  } else if (kint) {
+    // K interleave: the four lane quarters hold the same output rows and
+    // every fourth K stage.  Their sums are added here, in quarter order, so
+    // one partial sum per split is written (shared memory is free again: the
+    // loader has seen its last copy land).
+    const int ncol = 3 * job.nb;
+    float* red = reinterpret_cast<float*>(smem);  // [quarter][column][lane]
+    if (warp < kProducerWarps) {
+      const int q = warp & 3;
+      for (int c0 = 16 * (warp >> 2); c0 < ncol; c0 += 16 * (kProducerWarps / 4)) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+#pragma unroll
+        for (int u = 0; u < 16; ++u) red[((size_t)q * ncol + c0 + u) * 32 + lane] = v[u];
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < ncol * 32; e += kThreads) {
+      const int col = e >> 5, r = e & 31, ch = col / job.nb, n = col - ch * job.nb;
+      const int x = x0 + job.m * (n0 + n);
+      if (r < job.ho && n0 + n < job.nres && x < job.wo) {
+        const size_t c = (size_t)col * 32 + r, qs = (size_t)ncol * 32;
+        const float sum = ((red[c] + red[qs + c]) + red[2 * qs + c]) + red[3 * qs + c];
+        job.partial[(((size_t)split * 3 + ch) * job.wo + x) * job.ho + r] =
+            total > 0 ? sum : 0.0f;
+      }
+    }
+    if (tid < 32 && want_wsum && tid < job.ho) {
+      double ws = 0.0;
+      for (int q = 0; q < 4; ++q)
+        for (int hh = 0; hh < kProducerWarps / 4; ++hh) ws += wsum_sh[hh][32 * q + tid];
+      job.wsum_part[(size_t)split * job.ho + tid] = ws;
+    }
   } else {
     const int q = warp & 3;
     if (warp < kProducerWarps && quarter_live(q)) {
       // accumulators -> partial sums (lane = output row, column = (channel, n));
       // the four warps of a lane quarter take every fourth 16-column chunk
       const bool second = job.pair && q >= 2;
-      const int gi = kint ? lane : (second ? 32 * (q - 2) + lane : i0 + 32 * q + lane);
+      const int gi = second ? 32 * (q - 2) + lane : i0 + 32 * q + lane;
       const int ho_here = second ? job.ho_b : job.ho;
       float* part = second ? job.partial_b : job.partial;
-      const int slot_split = kint ? split * job.kinter + q : split;
+      const int slot_split = split;
       for (int c0 = 16 * (warp >> 2); c0 < 3 * job.nb; c0 += 16 * (kProducerWarps / 4)) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
@@ -785,8 +819,8 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
     }
     if (tid < kM) {
       const bool second = job.pair && tid >= 64;
-      const int gi = kint ? (tid & 31) : (second ? tid - 64 : i0 + tid);
-      const int slot_split = kint ? split * job.kinter + (tid >> 5) : split;
+      const int gi = second ? tid - 64 : i0 + tid;
+      const int slot_split = split;
       if (second ? (want_wsum_b && gi < job.ho_b) : (want_wsum && gi < job.ho)) {
         double ws = 0.0;
         for (int hh = 0; hh < kProducerWarps / 4; ++hh) ws += wsum_sh[hh][tid];
@@ -992,6 +1026,7 @@ struct TableArgs {
   int* vis[kMaxTcJobs];
   int ntiles[kMaxTcJobs], ho_b[kMaxTcJobs], g[kMaxTcJobs], krow[kMaxTcJobs];
 };
+constexpr int kMaxTiles = 512;  // row tiles of an output (65536 rows / kM)
 
 // Half-width of the visible offset window for output rows [ia, ib] (texel
 // corners of an ho-row output) against source row q.  c = cos p cos q cos D +
@@ -1003,21 +1038,26 @@ struct TableArgs {
 // (+ 2 texels) in phase-row units u (t = g u + ph).  -1: X' > 1 for every
 // row (every weight of the tile for this source row is exactly 0); >= krow:
 // every offset.
-__device__ int visible_halfwidth(double q, int ia, int ib, int ho, int ws, int g, int krow) {
+__host__ __device__ inline int visible_halfwidth_sc(double sq, double cq, double spa,
+                                                    double cpa, double spb, double cpb, int ws,
+                                                    int g, int krow) {
   const double pi = 3.14159265358979323846;
-  double xmin = 1e300;
-  for (int e = 0; e < 2; ++e) {
-    const int i = e ? ib : ia;
-    const double p = pi * ((double)i / ho - 0.5);
-    const double den = cos(p) * cos(q);  // > 0 (cos p = 6e-17 at a pole corner)
-    xmin = fmin(xmin, -(sin(p) * sin(q)) / den);
-  }
+  // X = -tan p tan q at the two end rows (cos p = 6e-17 at a pole corner: finite)
+  double xmin = fmin(-(spa * sq) / (cpa * cq), -(spb * sq) / (cpb * cq));
   xmin -= 1e-6 * (1.0 + fabs(xmin));
   if (xmin > 1.0) return -1;
   const double a = acos(fmax(-1.0, xmin));
   const double T = a * ws / (2.0 * pi) + 2.0;  // texels, two-texel margin
   const double uh = ceil((T + 0.5 + g) / g) + 1.0;
   return uh * 2.0 + 8.0 >= (double)krow ? krow : (int)uh;
+}
+
+// The same from the rows' indices (the host-side planning statistics).
+__host__ __device__ inline int visible_halfwidth(double q, int ia, int ib, int ho, int ws, int g,
+                                                 int krow) {
+  const double pi = 3.14159265358979323846;
+  const double pa = pi * ((double)ia / ho - 0.5), pb = pi * ((double)ib / ho - 0.5);
+  return visible_halfwidth_sc(sin(q), cos(q), sin(pa), cos(pa), sin(pb), cos(pb), ws, g, krow);
 }
 
 __global__ void tables_kernel(const TableArgs a) {
@@ -1038,16 +1078,35 @@ __global__ void tables_kernel(const TableArgs a) {
     a.orows[jb][2 * t] = (float)cos(p);
     a.orows[jb][2 * t + 1] = (float)sin(p);
   }
-  if (t < hs && a.vis[jb]) {
-    const double q = pi * ((t + 0.5) / hs - 0.5);
-    for (int tile = 0; tile < a.ntiles[jb]; ++tile) {
+  if (!a.vis[jb]) return;
+  // sin and cos of the tiles' end rows, once per block: [tile][end][sin, cos];
+  // the entry after the last tile is a pair's second output
+  __shared__ double endrows[kMaxTiles + 1][2][2];
+  const int ntiles = a.ntiles[jb];
+  for (int e = threadIdx.x; e < 2 * (ntiles + 1); e += blockDim.x) {
+    const int tile = e >> 1, end = e & 1;
+    double p;
+    if (tile < ntiles) {
       const int ia = tile * kM, ib = min(ho, ia + kM) - 1;
-      int uh = visible_halfwidth(q, ia, ib, ho, ws, a.g[jb], a.krow[jb]);
-      if (a.ho_b[jb] > 0) {  // a pair: the union with the second output's rows
-        const int ub = visible_halfwidth(q, 0, a.ho_b[jb] - 1, a.ho_b[jb], ws, a.g[jb],
-                                         a.krow[jb]);
-        uh = max(uh, ub);
-      }
+      p = pi * ((double)(end ? ib : ia) / ho - 0.5);
+    } else {
+      const int hb = a.ho_b[jb] > 0 ? a.ho_b[jb] : 1;
+      p = pi * ((double)(end ? hb - 1 : 0) / hb - 0.5);
+    }
+    endrows[tile][end][0] = sin(p);
+    endrows[tile][end][1] = cos(p);
+  }
+  __syncthreads();
+  if (t < hs) {
+    const double q = pi * ((t + 0.5) / hs - 0.5), sq = sin(q), cq = cos(q);
+    for (int tile = 0; tile < ntiles; ++tile) {
+      int uh = visible_halfwidth_sc(sq, cq, endrows[tile][0][0], endrows[tile][0][1],
+                                    endrows[tile][1][0], endrows[tile][1][1], ws, a.g[jb],
+                                    a.krow[jb]);
+      if (a.ho_b[jb] > 0)  // a pair: the union with the second output's rows
+        uh = max(uh, visible_halfwidth_sc(sq, cq, endrows[ntiles][0][0], endrows[ntiles][0][1],
+                                          endrows[ntiles][1][0], endrows[ntiles][1][1], ws,
+                                          a.g[jb], a.krow[jb]));
       a.vis[jb][(size_t)tile * hs + t] = uh;
     }
   }
@@ -1108,16 +1167,17 @@ __global__ void rows_kernel(const RowsArgs a) {
   }
 }
 
-// Sum the K splits (FP32, in ascending split order), normalise by the FP64
-// weight sum, write RGBA32F or RGBA16F.  One thread per (four consecutive
-// output rows, one column): the partial sums are [split][channel][x][row],
-// rows fastest, so a warp reads 32 x 16 contiguous bytes per (split,
-// channel) with float4 loads, and each thread keeps the loads of four splits
-// (12 x 16 bytes, plus the weight sums) in flight.  Rows of outputs whose
+// Sum the K splits (FP32, fixed order), normalise by the FP64 weight sum,
+// write RGBA32F or RGBA16F.  A block of 8 warps covers 32 slots of four
+// consecutive output rows (slot = (column, row quad), quads fastest: the
+// partial sums are [split][channel][x][row], rows fastest, so a warp reads
+// contiguous float4s); warp w adds the splits k = w, w + 8, ... (two in
+// flight), and warp 0 combines the eight in order.  Rows of outputs whose
 // height is not a multiple of 4 are read one by one.  FP64 is used only for
 // the weight sums and the final normalisation.
-constexpr int kFinishRows = 4;   // output rows per thread
-constexpr int kFinishThreads = 256;
+constexpr int kFinishRows = 4;   // output rows per slot
+constexpr int kFinishWarps = 8;
+constexpr int kFinishThreads = 32 * kFinishWarps;
 
 __device__ __forceinline__ void store_texel(void* out, long long pitch, int i, int x, int half,
                                             float r, float g, float b) {
@@ -1132,8 +1192,15 @@ __device__ __forceinline__ void store_texel(void* out, long long pitch, int i, i
   }
 }
 
-__device__ __forceinline__ void finish_quad(const Job& job, void* __restrict__ out,
-                                            long long pitch, int quad, int x) {
+__device__ __forceinline__ void finish_block(const Job& job, void* __restrict__ out,
+                                             long long pitch, long long slot0) {
+  __shared__ float red[kFinishWarps][3][kFinishRows][32];
+  __shared__ double redw[kFinishWarps][kFinishRows][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int quads = (job.ho + kFinishRows - 1) / kFinishRows;
+  const long long slot = slot0 + lane;
+  const bool live = slot < (long long)quads * job.wo;
+  const int x = live ? (int)(slot / quads) : 0, quad = live ? (int)(slot % quads) : 0;
   const int i0 = quad * kFinishRows;
   const size_t plane = (size_t)job.wo * job.ho;
   const bool vec = (job.ho % kFinishRows) == 0;
@@ -1145,14 +1212,14 @@ __device__ __forceinline__ void finish_quad(const Job& job, void* __restrict__ o
     sw[r] = 0.0;
   }
   const float* base = job.partial + (size_t)x * job.ho + i0;
-  if (vec) {
-    constexpr int kU = 4;
-    for (int k0 = 0; k0 < job.nparts; k0 += kU) {
+  if (live && vec) {
+    constexpr int kU = 2;
+    for (int k0 = w; k0 < job.nparts; k0 += kU * kFinishWarps) {
       float4 v[kU][3];
       double2 wv[kU][2];
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
-        const int k = k0 + u;
+        const int k = k0 + u * kFinishWarps;
         if (k < job.nparts) {
           const float* p = base + (size_t)k * 3 * plane;
 #pragma unroll
@@ -1166,7 +1233,7 @@ __device__ __forceinline__ void finish_quad(const Job& job, void* __restrict__ o
       }
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
-        if (k0 + u < job.nparts) {
+        if (k0 + u * kFinishWarps < job.nparts) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             s[c][0] += v[u][c].x;
@@ -1183,8 +1250,8 @@ __device__ __forceinline__ void finish_quad(const Job& job, void* __restrict__ o
         }
       }
     }
-  } else {
-    for (int k = 0; k < job.nparts; ++k) {
+  } else if (live) {
+    for (int k = w; k < job.nparts; k += kFinishWarps) {
       const float* p = base + (size_t)k * 3 * plane;
 #pragma unroll
       for (int r = 0; r < kFinishRows; ++r) {
@@ -1198,38 +1265,46 @@ __device__ __forceinline__ void finish_quad(const Job& job, void* __restrict__ o
   }
 #pragma unroll
   for (int r = 0; r < kFinishRows; ++r) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) red[w][c][r][lane] = s[c][r];
+    redw[w][r][lane] = sw[r];
+  }
+  __syncthreads();
+  if (w != 0 || !live) return;
+#pragma unroll
+  for (int r = 0; r < kFinishRows; ++r) {
     if (i0 + r >= job.ho) break;
-    const double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / sw[r]);
-    store_texel(out, pitch, i0 + r, x, job.out_half, (float)(s[0][r] * norm),
-                (float)(s[1][r] * norm), (float)(s[2][r] * norm));
+    float t0 = 0.0f, t1 = 0.0f, t2 = 0.0f;
+    double tw = 0.0;
+    for (int ww = 0; ww < kFinishWarps; ++ww) {
+      t0 += red[ww][0][r][lane];
+      t1 += red[ww][1][r][lane];
+      t2 += red[ww][2][r][lane];
+      tw += redw[ww][r][lane];
+    }
+    const double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / tw);
+    store_texel(out, pitch, i0 + r, x, job.out_half, (float)(t0 * norm), (float)(t1 * norm),
+                (float)(t2 * norm));
   }
 }
 
-// Every tensor job's finish in one launch: thread t belongs to the job k with
-// begin[k] <= t < begin[k + 1] and covers (four rows, one column) of it.
+// Every tensor job's finish in one launch: block b belongs to the job k with
+// begin[k] <= b < begin[k + 1] and covers 32 slots (four rows, one column) of it.
 constexpr int kMaxFinishJobs = ALTHEA_IBL_MAX_MIPS + 1;
 struct FinishArgs {
   Job job[kMaxFinishJobs];
   void* out[kMaxFinishJobs];
   long long pitch[kMaxFinishJobs];
-  long long begin[kMaxFinishJobs + 1];
+  int begin[kMaxFinishJobs + 1];
   int n;
 };
 
-__device__ __forceinline__ long long finish_threads(const Job& J) {
-  return (long long)((J.ho + kFinishRows - 1) / kFinishRows) * J.wo;
-}
-
 __global__ void __launch_bounds__(kFinishThreads) finish_all_kernel(
     const __grid_constant__ FinishArgs a) {
-  const long long t = (long long)blockIdx.x * kFinishThreads + threadIdx.x;
-  if (t >= a.begin[a.n]) return;
+  const int b = blockIdx.x;
   int k = 0;
-  while (k + 1 < a.n && t >= a.begin[k + 1]) ++k;
-  const Job& J = a.job[k];
-  const long long local = t - a.begin[k];
-  const int quads = (J.ho + kFinishRows - 1) / kFinishRows;
-  finish_quad(J, a.out[k], a.pitch[k], (int)(local % quads), (int)(local / quads));
+  while (k + 1 < a.n && b >= a.begin[k + 1]) ++k;
+  finish_block(a.job[k], a.out[k], a.pitch[k], (long long)(b - a.begin[k]) * 32);
 }
 
 }  // namespace tc
@@ -1410,8 +1485,8 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   J.ksplit = ks;
   J.kinter = 1;
   J.nparts = ks;
-  // room for a K interleave (the plan decides after pairing)
-  const int parts = oh <= 32 ? 4 * ks : ks;
+  // one partial sum per split (a K interleave adds its quarters in the CTA)
+  const int parts = ks;
   jp.level = li;
   jp.cosd_off = off;
   off = al256(off + (size_t)J.ws * 4);
@@ -1502,7 +1577,7 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
   for (auto& jp : P.jobs)
     if (jp.level >= 0 && !jp.narrow && !jp.paired && jp.pair_with < 0 && jp.J.ho <= 32) {
       jp.J.kinter = 4;
-      jp.J.nparts = 4 * jp.J.ksplit;
+      jp.J.nparts = jp.J.ksplit;
       jp.J.two_prod = 0;
     }
   P.total = off;
@@ -1510,6 +1585,55 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
 }
 
 }  // namespace
+
+extern "C" int althea_ibl_tc_stats(int w, int h, const althea_ibl_mip_target* mips, int n,
+                                   const int* levels, int irr_w, int irr_h, int irr_level,
+                                   althea_ibl_tc_work* out) {
+  if (!out) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "tc stats: null output");
+  memset(out, 0, sizeof(*out));
+  if (check_env(w, h)) return ALTHEA_IBL_ERR_INVALID_ARGUMENT;
+  if (n < 0 || n > ALTHEA_IBL_MAX_MIPS || (n > 0 && !mips))
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "tc stats: %d mips (0..%d, non-null)", n,
+                     ALTHEA_IBL_MAX_MIPS);
+  TcPlan P;
+  int st = make_plan(w, h, mips, n, levels, irr_w, irr_h, irr_level, P);
+  if (st) return st;
+  const double pi = 3.14159265358979323846;
+  for (const JobPlan& jp : P.jobs) {
+    const Job& J = jp.J;
+    if (jp.level < 0 && !jp.narrow) continue;  // roughness 0: the delta pass
+    const double dense = (double)J.ho * J.wo * J.hs * J.ws;
+    if (jp.narrow) {
+      out->cuda_core_pairs += dense;
+      continue;
+    }
+    out->dense_pairs += dense;
+    if (jp.paired) continue;  // contracted inside its partner's launch
+    out->tensor_launches += 1;
+    const bool pair = jp.pair_with >= 0;
+    const int ho_b = pair ? P.jobs[jp.pair_with].J.ho : 0;
+    const int KS = J.two_prod ? 2 * kKS : kKS;
+    const int kchunks = J.kpad / KS, products = J.two_prod ? 2 : 3;
+    const int ntiles = (J.ho + kM - 1) / kM, gy = J.m * J.nblk;
+    // flops of one stage's MMAs: 3 channels x products x K/16 MMAs of M = 128, N = nb, K = 16
+    const double stage_flops = 3.0 * products * (KS / 16) * 2.0 * kM * J.nb * 16;
+    for (int tile = 0; tile < ntiles; ++tile) {
+      const int ia = tile * kM, ib = std::min(J.ho, ia + kM) - 1;
+      const int rows = ib - ia + 1 + ho_b;
+      for (int j = 0; j < J.hs; ++j) {
+        const double q = pi * ((j + 0.5) / J.hs - 0.5);
+        int uh = visible_halfwidth(q, ia, ib, J.ho, J.ws, J.g, J.krow);
+        if (pair) uh = std::max(uh, visible_halfwidth(q, 0, ho_b - 1, ho_b, J.ws, J.g, J.krow));
+        int ca, cb;
+        visible_chunks(uh, J.krow, KS, kchunks, ca, cb);
+        const int nvis = ca + kchunks - cb;
+        out->tensor_flops += (double)gy * J.g * nvis * stage_flops;
+        out->visible_pairs += (double)rows * J.wo * J.g * std::min(J.krow, nvis * KS);
+      }
+    }
+  }
+  return ALTHEA_IBL_OK;
+}
 
 extern "C" size_t althea_ibl_tc_workspace_size(int w, int h, const althea_ibl_mip_target* mips,
                                                int n, const int* levels, int irr_w, int irr_h,
@@ -1638,7 +1762,7 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
   static_assert(sizeof(FinishArgs) <= 32000, "finish arguments fit the kernel parameter space");
   FinishArgs fa;
   memset(&fa, 0, sizeof(fa));
-  long long finish_threads_total = 0;
+  int finish_blocks = 0;
   for (size_t k = 0; k < P.jobs.size(); ++k) {
     JobPlan& jp = P.jobs[k];
     void* out = nullptr;
@@ -1700,8 +1824,9 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     fa.job[fa.n] = J;
     fa.out[fa.n] = out;
     fa.pitch[fa.n] = pitch;
-    fa.begin[fa.n] = finish_threads_total;
-    finish_threads_total += (long long)((J.ho + kFinishRows - 1) / kFinishRows) * J.wo;
+    fa.begin[fa.n] = finish_blocks;
+    finish_blocks +=
+        (int)(((long long)((J.ho + kFinishRows - 1) / kFinishRows) * J.wo + 31) / 32);
     ++fa.n;
     if (jp.paired) continue;  // contracted inside its partner's launch
     J.pair = 0;
@@ -1715,9 +1840,11 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
       J.partial_b = reinterpret_cast<float*>(base + bp.partial_off);
       J.wsum_part_b = reinterpret_cast<double*>(base + bp.wsum_off);
     }
-    // At least 120 KB so no two CTAs share an SM (each allocates all of TMEM).
+    // At least 120 KB so no two CTAs share an SM (each allocates all of TMEM),
+    // and room for a K interleave's quarter sums ([4][3 nb][32] floats).
     int smem = (int)smem_plan(J).total;
     if (smem < 120 * 1024) smem = 120 * 1024;
+    if (J.kinter > 1 && smem < 4 * 3 * J.nb * 32 * 4) smem = 4 * 3 * J.nb * 32 * 4;
     dim3 grid((J.ho + kM - 1) / kM, J.m * J.nblk, J.ksplit);
     auto kern = J.kind == 1 ? contract_kernel<1, false>
                             : (J.two_prod ? contract_kernel<0, true> : contract_kernel<0, false>);
@@ -1728,10 +1855,8 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     if (e != cudaSuccess) return cuda_status(e, "tc contraction launch");
   }
   if (fa.n > 0) {
-    fa.begin[fa.n] = finish_threads_total;
-    const unsigned blocks =
-        (unsigned)((finish_threads_total + kFinishThreads - 1) / kFinishThreads);
-    finish_all_kernel<<<blocks, kFinishThreads, 0, s>>>(fa);
+    fa.begin[fa.n] = finish_blocks;
+    finish_all_kernel<<<finish_blocks, kFinishThreads, 0, s>>>(fa);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "tc finish launch");
   }

@@ -63,6 +63,12 @@ class Outputs(ctypes.Structure):
                 ("lut_dev", ctypes.c_void_p), ("lut_pitch_bytes", ctypes.c_size_t)]
 
 
+class TcWork(ctypes.Structure):
+    _fields_ = [("dense_pairs", ctypes.c_double), ("visible_pairs", ctypes.c_double),
+                ("tensor_flops", ctypes.c_double), ("cuda_core_pairs", ctypes.c_double),
+                ("tensor_launches", ctypes.c_int)]
+
+
 class Probe(ctypes.Structure):
     _fields_ = [("level0_dev", ctypes.c_void_p), ("chain_dev", ctypes.c_void_p),
                 ("env_width", ctypes.c_int), ("env_height", ctypes.c_int),
@@ -196,6 +202,8 @@ def load(build_if_missing: bool = True):
         "althea_ibl_bake_tc": (i, [vp, i, i, ctypes.POINTER(MipTarget), i, ctypes.POINTER(i),
                                    vp, i, i, sz, i, vp, sz, vp]),
         "althea_ibl_tc_error": (i, [vp, vp]),
+        "althea_ibl_tc_stats": (i, [i, i, ctypes.POINTER(MipTarget), i, ctypes.POINTER(i), i, i,
+                                    i, ctypes.POINTER(TcWork)]),
         "althea_ibl_tc_wait_selftest": (i, [ctypes.c_ulonglong, ctypes.POINTER(i), vp]),
         "althea_ibl_bake_tc_ex": (i, [vp, i, i, ctypes.POINTER(MipTarget), i, ctypes.POINTER(i),
                                       vp, i, i, sz, i, vp, sz, i, vp]),
@@ -745,6 +753,21 @@ def tc_plan(w: int, h: int, mip_sizes: List[tuple], roughness: List[float],
     il = ctypes.c_int()
     _check(load().althea_ibl_tc_plan(w, h, arr, n, irradiance_width, lv, ctypes.byref(il)))
     return [lv[k] for k in range(n)], il.value
+
+
+def tc_stats(w: int, h: int, mip_sizes: List[tuple], roughness: List[float],
+             irradiance_size=None) -> TcWork:
+    """The planned work of a precision bake with the planner's levels: dense
+    and visible (output, source) pairs, tensor-core flops issued, CUDA-core
+    pairs, contraction launches (host only)."""
+    n = len(mip_sizes)
+    arr = (MipTarget * max(n, 1))()
+    for k, ((mw, mh), r) in enumerate(zip(mip_sizes, roughness)):
+        arr[k] = MipTarget(0, mw * 16, mw, mh, float(r))
+    iw, ih = irradiance_size or (0, 0)
+    out = TcWork()
+    _check(load().althea_ibl_tc_stats(w, h, arr, n, None, iw, ih, -1, ctypes.byref(out)))
+    return out
 
 
 def tc_wait_selftest(limit_ms: float = 20.0, stream=None) -> int:

@@ -237,6 +237,21 @@ int althea_ibl_bake_tc(const float* chain_dev, int env_width, int env_height,
                        size_t irradiance_pitch_bytes, int irradiance_level, void* workspace_dev,
                        size_t workspace_bytes, void* stream);
 int althea_ibl_tc_error(const void* workspace_dev, void* stream);
+/* The planned work of a precision bake, as its kernels run it (host only, no
+ * device access): for benchmarks and rooflines.  No counterpart in the
+ * reference. */
+typedef struct {
+  double dense_pairs;        /* (output texel, source texel) pairs of the tensor-core outputs */
+  double visible_pairs;      /* of those, the pairs in the K stages the kernels run (the rest
+                                lie below every row's horizon: exact zeros, skipped) */
+  double tensor_flops;       /* flops of the tcgen05.mma instructions issued (M = 128 tiles,
+                                padding rows and columns included) */
+  double cuda_core_pairs;    /* pairs of the outputs summed on the CUDA cores */
+  int tensor_launches;       /* contraction launches (a paired launch counts once) */
+} althea_ibl_tc_work;
+int althea_ibl_tc_stats(int env_width, int env_height, const althea_ibl_mip_target* mips,
+                        int mip_count, const int* levels, int irradiance_width,
+                        int irradiance_height, int irradiance_level, althea_ibl_tc_work* out);
 /* Diagnostics: runs the precision kernel's bounded mbarrier wait on a barrier
  * that nothing completes, with a limit of limit_ns (1 ns .. 1 s).  Returns
  * ALTHEA_IBL_OK when the wait gave up, raised its abort flag and the kernel

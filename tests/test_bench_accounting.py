@@ -43,6 +43,14 @@ def test_precision_flops_and_jobs():
     alg, executed = bench.tc_flops(levels, irr_level)
     assert alg == 8 * pairs and executed == 6 * executed_pairs
     assert round(alg / 1e12, 2) == 3.21
+    # the library's own account: the same pairs (tensor + CUDA cores), the
+    # visible part of them smaller, and at least the flops of the visible
+    # pairs at two products per channel issued on the tensor cores
+    work = bench.tc_work()
+    assert work["dense_pairs"] + work["cuda_core_pairs"] == pairs
+    assert 0.5 * work["dense_pairs"] < work["visible_pairs"] < work["dense_pairs"]
+    assert work["tensor_flops_issued"] >= 2 * 3 * 2 * work["visible_pairs"]
+    assert work["tensor_launches"] == 6
     # phase counts: s = source / output width; g = 1, s / 8 or s
     for w, h, ws, hs, lv, g in bench.tc_jobs(levels, irr_level):
         s = ws // w

@@ -199,7 +199,7 @@ _LAYOUTS = [
     (ibl.BatchParams, "althea_ibl_batch_params"), (ibl.BatchInfo, "althea_ibl_batch_info"),
     (ibl.ServerConfig, "althea_ibl_server_config"), (ibl.Request, "althea_ibl_request"),
     (ibl.Completion, "althea_ibl_completion"), (ibl.ServerStats, "althea_ibl_server_stats"),
-    (ibl.Sun, "althea_ibl_sun"),
+    (ibl.Sun, "althea_ibl_sun"), (ibl.TcWork, "althea_ibl_tc_work"),
 ]
 # Python constant -> C enum constant or macro
 _CONSTANTS = {
