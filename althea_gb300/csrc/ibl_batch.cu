@@ -286,29 +286,20 @@ struct althea_ibl_batch {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t exec_stream = nullptr;
   int graph_kernels = -1;  // kernel nodes of the captured bake (-1: not captured)
-  // precision path (ALTHEA_IBL_BATCH_PRECISION): one tensor-core bake per
-  // probe after the shared chain pass.  The bakes run on kTcLanes streams
-  // forked from the caller's (joined back before the run ends), so the small
-  // contractions of different probes overlap on the GPU; probes of one shape
-  // on one lane share a workspace (their bakes are ordered on that lane).
+  // precision path (ALTHEA_IBL_BATCH_PRECISION), after the shared chain
+  // pass: every probe's split planes, tables and CUDA-core outputs on
+  // kTcLanes streams forked from the caller's, ONE persistent tcgen05
+  // contraction over the work items of every probe, then every probe's finish
+  // on the lanes (joined back before the run ends).  Each probe has its own
+  // workspace: all of their contractions are in flight at once.
   bool precision = false;
   std::vector<cudaStream_t> lanes;
   cudaEvent_t fork_ev = nullptr;
   std::vector<cudaEvent_t> join_ev;
   int out_format = ALTHEA_IBL_FORMAT_RGBA32F;
-  struct TcProbe {
-    const float* chain;
-    int w, h;
-    std::vector<althea_ibl_mip_target> mips;
-    float* irr;
-    int irr_w, irr_h;
-    size_t irr_pitch;
-    int ws;    // index into tc_ws
-    int lane;  // index into lanes
-  };
-  std::vector<TcProbe> tc;
-  std::vector<void*> tc_ws;
-  std::vector<size_t> tc_ws_bytes;
+  std::vector<void*> tc_ws;   // one per probe
+  std::vector<int> tc_lane;   // lane of each probe
+  ibl::TcBatch* tcb = nullptr;
 };
 
 namespace {
@@ -325,6 +316,7 @@ void free_batch(althea_ibl_batch* b) {
   cudaFree(b->d_irr_begins);
   cudaFree(b->d_irr_texel_begins);
   cudaFree(b->d_partial);
+  tc_batch_destroy(b->tcb);
   for (void* p : b->tc_ws) cudaFree(p);
   for (cudaStream_t l : b->lanes) cudaStreamDestroy(l);
   for (cudaEvent_t e : b->join_ev) cudaEventDestroy(e);
@@ -472,25 +464,8 @@ int launch_irradiance_batch(althea_ibl_batch* b, cudaStream_t st) {
 }
 
 int launch_tc(althea_ibl_batch* b, cudaStream_t st) {
-  // fork: every lane starts after the chain pass on `st`
-  cudaError_t e = cudaEventRecord(b->fork_ev, st);
-  for (size_t l = 0; l < b->lanes.size() && e == cudaSuccess; ++l)
-    e = cudaStreamWaitEvent(b->lanes[l], b->fork_ev, 0);
-  if (e != cudaSuccess) return cuda_status(e, "precision lanes fork");
-  int r = ALTHEA_IBL_OK;
-  for (size_t i = 0; i < b->tc.size() && !r; ++i) {
-    const althea_ibl_batch::TcProbe& p = b->tc[i];
-    r = tc_bake(p.chain, p.w, p.h, p.mips.data(), (int)p.mips.size(), nullptr, p.irr, p.irr_w,
-                p.irr_h, p.irr_pitch, -1, b->tc_ws[p.ws], b->tc_ws_bytes[p.ws], b->out_format,
-                b->lanes[p.lane]);
-  }
-  // join (also after an error, so that a stream capture can end cleanly)
-  for (size_t l = 0; l < b->lanes.size(); ++l) {
-    cudaError_t j = cudaEventRecord(b->join_ev[l], b->lanes[l]);
-    if (j == cudaSuccess) j = cudaStreamWaitEvent(st, b->join_ev[l], 0);
-    if (j != cudaSuccess && !r) r = cuda_status(j, "precision lanes join");
-  }
-  return r;
+  return tc_batch_run(b->tcb, st, b->lanes.data(), (int)b->lanes.size(), b->tc_lane.data(),
+                      b->fork_ev, b->join_ev.data());
 }
 
 int launch_all(althea_ibl_batch* b, cudaStream_t st) {
@@ -714,15 +689,14 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
       lane_of[i] = l;
       load[l] += (double)probes[i].env_width * probes[i].env_height;
     }
-    std::map<std::string, int> ws_of;
+    b->tc_lane = lane_of;
+    std::vector<TcBatchProbe> tp(n);
     for (int i = 0; i < n; ++i) {
       const althea_ibl_probe& p = probes[i];
-      althea_ibl_batch::TcProbe t;
+      TcBatchProbe& t = tp[i];
       t.chain = p.chain_dev;
       t.w = p.env_width;
       t.h = p.env_height;
-      std::ostringstream key;
-      key << p.env_width << 'x' << p.env_height;
       for (int m = 0; m < p.mip_count; ++m) {
         althea_ibl_mip_target mt;
         mt.out_dev = p.mip_dev[m];
@@ -731,35 +705,31 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
         mt.height = p.mip_height[m];
         mt.roughness = p.mip_roughness[m];
         t.mips.push_back(mt);
-        key << ',' << mt.width << 'x' << mt.height << '@' << mt.roughness;
       }
       t.irr = p.irradiance_dev;
       t.irr_w = p.irradiance_dev ? p.irradiance_width : 0;
       t.irr_h = p.irradiance_dev ? p.irradiance_height : 0;
       t.irr_pitch = p.irradiance_pitch_bytes;
-      t.lane = lane_of[i];
-      key << '|' << t.irr_w << 'x' << t.irr_h << "#lane" << t.lane;
-      auto it = ws_of.find(key.str());
-      if (it == ws_of.end()) {
-        const size_t bytes = tc_workspace_bytes(t.w, t.h, t.mips.data(), (int)t.mips.size(),
-                                                nullptr, t.irr_w, t.irr_h, -1);
-        if (bytes == 0) {
-          free_batch(b);
-          return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "probe %d: precision plan: %s", i,
-                           last_error());
-        }
-        void* ws = nullptr;
-        cudaError_t e = cudaMalloc(&ws, bytes);
-        if (e != cudaSuccess) {
-          free_batch(b);
-          return cuda_status(e, "precision workspace");
-        }
-        b->tc_ws.push_back(ws);
-        b->tc_ws_bytes.push_back(bytes);
-        it = ws_of.emplace(key.str(), (int)b->tc_ws.size() - 1).first;
+      t.ws_bytes = tc_workspace_bytes(t.w, t.h, t.mips.data(), (int)t.mips.size(), nullptr,
+                                      t.irr_w, t.irr_h, -1);
+      if (t.ws_bytes == 0) {
+        free_batch(b);
+        return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "probe %d: precision plan: %s", i,
+                         last_error());
       }
-      t.ws = it->second;
-      b->tc.push_back(std::move(t));
+      void* ws = nullptr;
+      cudaError_t e = cudaMalloc(&ws, t.ws_bytes);
+      if (e != cudaSuccess) {
+        free_batch(b);
+        return cuda_status(e, "precision workspace");
+      }
+      b->tc_ws.push_back(ws);
+      t.ws = ws;
+    }
+    int r = tc_batch_create(tp.data(), n, b->out_format, &b->tcb);
+    if (r) {
+      free_batch(b);
+      return r;
     }
   }
   // ---- prefilter queue: full-sample jobs first, roughness 0 last ----------
@@ -858,6 +828,7 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
 }
 
 extern "C" int althea_ibl_batch_run(althea_ibl_batch* b, void* stream) {
+  ibl::NvtxRange nvtx_range("althea_ibl_batch_run");
   if (!b) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null batch");
   cudaStream_t st = (cudaStream_t)stream;
   const bool want_graph = (b->params.flags & ALTHEA_IBL_BATCH_GRAPH) && st != nullptr;
@@ -916,7 +887,15 @@ extern "C" int althea_ibl_batch_describe(const althea_ibl_batch* b, althea_ibl_b
   info->tuned = b->tuned;
   info->graph = b->exec != nullptr;
   info->graph_kernels = b->exec ? b->graph_kernels : -1;
+  info->contraction_items = b->tcb ? tc_batch_items(b->tcb) : 0;
   return ALTHEA_IBL_OK;
+}
+
+extern "C" int althea_ibl_batch_status(const althea_ibl_batch* b, void* stream) {
+  if (!b) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null batch");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (b->tcb) return tc_batch_error(b->tcb, st);
+  return cuda_status(cudaStreamSynchronize(st), "batch status");
 }
 
 extern "C" int althea_ibl_batch_destroy(althea_ibl_batch* b) {

@@ -224,6 +224,7 @@ extern "C" const float* althea_ibl_env_chain(const althea_ibl_context* c) {
 
 extern "C" int althea_ibl_upload_env(althea_ibl_context* c, const float* rgba, int src_is_device,
                                      void* stream) {
+  ibl::NvtxRange nvtx_range("althea_ibl_upload_env");
   if (!c || !rgba) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
   int r = check_device(c);
   if (r) return r;
@@ -239,6 +240,7 @@ extern "C" int althea_ibl_upload_env(althea_ibl_context* c, const float* rgba, i
 }
 
 extern "C" int althea_ibl_bake(althea_ibl_context* c, const althea_ibl_outputs* o, void* stream) {
+  ibl::NvtxRange nvtx_range("althea_ibl_bake");
   if (!c || !o) return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "null argument");
   if (!c->env_ready)
     return set_error(ALTHEA_IBL_ERR_NOT_READY, "no environment map uploaded to this context");

@@ -3,12 +3,24 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstddef>
+#include <vector>
 
 #include "althea_ibl.h"
 
 namespace ibl {
+
+// An NVTX range around a public call (header-only NVTX3: without a profiler
+// attached the push and pop return at once).  Profilers show the library's
+// stages on the host timeline under these names.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct IrrPlan {
   int phi;             // int(300 * H / W)
@@ -56,6 +68,30 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
             const SideStream* side = nullptr);
 size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n,
                           const int* levels, int irr_w, int irr_h, int irr_level);
+
+// Precision batches (ibl_tc.cu): every probe planned with the planner's
+// levels into its own workspace; a run launches each probe's split planes and
+// tables on its lane, then ONE persistent contraction kernel over a queue of
+// (job, row tile, column block, split) work items of every probe, then each
+// probe's finish on its lane.  The results equal the probes' single bakes.
+struct TcBatchProbe {
+  const float* chain;
+  int w, h;
+  std::vector<althea_ibl_mip_target> mips;
+  float* irr;  // may be null
+  int irr_w, irr_h;
+  size_t irr_pitch;
+  void* ws;    // tc_workspace_bytes of this probe, 256-byte aligned
+  size_t ws_bytes;
+};
+struct TcBatch;
+int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, TcBatch** out);
+int tc_batch_run(TcBatch* b, cudaStream_t st, const cudaStream_t* lanes, int nlanes,
+                 const int* lane_of, cudaEvent_t fork_ev, const cudaEvent_t* join_ev);
+int tc_batch_items(const TcBatch* b);
+// Synchronises `st` and reports a work item whose bounded wait gave up.
+int tc_batch_error(const TcBatch* b, cudaStream_t st);
+void tc_batch_destroy(TcBatch* b);
 int launch_brdf_lut(float* out, int n, size_t pitch_bytes, int samples, int orientation,
                     cudaStream_t st);
 // Sun lobes added to an env level 0 (ibl_suns.cu); out may equal base.

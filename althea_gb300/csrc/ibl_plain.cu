@@ -478,6 +478,7 @@ extern "C" int althea_ibl_build_env_chain(const float* level0, int w, int h, flo
 extern "C" int althea_ibl_prefilter(const float* chain, int w, int h,
                                     const althea_ibl_mip_target* mips, int mip_count,
                                     int samples, int generator, void* stream) {
+  ibl::NvtxRange nvtx_range("althea_ibl_prefilter");
   int st = check_env(w, h);
   if (st) return st;
   if (!chain || ((uintptr_t)chain) % 16)
@@ -509,6 +510,7 @@ extern "C" size_t althea_ibl_irradiance_workspace_size(int w, int h, int ow, int
 
 extern "C" int althea_ibl_irradiance(const float* chain, int w, int h, float* out, int ow, int oh,
                                      size_t pitch, void* ws, size_t ws_bytes, void* stream) {
+  ibl::NvtxRange nvtx_range("althea_ibl_irradiance");
   int st = check_env(w, h);
   if (st) return st;
   st = check_irradiance_args(w, h, ow, oh);

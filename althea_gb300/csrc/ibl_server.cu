@@ -195,6 +195,7 @@ void pool_release(althea_ibl_server* s, void* p, size_t bytes) {
 }
 
 int start(althea_ibl_server* s, Slot* slot, const Pending& pend, const Layout& L) {
+  ibl::NvtxRange nvtx_range("server request");
   const althea_ibl_request& r = pend.req;
   cudaStream_t st = slot->stream;
   char* base = static_cast<char*>(slot->block);

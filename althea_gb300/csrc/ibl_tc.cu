@@ -65,6 +65,7 @@
 #include <cstdint>
 #include <algorithm>
 #include <cstring>
+#include <new>
 #include <vector>
 
 #include "althea_ibl.h"
@@ -101,6 +102,10 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
@@ -268,6 +273,57 @@ __device__ __forceinline__ void mma_stage64_ts2(uint32_t d, uint32_t a, uint64_t
       : "memory");
 }
 
+// Column tiles (both operands in shared memory): one K = 32 stage of one
+// channel, hi/lo split, then a commit to `bar`:
+//   D += Lhi*Whi + Lhi*Wlo + Llo*Whi  for K = 0..15 and 16..31
+// A = radiance descriptors ah/al (hi/lo plane, the next K = 16 at +2 units of
+// 16 bytes), B = weight descriptors bh/bl (the next K = 16 at +bk units).
+__device__ __forceinline__ void mma_stage_ss(uint32_t d, uint64_t ah, uint64_t al, uint64_t bh,
+                                             uint64_t bl, uint32_t bk, uint32_t idesc,
+                                             uint32_t accumulate, uint64_t* bar) {
+  asm volatile(
+      "{\n .reg .pred p, t;\n .reg .b64 bk64, ah2, al2, bh2, bl2;\n"
+      " setp.ne.b32 p, %7, 0;\n setp.eq.b32 t, %7, %7;\n cvt.u64.u32 bk64, %5;\n"
+      " add.u64 ah2, %1, 2;\n add.u64 al2, %2, 2;\n add.u64 bh2, %3, bk64;\n"
+      " add.u64 bl2, %4, bk64;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %3, %6, p;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %4, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %2, %3, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], ah2, bh2, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], ah2, bl2, %6, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], al2, bh2, %6, t;\n"
+      " tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%8];\n}\n" ::"r"(d),
+      "l"(ah), "l"(al), "l"(bh), "l"(bl), "r"(bk), "r"(idesc), "r"(accumulate),
+      "r"((uint32_t)__cvta_generic_to_shared(bar))
+      : "memory");
+}
+
+// Column tiles, a K = 64 stage with the weights as BF16 hi only:
+//   D += Lhi*Whi + Llo*Whi  for K = 16t .. 16t + 15, t = 0..3
+// (A at +2t units, B at +t bk units).
+__device__ __forceinline__ void mma_stage64_ss2(uint32_t d, uint64_t ah, uint64_t al, uint64_t bh,
+                                                uint32_t bk, uint32_t idesc, uint32_t accumulate,
+                                                uint64_t* bar) {
+  asm volatile(
+      "{\n .reg .pred p, t;\n .reg .b64 bk64, a1, a2, a3, l1, l2, l3, b1, b2, b3;\n"
+      " setp.ne.b32 p, %6, 0;\n setp.eq.b32 t, %6, %6;\n cvt.u64.u32 bk64, %4;\n"
+      " add.u64 a1, %1, 2;\n add.u64 a2, %1, 4;\n add.u64 a3, %1, 6;\n"
+      " add.u64 l1, %2, 2;\n add.u64 l2, %2, 4;\n add.u64 l3, %2, 6;\n"
+      " add.u64 b1, %3, bk64;\n add.u64 b2, b1, bk64;\n add.u64 b3, b2, bk64;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %3, %5, p;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %2, %3, %5, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], a1, b1, %5, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], l1, b1, %5, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], a2, b2, %5, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], l2, b2, %5, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], a3, b3, %5, t;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], l3, b3, %5, t;\n"
+      " tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%7];\n}\n" ::"r"(d),
+      "l"(ah), "l"(al), "l"(bh), "r"(bk), "r"(idesc), "r"(accumulate),
+      "r"((uint32_t)__cvta_generic_to_shared(bar))
+      : "memory");
+}
+
 // Hardware reciprocal approximation (one MUFU operation, ~1 ulp).
 __device__ __forceinline__ float rcp_approx(float x) {
   float r;
@@ -401,23 +457,49 @@ __host__ __device__ __forceinline__ void visible_chunks(int uh, int krow, int ks
   }
 }
 
-// The contraction kernel.  Grid: (ceil(ho/128), m * nblk, ksplit); each CTA
-// sums at most kMaxK of K in one TMEM accumulation chain per channel.
+// Shared state of one contraction CTA: the barriers, the abort flag and the
+// producers' weight sums.
+struct CtaShared {
+  uint64_t a_full[kStages], a_empty[kStages];
+  uint64_t slot_full[kMaxSlots], slot_empty[kMaxSlots];
+  uint64_t done_bar;
+  int abort;
+  double wsum[kProducerWarps / 4][kM];
+};
+
+// Bounded wait for a barrier phase that is known to complete (the arrivals
+// are already in flight); false after kWaitNs.
+__device__ __forceinline__ bool settle(uint64_t* bar, uint32_t parity) {
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (global_ns() - t0 > kWaitNs) return false;
+  return true;
+}
+
+// One CTA of a contraction: output rows bx * 128 .., column block by, source
+// rows of split bz -- the grid coordinates of a one-shot launch, or one work
+// item of the persistent batch kernel.  Each CTA sums at most kMaxK of K in
+// one TMEM accumulation chain per channel.  The caller holds all 512 TMEM
+// columns at `tmem`.  Returns false when a bounded wait gave up (the job's
+// error word is set).  Otherwise every barrier is quiescent and invalidated
+// on return, so the CTA may run another item.
 template <int KIND, bool TWO>
-__global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t a_full[kStages], a_empty[kStages];
-  __shared__ uint64_t slot_full[kMaxSlots], slot_empty[kMaxSlots];
-  __shared__ uint64_t done_bar;
-  __shared__ uint32_t tmem_base_sh;
-  __shared__ int abort_sh;
-  __shared__ double wsum_sh[kProducerWarps / 4][kM];
+__device__ __forceinline__ bool contract_cta(const Job& job, int bx, int by, int bz,
+                                             uint32_t tmem, unsigned char* smem,
+                                             CtaShared& sh) {
+  uint64_t* const a_full = sh.a_full;
+  uint64_t* const a_empty = sh.a_empty;
+  uint64_t* const slot_full = sh.slot_full;
+  uint64_t* const slot_empty = sh.slot_empty;
+  uint64_t& done_bar = sh.done_bar;
+  int& abort_sh = sh.abort;
+  double(*wsum_sh)[kM] = sh.wsum;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int i0 = blockIdx.x * kM;
-  const int x0 = blockIdx.y / job.nblk;
-  const int n0 = (blockIdx.y - x0 * job.nblk) * job.nb;
-  const int split = blockIdx.z;
+  const int i0 = bx * kM;
+  const int x0 = by / job.nblk;
+  const int n0 = (by - x0 * job.nblk) * job.nb;
+  const int split = bz;
   const SmemPlan sp = smem_plan(job);
   __nv_bfloat16* slots = reinterpret_cast<__nv_bfloat16*>(smem + sp.slots);
   float* cosd_sm = reinterpret_cast<float*>(smem + sp.cosd);
@@ -461,16 +543,12 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
       cosd_sm[e] = k < job.krow ? job.cos_d[job.g * kk + ph] : 0.0f;
     }
   }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(&tmem_base_sh)),
-                 "r"((uint32_t)kTmemCols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
+  // generic shared-memory writes of a previous work item (the K-interleave
+  // reduction) come before this item's bulk copies into the same bytes
+  fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const uint32_t tmem = tmem_base_sh;
   if (kint) {
     // K interleave: a quarter's lanes in the three stage slots it does not
     // own stay zero, so the MMAs of other quarters' stages add nothing there
@@ -501,15 +579,15 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   constexpr int NG = KW / 8;   // groups of 8 K per producer warp and stage
   const int kchunks = job.kpad / KS;
   // stages this CTA runs: the visible chunks of each of its source rows
-  const int* vis_row = job.vis + (size_t)blockIdx.x * job.hs;
+  const int* vis_row = job.vis + (size_t)bx * job.hs;
   long long total = 0;
   for (int j = split; j < job.hs; j += jstep) {
     int ca, cb;
     visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
     total += (long long)job.g * (ca + kchunks - cb);
   }
-  const bool want_wsum = KIND == 0 && blockIdx.y == 0;
-  const bool want_wsum_b = job.pair && job.kind_b == 0 && blockIdx.y == 0;
+  const bool want_wsum = KIND == 0 && by == 0;
+  const bool want_wsum_b = job.pair && job.kind_b == 0 && by == 0;
 
   if (warp < kProducerWarps) {
     // ---- weight producers: rows 32q + lane, K sub-range [8h, 8h + 8) of each stage
@@ -706,12 +784,18 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
       // every MMA issued by all issuers has completed before the accumulators
       // are read and TMEM is released
       mma_commit(&done_bar);
-      const unsigned long long t0 = global_ns();
-      while (!mbar_try_wait(&done_bar, 0u))
-        if (global_ns() - t0 > kWaitNs) {
-          *abort_flag = 1;
-          break;
-        }
+      if (!settle(&done_bar, 0u)) *abort_flag = 1;
+      // The last commits' arrivals on the stage and slot barriers land too,
+      // before anything invalidates the barriers for reuse.
+      for (uint32_t st = 0; ok && st < (uint32_t)kStages && st < gidx; ++st) {
+        const uint32_t last = st + kStages * ((gidx - 1 - st) / kStages);
+        if (!settle(&a_empty[st], (last / kStages) & 1u)) *abort_flag = 1;
+      }
+      const uint32_t ns_ = (uint32_t)job.nslots;
+      for (uint32_t sl = 0; ok && sl < ns_ && sl < row_id; ++sl) {
+        const uint32_t last = sl + ns_ * ((row_id - 1 - sl) / ns_);
+        if (!settle(&slot_empty[sl], (last / ns_) & 1u)) *abort_flag = 1;
+      }
     }
   } else if (lane == 0) {
     // ---- Hankel row loader: slot[p][t] = P_ph[(t + 8 n0) mod krow], t < rlen ----
@@ -834,9 +918,102 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0)
+  if (failed) return false;
+  // quiescent: every arrival has landed (the MMA issuer settled the last
+  // phases), so the barriers can be invalidated for the next work item
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_inval(&a_full[s]);
+      mbar_inval(&a_empty[s]);
+    }
+    for (int s = 0; s < kMaxSlots; ++s) {
+      mbar_inval(&slot_full[s]);
+      mbar_inval(&slot_empty[s]);
+    }
+    mbar_inval(&done_bar);
+  }
+  return true;
+}
+
+// TMEM for a contraction CTA: all 512 columns, allocated by warp 0.
+__device__ __forceinline__ uint32_t tmem_alloc_all(uint32_t* slot) {
+  if ((threadIdx.x >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(slot)),
+                 "r"((uint32_t)kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  return *slot;
+}
+
+__device__ __forceinline__ void tmem_free_all(uint32_t tmem) {
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if ((threadIdx.x >> 5) == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"((uint32_t)kTmemCols));
+}
+
+// The contraction kernel of one job.  Grid: (ceil(ho/128), m * nblk, ksplit).
+template <int KIND, bool TWO>
+__global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ CtaShared sh;
+  __shared__ uint32_t tmem_base_sh;
+  const uint32_t tmem = tmem_alloc_all(&tmem_base_sh);
+  contract_cta<KIND, TWO>(job, blockIdx.x, blockIdx.y, blockIdx.z, tmem, smem, sh);
+  tmem_free_all(tmem);
+}
+
+// One CTA of some job of a batch.
+struct WorkItem {
+  int job;         // index into the job table
+  int bx, by, bz;  // the CTA of that job's one-shot grid
+};
+
+// The persistent contraction kernel of a batch: one CTA per SM (each holds
+// all of TMEM for its lifetime), pulling (job, tile, column block, split)
+// work items from a queue in the order given (largest first) until it is
+// empty.  Each item runs exactly the CTA of that job's one-shot launch, so
+// the results are the same bits.  A CTA whose bounded wait gave up stops
+// taking items (the job's error word is set).
+__global__ void __launch_bounds__(kThreads, 1)
+    contract_persistent_kernel(const Job* __restrict__ jobs, const WorkItem* __restrict__ items,
+                               int nitems, unsigned int* __restrict__ next) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ CtaShared sh;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int item_sh;
+  __shared__ __align__(16) Job job_sh;
+  static_assert(sizeof(Job) % 8 == 0, "job copy in 8-byte words");
+  const uint32_t tmem = tmem_alloc_all(&tmem_base_sh);
+  for (;;) {
+    if (threadIdx.x == 0) item_sh = (int)atomicAdd(next, 1u);
+    __syncthreads();
+    const int it = item_sh;
+    if (it >= nitems) break;
+    const WorkItem wi = items[it];
+    {
+      const unsigned long long* src = reinterpret_cast<const unsigned long long*>(jobs + wi.job);
+      unsigned long long* dst = reinterpret_cast<unsigned long long*>(&job_sh);
+      for (int e = threadIdx.x; e < (int)(sizeof(Job) / 8); e += blockDim.x) dst[e] = src[e];
+    }
+    __syncthreads();
+    bool ok;
+    if (job_sh.kind == 1)
+      ok = contract_cta<1, false>(job_sh, wi.bx, wi.by, wi.bz, tmem, smem, sh);
+    else if (job_sh.two_prod)
+      ok = contract_cta<0, true>(job_sh, wi.bx, wi.by, wi.bz, tmem, smem, sh);
+    else
+      ok = contract_cta<0, false>(job_sh, wi.bx, wi.by, wi.bz, tmem, smem, sh);
+    if (!ok) break;  // uniform: every thread read the same abort flag
+    __syncthreads();  // item_sh and job_sh are rewritten next
+  }
+  tmem_free_all(tmem);
 }
 
 // ---- narrow outputs on the CUDA cores ----------------------------------------------
@@ -1360,12 +1537,31 @@ struct JobPlan {
   bool paired = false;  // this job runs inside another's launch (finish only)
   size_t cosd_off = 0, rows_off = 0, orows_off = 0, partial_off = 0,
          wsum_off = 0, vis_off = 0;
+  void* out = nullptr;   // the output image and its pitch (texels), set at setup
+  long long pitch = 0;
+  int finish_slot = -1;  // this job's entry in the finish arguments
 };
 
 struct TcPlan {
   std::vector<JobPlan> jobs;
   std::vector<LevelPlanes> levels;
   size_t total = 0;
+};
+
+// One planned precision bake with every pointer set (tc_setup), launched in
+// phases: prep (split planes, tables, CUDA-core outputs), contractions,
+// finish (split sums, roughness-0 mips).
+struct TcBake {
+  TcPlan P;
+  const float* chain = nullptr;
+  int w = 0, h = 0, n = 0;
+  althea_ibl_mip_target mips[ALTHEA_IBL_MAX_MIPS];
+  int out_half = 0;
+  char* base = nullptr;
+  ChainTable tab;
+  FinishArgs fa;
+  int finish_blocks = 0;
+  std::vector<int> launch_jobs;  // P.jobs run by a contraction launch (not paired, not narrow)
 };
 
 size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -1657,17 +1853,16 @@ extern "C" int althea_ibl_tc_plan(int w, int h, const althea_ibl_mip_target* mip
 
 namespace ibl {
 
-int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
-            const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
-            int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream,
-            const SideStream* side) {
+int tc_setup(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
+             const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
+             int irr_level, void* ws, size_t ws_bytes, int out_format, TcBake& B) {
   int st = check_env(w, h);
   if (st) return st;
   if (out_format != ALTHEA_IBL_FORMAT_RGBA32F && out_format != ALTHEA_IBL_FORMAT_RGBA16F)
     return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "tensor path: output format %d",
                      out_format);
-  const int out_half = out_format == ALTHEA_IBL_FORMAT_RGBA16F;
-  const size_t texel = out_half ? 8 : 16;
+  B.out_half = out_format == ALTHEA_IBL_FORMAT_RGBA16F;
+  const size_t texel = B.out_half ? 8 : 16;
   if (!chain || ((uintptr_t)chain) % 16 || n < 0 || n > ALTHEA_IBL_MAX_MIPS || (n && !mips))
     return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "tensor path: chain/mips");
   for (int m = 0; m < n; ++m) {
@@ -1679,18 +1874,90 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     st = check_image(irr_out, irr_w, irr_h, irr_pitch, texel, "tc irradiance");
     if (st) return st;
   }
-  TcPlan P;
+  TcPlan& P = B.P;
   st = make_plan(w, h, mips, n, levels, irr_out ? irr_w : 0, irr_h, irr_level, P);
   if (st) return st;
   if (!ws || ws_bytes < P.total || ((uintptr_t)ws) % 256)
     return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
                      "tensor path workspace needs %zu bytes (256-byte aligned)", P.total);
-  cudaStream_t s = stream;
-  char* base = static_cast<char*>(ws);
+  B.chain = chain;
+  B.w = w;
+  B.h = h;
+  B.n = n;
+  for (int m = 0; m < n; ++m) B.mips[m] = mips[m];
+  B.base = static_cast<char*>(ws);
+  make_table(w, h, &B.tab);
+  char* base = B.base;
+  // Every pointer of every job, and the finish arguments.
+  memset(&B.fa, 0, sizeof(B.fa));
+  B.finish_blocks = 0;
+  B.launch_jobs.clear();
+  for (size_t k = 0; k < P.jobs.size(); ++k) {
+    JobPlan& jp = P.jobs[k];
+    if (jp.level < 0 && !jp.narrow) continue;  // roughness 0: the delta pass
+    Job& J = jp.J;
+    J.cos_d = reinterpret_cast<float*>(base + jp.cosd_off);
+    J.src_rows = reinterpret_cast<float*>(base + jp.rows_off);
+    J.out_rows = reinterpret_cast<float*>(base + jp.orows_off);
+    void* out = nullptr;
+    long long pitch = 0;
+    if ((int)k < n) {
+      out = mips[k].out_dev;
+      pitch = (long long)(mips[k].pitch_bytes / texel);
+    } else {
+      out = irr_out;
+      pitch = (long long)(irr_pitch / texel);
+    }
+    jp.out = out;
+    jp.pitch = pitch;
+    if (jp.narrow) continue;
+    const LevelPlanes& L = P.levels[jp.level];
+    J.src = reinterpret_cast<const __nv_bfloat16*>(base + L.offset);
+    J.partial = reinterpret_cast<float*>(base + jp.partial_off);
+    J.wsum_part = reinterpret_cast<double*>(base + jp.wsum_off);
+    J.error = reinterpret_cast<int*>(base);
+    J.out_half = B.out_half;
+    if (B.fa.n >= kMaxFinishJobs)
+      return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "tc: too many jobs");
+    B.fa.out[B.fa.n] = out;
+    B.fa.pitch[B.fa.n] = pitch;
+    B.fa.begin[B.fa.n] = B.finish_blocks;
+    B.finish_blocks +=
+        (int)(((long long)((J.ho + kFinishRows - 1) / kFinishRows) * J.wo + 31) / 32);
+    jp.finish_slot = B.fa.n++;
+    if (jp.paired) continue;  // contracted inside its partner's launch
+    J.vis = reinterpret_cast<const int*>(base + jp.vis_off);
+    J.pair = 0;
+    if (jp.pair_with >= 0) {
+      const JobPlan& bp = P.jobs[jp.pair_with];
+      J.pair = 1;
+      J.ho_b = bp.J.ho;
+      J.kind_b = bp.J.kind;
+      J.a2_b = bp.J.a2;
+      J.out_rows_b = reinterpret_cast<const float*>(base + bp.orows_off);
+      J.partial_b = reinterpret_cast<float*>(base + bp.partial_off);
+      J.wsum_part_b = reinterpret_cast<double*>(base + bp.wsum_off);
+    }
+    B.launch_jobs.push_back((int)k);
+  }
+  // the paired jobs' pointers are set above too: copy every job into its slot
+  for (const JobPlan& jp : P.jobs)
+    if (jp.finish_slot >= 0) B.fa.job[jp.finish_slot] = jp.J;
+  B.fa.begin[B.fa.n] = B.finish_blocks;
+  return ALTHEA_IBL_OK;
+}
+
+int tc_launch_narrow(const TcBake& B, cudaStream_t ns);
+
+// Split planes and tables; with `narrow`, the CUDA-core outputs too (on the
+// side stream when there is one, returned in *ns_out).
+int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream_t* ns_out,
+                   bool narrow = true) {
+  const TcPlan& P = B.P;
+  char* base = B.base;
+  *ns_out = s;
   cudaError_t e = cudaMemsetAsync(base, 0, 256, s);
   if (e != cudaSuccess) return cuda_status(e, "tc error flag");
-  ChainTable tab;
-  make_table(w, h, &tab);
   // One split pass per source level, writing every phase decomposition of it
   // (up to kMaxRowsOut per pass).
   std::vector<char> done(P.levels.size(), 0);
@@ -1699,7 +1966,7 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     const LevelPlanes& L = P.levels[a0];
     RowsArgs ra;
     memset(&ra, 0, sizeof(ra));
-    ra.src = reinterpret_cast<const float4*>(chain) + tab.off[L.level];
+    ra.src = reinterpret_cast<const float4*>(B.chain) + B.tab.off[L.level];
     ra.ws = L.ws;
     ra.hs = L.hs;
     for (size_t a1 = a0; a1 < P.levels.size() && ra.n < kMaxRowsOut; ++a1) {
@@ -1723,12 +1990,9 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     memset(&ta, 0, sizeof(ta));
     int nt = 0, nmax = 1;
     for (size_t k = 0; k < P.jobs.size(); ++k) {
-      JobPlan& jp = P.jobs[k];
+      const JobPlan& jp = P.jobs[k];
       if (jp.level < 0 && !jp.narrow) continue;
-      Job& J = jp.J;
-      J.cos_d = reinterpret_cast<float*>(base + jp.cosd_off);
-      J.src_rows = reinterpret_cast<float*>(base + jp.rows_off);
-      J.out_rows = reinterpret_cast<float*>(base + jp.orows_off);
+      const Job& J = jp.J;
       ta.ws[nt] = J.ws;
       ta.hs[nt] = J.hs;
       ta.ho[nt] = J.ho;
@@ -1736,7 +2000,6 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
       ta.srows[nt] = const_cast<float*>(J.src_rows);
       ta.orows[nt] = const_cast<float*>(J.out_rows);
       if (!jp.narrow && !jp.paired) {  // a tensor launch: its visible-offset windows
-        J.vis = reinterpret_cast<const int*>(base + jp.vis_off);
         ta.vis[nt] = const_cast<int*>(J.vis);
         ta.ntiles[nt] = (J.ho + kM - 1) / kM;
         ta.ho_b[nt] = jp.pair_with >= 0 ? P.jobs[jp.pair_with].J.ho : 0;
@@ -1752,6 +2015,7 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
   // one (they need the tables, nothing else of the tensor path).
   bool any_narrow = false;
   for (const JobPlan& jp : P.jobs) any_narrow |= jp.narrow;
+  if (!narrow) return cuda_status(cudaGetLastError(), "tensor path prep launch");
   cudaStream_t ns = s;
   if (side && any_narrow) {
     e = cudaEventRecord(side->fork, s);
@@ -1759,111 +2023,92 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     if (e != cudaSuccess) return cuda_status(e, "tc side-stream fork");
     ns = side->stream;
   }
-  static_assert(sizeof(FinishArgs) <= 32000, "finish arguments fit the kernel parameter space");
-  FinishArgs fa;
-  memset(&fa, 0, sizeof(fa));
-  int finish_blocks = 0;
-  for (size_t k = 0; k < P.jobs.size(); ++k) {
-    JobPlan& jp = P.jobs[k];
-    void* out = nullptr;
-    long long pitch = 0;
-    if ((int)k < n) {
-      out = mips[k].out_dev;
-      pitch = (long long)(mips[k].pitch_bytes / texel);
+  *ns_out = ns;
+  return tc_launch_narrow(B, ns);
+}
+
+// The outputs summed on the CUDA cores (after the prep launches' tables).
+int tc_launch_narrow(const TcBake& B, cudaStream_t ns) {
+  const TcPlan& P = B.P;
+  char* base = B.base;
+  cudaError_t e;
+  for (const JobPlan& jp : P.jobs) {
+    if (!jp.narrow) continue;
+    const Job& J = jp.J;
+    NarrowJob nj;
+    nj.src = reinterpret_cast<const float4*>(B.chain) + B.tab.off[jp.src_level];
+    nj.ws = J.ws;
+    nj.hs = J.hs;
+    nj.wo = J.wo;
+    nj.ho = J.ho;
+    nj.s = J.ws / J.wo;
+    nj.ksplit = J.ksplit;
+    nj.a2 = J.a2;
+    nj.cos_d = J.cos_d;
+    nj.src_rows = J.src_rows;
+    nj.out_rows = J.out_rows;
+    nj.partial = reinterpret_cast<double*>(base + jp.partial_off);
+    // dynamic part; with the 8 KB static reduction buffer it can pass the
+    // 48 KB default, so the limit is always raised to what this job needs
+    const int smem = (int)narrow_smem_bytes(J.ws, J.wo);
+    const dim3 grid(J.ho, J.ksplit);
+    if (J.kind == 0) {
+      e = cudaFuncSetAttribute(narrow_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               smem);
+      if (e != cudaSuccess) return cuda_status(e, "tc narrow smem attribute");
+      narrow_kernel<0><<<grid, kNarrowThreads, smem, ns>>>(nj);
     } else {
-      out = irr_out;
-      pitch = (long long)(irr_pitch / texel);
+      e = cudaFuncSetAttribute(narrow_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               smem);
+      if (e != cudaSuccess) return cuda_status(e, "tc narrow smem attribute");
+      narrow_kernel<1><<<grid, kNarrowThreads, smem, ns>>>(nj);
     }
-    if (jp.narrow) {
-      const Job& J = jp.J;
-      NarrowJob nj;
-      nj.src = reinterpret_cast<const float4*>(chain) + tab.off[jp.src_level];
-      nj.ws = J.ws;
-      nj.hs = J.hs;
-      nj.wo = J.wo;
-      nj.ho = J.ho;
-      nj.s = J.ws / J.wo;
-      nj.ksplit = J.ksplit;
-      nj.a2 = J.a2;
-      nj.cos_d = J.cos_d;
-      nj.src_rows = J.src_rows;
-      nj.out_rows = J.out_rows;
-      nj.partial = reinterpret_cast<double*>(base + jp.partial_off);
-      // dynamic part; with the 8 KB static reduction buffer it can pass the
-      // 48 KB default, so the limit is always raised to what this job needs
-      const int smem = (int)narrow_smem_bytes(J.ws, J.wo);
-      const dim3 grid(J.ho, J.ksplit);
-      if (J.kind == 0) {
-        e = cudaFuncSetAttribute(narrow_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem);
-        if (e != cudaSuccess) return cuda_status(e, "tc narrow smem attribute");
-        narrow_kernel<0><<<grid, kNarrowThreads, smem, ns>>>(nj);
-      } else {
-        e = cudaFuncSetAttribute(narrow_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem);
-        if (e != cudaSuccess) return cuda_status(e, "tc narrow smem attribute");
-        narrow_kernel<1><<<grid, kNarrowThreads, smem, ns>>>(nj);
-      }
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return cuda_status(e, "tc narrow launch");
-      narrow_finish_kernel<<<J.wo * J.ho, 32, 0, ns>>>(nj, J.kind, out, pitch, out_half);
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return cuda_status(e, "tc narrow finish launch");
-      continue;
-    }
-    if (jp.level < 0) continue;
-    Job& J = jp.J;
-    const LevelPlanes& L = P.levels[jp.level];
-    J.src = reinterpret_cast<const __nv_bfloat16*>(base + L.offset);
-    J.partial = reinterpret_cast<float*>(base + jp.partial_off);
-    J.wsum_part = reinterpret_cast<double*>(base + jp.wsum_off);
-    J.error = reinterpret_cast<int*>(base);
-    J.out_half = out_half;
-    // every tensor job's finish runs in one launch after the contractions
-    if (fa.n >= kMaxFinishJobs) return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "tc: too many jobs");
-    fa.job[fa.n] = J;
-    fa.out[fa.n] = out;
-    fa.pitch[fa.n] = pitch;
-    fa.begin[fa.n] = finish_blocks;
-    finish_blocks +=
-        (int)(((long long)((J.ho + kFinishRows - 1) / kFinishRows) * J.wo + 31) / 32);
-    ++fa.n;
-    if (jp.paired) continue;  // contracted inside its partner's launch
-    J.pair = 0;
-    if (jp.pair_with >= 0) {
-      const JobPlan& bp = P.jobs[jp.pair_with];
-      J.pair = 1;
-      J.ho_b = bp.J.ho;
-      J.kind_b = bp.J.kind;
-      J.a2_b = bp.J.a2;
-      J.out_rows_b = reinterpret_cast<const float*>(base + bp.orows_off);
-      J.partial_b = reinterpret_cast<float*>(base + bp.partial_off);
-      J.wsum_part_b = reinterpret_cast<double*>(base + bp.wsum_off);
-    }
-    // At least 120 KB so no two CTAs share an SM (each allocates all of TMEM),
-    // and room for a K interleave's quarter sums ([4][3 nb][32] floats).
-    int smem = (int)smem_plan(J).total;
-    if (smem < 120 * 1024) smem = 120 * 1024;
-    if (J.kinter > 1 && smem < 4 * 3 * J.nb * 32 * 4) smem = 4 * 3 * J.nb * 32 * 4;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e, "tc narrow launch");
+    narrow_finish_kernel<<<J.wo * J.ho, 32, 0, ns>>>(nj, J.kind, jp.out, jp.pitch, B.out_half);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e, "tc narrow finish launch");
+  }
+  return cuda_status(cudaGetLastError(), "tensor path prep launch");
+}
+
+// Dynamic shared memory of a contraction CTA of job J: its staging slots and
+// cos table, at least 120 KB so that no two CTAs share an SM (each allocates
+// all of TMEM), and room for a K interleave's quarter sums.
+int contract_smem(const Job& J) {
+  int smem = (int)smem_plan(J).total;
+  if (smem < 120 * 1024) smem = 120 * 1024;
+  if (J.kinter > 1 && smem < 4 * 3 * J.nb * 32 * 4) smem = 4 * 3 * J.nb * 32 * 4;
+  return smem;
+}
+
+int tc_launch_contract(const TcBake& B, cudaStream_t s) {
+  for (int k : B.launch_jobs) {
+    const Job& J = B.P.jobs[k].J;
+    const int smem = contract_smem(J);
     dim3 grid((J.ho + kM - 1) / kM, J.m * J.nblk, J.ksplit);
     auto kern = J.kind == 1 ? contract_kernel<1, false>
                             : (J.two_prod ? contract_kernel<0, true> : contract_kernel<0, false>);
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
     kern<<<grid, kThreads, smem, s>>>(J);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "tc contraction launch");
   }
-  if (fa.n > 0) {
-    fa.begin[fa.n] = finish_blocks;
-    finish_all_kernel<<<finish_blocks, kFinishThreads, 0, s>>>(fa);
+  return ALTHEA_IBL_OK;
+}
+
+int tc_launch_finish(TcBake& B, cudaStream_t s, cudaStream_t ns, const SideStream* side) {
+  cudaError_t e;
+  if (B.fa.n > 0) {
+    finish_all_kernel<<<B.finish_blocks, kFinishThreads, 0, s>>>(B.fa);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "tc finish launch");
   }
   // Roughness-0 mips are a delta (no contraction): the reflected sample itself.
-  for (int m = 0; m < n; ++m) {
-    if (P.jobs[m].level >= 0 || P.jobs[m].narrow) continue;
-    st = launch_delta_mip(chain, w, h, &mips[m], out_half, s);
+  for (int m = 0; m < B.n; ++m) {
+    if (B.P.jobs[m].level >= 0 || B.P.jobs[m].narrow) continue;
+    const int st = launch_delta_mip(B.chain, B.w, B.h, &B.mips[m], B.out_half, s);
     if (st) return st;
   }
   if (ns != s) {  // join the side stream
@@ -1872,6 +2117,22 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
     if (e != cudaSuccess) return cuda_status(e, "tc side-stream join");
   }
   return cuda_status(cudaGetLastError(), "tensor path launch");
+}
+
+int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
+            const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
+            int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream,
+            const SideStream* side) {
+  ibl::NvtxRange nvtx_range("precision bake");
+  TcBake B;
+  int st = tc_setup(chain, w, h, mips, n, levels, irr_out, irr_w, irr_h, irr_pitch, irr_level,
+                    ws, ws_bytes, out_format, B);
+  if (st) return st;
+  cudaStream_t ns = stream;
+  st = tc_launch_prep(B, stream, side, &ns);
+  if (!st) st = tc_launch_contract(B, stream);
+  if (!st) st = tc_launch_finish(B, stream, ns, side);
+  return st;
 }
 
 size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n,
@@ -1885,6 +2146,174 @@ size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n
   TcPlan P;
   if (make_plan(w, h, mips, n, levels, irr_w, irr_h, irr_level, P)) return 0;
   return P.total;
+}
+
+// ---- precision batches: one persistent contraction for every probe --------------
+struct TcBatch {
+  std::vector<TcBake*> bakes;   // one per probe
+  Job* d_jobs = nullptr;        // every contraction launch of every probe
+  WorkItem* d_items = nullptr;  // every CTA of those launches, largest first
+  unsigned int* d_next = nullptr;
+  int* d_error = nullptr;       // set by any work item whose bounded wait gave up
+  int nitems = 0, njobs = 0, smem = 0, ctas = 0;
+};
+
+void tc_batch_destroy(TcBatch* b) {
+  if (!b) return;
+  for (TcBake* B : b->bakes) delete B;
+  if (b->d_jobs) cudaFree(b->d_jobs);
+  if (b->d_items) cudaFree(b->d_items);
+  if (b->d_next) cudaFree(b->d_next);
+  if (b->d_error) cudaFree(b->d_error);
+  delete b;
+}
+
+int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, TcBatch** out) {
+  *out = nullptr;
+  TcBatch* b = new (std::nothrow) TcBatch();
+  if (!b) return set_error(ALTHEA_IBL_ERR_OUT_OF_MEMORY, "host allocation");
+  std::vector<Job> jobs;
+  struct Cand {
+    WorkItem wi;
+    long long k;  // K this CTA sums (its source rows x phase rows), for the order
+  };
+  std::vector<Cand> items;
+  for (int i = 0; i < n; ++i) {
+    const TcBatchProbe& p = probes[i];
+    TcBake* B = new (std::nothrow) TcBake();
+    if (!B) {
+      tc_batch_destroy(b);
+      return set_error(ALTHEA_IBL_ERR_OUT_OF_MEMORY, "host allocation");
+    }
+    b->bakes.push_back(B);
+    int st = tc_setup(p.chain, p.w, p.h, p.mips.data(), (int)p.mips.size(), nullptr, p.irr,
+                      p.irr_w, p.irr_h, p.irr_pitch, -1, p.ws, p.ws_bytes, out_format, *B);
+    if (st) {
+      tc_batch_destroy(b);
+      return st;
+    }
+    for (int k : B->launch_jobs) {
+      const Job& J = B->P.jobs[k].J;
+      const int jid = (int)jobs.size();
+      jobs.push_back(J);
+      b->smem = std::max(b->smem, contract_smem(J));
+      const int gx = (J.ho + kM - 1) / kM, gy = J.m * J.nblk, gz = J.ksplit;
+      for (int bz = 0; bz < gz; ++bz) {
+        const long long rows = (J.hs - bz + gz - 1) / gz;  // rows bz, bz + gz, ...
+        for (int by = 0; by < gy; ++by)
+          for (int bx = 0; bx < gx; ++bx)
+            items.push_back(Cand{WorkItem{jid, bx, by, bz}, rows * J.g * J.kpad});
+      }
+    }
+  }
+  std::stable_sort(items.begin(), items.end(),
+                   [](const Cand& a, const Cand& c) { return a.k > c.k; });
+  std::vector<WorkItem> wi(items.size());
+  for (size_t k = 0; k < items.size(); ++k) wi[k] = items[k].wi;
+  b->njobs = (int)jobs.size();
+  b->nitems = (int)wi.size();
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  b->ctas = sms > 0 ? sms : 1;
+  if (e == cudaSuccess && b->njobs > 0) e = cudaMalloc(&b->d_jobs, sizeof(Job) * jobs.size());
+  if (e == cudaSuccess && b->nitems > 0)
+    e = cudaMalloc(&b->d_items, sizeof(WorkItem) * wi.size());
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_next, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_error, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(b->d_error, 0, sizeof(int));
+  for (Job& J : jobs) J.error = b->d_error;  // one status word for the whole batch
+  if (e == cudaSuccess && b->njobs > 0)
+    e = cudaMemcpy(b->d_jobs, jobs.data(), sizeof(Job) * jobs.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && b->nitems > 0)
+    e = cudaMemcpy(b->d_items, wi.data(), sizeof(WorkItem) * wi.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && b->smem > 0)
+    e = cudaFuncSetAttribute(contract_persistent_kernel,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem);
+  if (e != cudaSuccess) {
+    tc_batch_destroy(b);
+    return cuda_status(e, "precision batch plan");
+  }
+  *out = b;
+  return ALTHEA_IBL_OK;
+}
+
+int tc_batch_items(const TcBatch* b) { return b ? b->nitems : 0; }
+
+int tc_batch_error(const TcBatch* b, cudaStream_t st) {
+  int flag = 0;
+  cudaError_t e = cudaMemcpyAsync(&flag, b->d_error, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "precision batch status");
+  if (flag)
+    return set_error(ALTHEA_IBL_ERR_CUDA, "precision batch: a bounded wait timed out");
+  return ALTHEA_IBL_OK;
+}
+
+int tc_batch_run(TcBatch* b, cudaStream_t st, const cudaStream_t* lanes, int nlanes,
+                 const int* lane_of, cudaEvent_t fork_ev, const cudaEvent_t* join_ev) {
+  ibl::NvtxRange nvtx_range("precision batch");
+  auto fork = [&]() -> cudaError_t {
+    cudaError_t e = cudaEventRecord(fork_ev, st);
+    for (int l = 0; l < nlanes && e == cudaSuccess; ++l)
+      e = cudaStreamWaitEvent(lanes[l], fork_ev, 0);
+    return e;
+  };
+  auto join = [&]() -> cudaError_t {
+    cudaError_t r = cudaSuccess;
+    for (int l = 0; l < nlanes; ++l) {
+      cudaError_t e = cudaEventRecord(join_ev[l], lanes[l]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, join_ev[l], 0);
+      if (e != cudaSuccess && r == cudaSuccess) r = e;
+    }
+    return r;
+  };
+  // each probe's split planes and tables, on lanes
+  cudaError_t e = fork();
+  if (e != cudaSuccess) return cuda_status(e, "precision batch fork");
+  int r = ALTHEA_IBL_OK;
+  for (size_t i = 0; i < b->bakes.size() && !r; ++i) {
+    cudaStream_t ns;
+    r = tc_launch_prep(*b->bakes[i], lanes[lane_of[i]], nullptr, &ns, false);
+  }
+  e = join();  // also after an error, so that a stream capture can end cleanly
+  if (r) return r;
+  if (e != cudaSuccess) return cuda_status(e, "precision batch join");
+  // Every contraction of every probe: one persistent launch over the queue.
+  // The CUDA-core outputs go to the lanes after it is launched (its CTAs are
+  // placed first; a contraction CTA leaves no registers for another block),
+  // and take the SMs that the persistent kernel leaves as its queue drains.
+  e = cudaEventRecord(fork_ev, st);
+  if (e != cudaSuccess) return cuda_status(e, "precision batch fork");
+  if (b->nitems > 0) {
+    e = cudaMemsetAsync(b->d_next, 0, sizeof(unsigned int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_error, 0, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_status(e, "precision batch queue reset");
+    contract_persistent_kernel<<<b->ctas, kThreads, b->smem, st>>>(b->d_jobs, b->d_items,
+                                                                   b->nitems, b->d_next);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e, "precision batch contraction launch");
+  }
+  for (int l = 0; l < nlanes && e == cudaSuccess; ++l)
+    e = cudaStreamWaitEvent(lanes[l], fork_ev, 0);
+  if (e != cudaSuccess) return cuda_status(e, "precision batch fork");
+  for (size_t i = 0; i < b->bakes.size() && !r; ++i)
+    r = tc_launch_narrow(*b->bakes[i], lanes[lane_of[i]]);
+  if (r) {
+    join();
+    return r;
+  }
+  // each probe's split sums and roughness-0 mips, on lanes (after its
+  // CUDA-core outputs there and the contraction)
+  e = fork();
+  if (e != cudaSuccess) return cuda_status(e, "precision batch fork");
+  for (size_t i = 0; i < b->bakes.size() && !r; ++i) {
+    cudaStream_t l = lanes[lane_of[i]];
+    r = tc_launch_finish(*b->bakes[i], l, l, nullptr);
+  }
+  e = join();
+  if (r) return r;
+  return cuda_status(e, "precision batch join");
 }
 
 }  // namespace ibl

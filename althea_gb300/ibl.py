@@ -90,7 +90,8 @@ class BatchParams(ctypes.Structure):
 class BatchInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in (
         "probes", "prefilter_jobs", "prefilter_tiles", "irradiance_blocks", "tile_x", "tile_y",
-        "persistent_blocks", "irradiance_target_blocks", "tuned", "graph", "graph_kernels")]
+        "persistent_blocks", "irradiance_target_blocks", "tuned", "graph", "graph_kernels",
+        "contraction_items")]
 
 
 BATCH_AUTOTUNE = 1
@@ -184,6 +185,7 @@ def load(build_if_missing: bool = True):
                                         ctypes.POINTER(vp)]),
         "althea_ibl_batch_run": (i, [vp, vp]),
         "althea_ibl_batch_describe": (i, [vp, ctypes.POINTER(BatchInfo)]),
+        "althea_ibl_batch_status": (i, [vp, vp]),
         "althea_ibl_batch_destroy": (i, [vp]),
         "althea_ibl_server_create": (i, [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]),
         "althea_ibl_server_submit": (i, [vp, ctypes.POINTER(Request)]),
@@ -721,6 +723,11 @@ class ProbeBatch:
 
     def run(self, stream=None) -> None:
         _check(load().althea_ibl_batch_run(self._plan, _stream_ptr(stream)))
+
+    def status(self, stream=None) -> None:
+        """Synchronises `stream`; raises when a bounded wait of the last run's
+        contraction gave up (its outputs are then undefined)."""
+        _check(load().althea_ibl_batch_status(self._plan, _stream_ptr(stream)))
 
     def info(self) -> BatchInfo:
         inf = BatchInfo()

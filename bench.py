@@ -931,6 +931,29 @@ def batch_envs(specs, seed0, sun_max, dev):
     return envs
 
 
+def batch_equals_solo(batch, specs, envs):
+    """The widest and the narrowest probe of a precision batch against their
+    own single bakes (stateless tensor-path calls, one launch per
+    contraction): True when every output is the same bits."""
+    import torch
+    from althea_gb300 import ibl
+    order = sorted(range(len(specs)), key=lambda i: specs[i].env_width)
+    for i in {order[0], order[-1]}:
+        s, env = specs[i], envs[i]
+        chain = ibl.build_env_chain(env)
+        mips = [torch.empty((h, w, 4), dtype=torch.float32, device=env.device)
+                for w, h in s.mip_sizes]
+        iw, ih = s.irradiance_size
+        irr = torch.empty((ih, iw, 4), dtype=torch.float32, device=env.device)
+        ibl.bake_tc(chain, s.env_width, s.env_height, mips, s.roughness, irradiance=irr)
+        torch.cuda.synchronize()
+        same = torch.equal(batch.chains[i], chain) and torch.equal(batch.irradiance[i], irr.half())
+        same = same and all(torch.equal(batch.mips[i][m], mips[m].half()) for m in range(len(mips)))
+        if not same:
+            return False
+    return True
+
+
 def measure_batch(n, precision, sun_max, steps, warmup, seed=0, clocks=None):
     """A batch of n probes of the batching configuration (widths uniform over
     256..2048, log2(W)-3 mips, 32x16 irradiance, one shared 256x256 LUT) as
@@ -958,7 +981,7 @@ def measure_batch(n, precision, sun_max, steps, warmup, seed=0, clocks=None):
             batch.run(stream)
             b.record(stream)
             evs.append((a, b))
-    torch.cuda.synchronize()
+    batch.status(stream)  # raises if a bounded wait of the contraction gave up
     ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
     info = batch.info()
     widths = {}
@@ -970,6 +993,8 @@ def measure_batch(n, precision, sun_max, steps, warmup, seed=0, clocks=None):
            "persistent_blocks": info.persistent_blocks,
            "irradiance_target_blocks": info.irradiance_target_blocks}
     if precision:
+        out["contraction_items"] = info.contraction_items
+        out["outputs_equal_solo_bakes"] = batch_equals_solo(batch, specs, envs)
         tpeak, tkind = read_tensor_peak()
         tflops = batch_tc_flops(specs) / (ms / 1e3) / 1e12
         out["roofline"] = {"bound": "tensor", "achieved": tflops, "peak": tpeak,

@@ -296,8 +296,14 @@ typedef struct {
 
 #define ALTHEA_IBL_BATCH_AUTOTUNE 1
 #define ALTHEA_IBL_BATCH_GRAPH 2
-/* Mips and irradiance by the precision path (althea_ibl_bake_tc_ex per probe
- * after the shared chain pass; probes of one shape share a workspace). */
+/* Mips and irradiance by the precision path, after the shared chain pass:
+ * every probe's split planes and tables, then ONE persistent tcgen05
+ * contraction kernel draining a queue of (probe output, row tile, column
+ * block, source split) work items of every probe, largest first, then every
+ * probe's finish.  Each probe gets its own workspace of
+ * althea_ibl_tc_workspace_size bytes.  Results are identical to
+ * althea_ibl_bake_tc_ex of each probe alone (planner's levels); check them
+ * with althea_ibl_batch_status. */
 #define ALTHEA_IBL_BATCH_PRECISION 4
 /* With ALTHEA_IBL_BATCH_PRECISION: RGBA16F outputs (8-byte texels). */
 #define ALTHEA_IBL_BATCH_HALF 8
@@ -321,6 +327,7 @@ typedef struct {
   int tuned;                 /* 1 if the choice came from timing (now or cached) */
   int graph;                 /* 1 once the bake is a captured CUDA graph */
   int graph_kernels;         /* kernel launches in that graph (-1 before capture) */
+  int contraction_items;     /* precision: work items of the persistent contraction */
 } althea_ibl_batch_info;
 
 typedef struct althea_ibl_batch althea_ibl_batch;
@@ -333,6 +340,10 @@ int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
 /* Bakes every probe (chains when level0_dev is set, mips, irradiance, LUT). */
 int althea_ibl_batch_run(althea_ibl_batch* batch, void* stream);
 int althea_ibl_batch_describe(const althea_ibl_batch* batch, althea_ibl_batch_info* info);
+/* Synchronises `stream` and reports the last run: ALTHEA_IBL_ERR_CUDA when a
+ * bounded wait of the precision path's contraction gave up (the outputs of
+ * that run are then undefined), else ALTHEA_IBL_OK. */
+int althea_ibl_batch_status(const althea_ibl_batch* batch, void* stream);
 int althea_ibl_batch_destroy(althea_ibl_batch* batch);
 
 /* ---- analytic sun lobes ---------------------------------------------------------
