@@ -63,20 +63,6 @@ struct IrrJob {
   long long partial_offset;
 };
 
-// Index of the last range whose begin <= key (begins ascending, begins[0] = 0).
-__device__ __forceinline__ int find_range(const long long* __restrict__ begins, int n,
-                                          long long key) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (begins[mid] <= key)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
 __global__ void __launch_bounds__(256) batch_blit_kernel(const BlitJob* __restrict__ jobs,
                                                          const long long* __restrict__ begins,
                                                          int njobs) {
@@ -191,8 +177,6 @@ constexpr TileShape kTileShapes[] = {{16, 8}, {32, 4}, {8, 8}, {16, 16}};
 constexpr int kNumTileShapes = 4;
 constexpr int kIrrTargets[] = {152 * 4, 152 * 8, 152 * 16};
 constexpr int kNumIrrTargets = 3;
-// Streams the precision bakes of a batch are spread over.
-constexpr int kTcLanes = 4;
 
 typedef void (*PfKernel)(const PfJob*, const long long*, int, long long, int, int, int,
                          unsigned long long*);
@@ -287,18 +271,16 @@ struct althea_ibl_batch {
   cudaStream_t exec_stream = nullptr;
   int graph_kernels = -1;  // kernel nodes of the captured bake (-1: not captured)
   // precision path (ALTHEA_IBL_BATCH_PRECISION), after the shared chain
-  // pass: every probe's split planes, tables and CUDA-core outputs on
-  // kTcLanes streams forked from the caller's, ONE persistent tcgen05
-  // contraction over the work items of every probe, then every probe's finish
-  // on the lanes (joined back before the run ends).  Each probe has its own
-  // workspace: all of their contractions are in flight at once.
+  // pass: the split passes of every probe, ONE persistent tcgen05
+  // contraction over the work items of every probe and every probe's finish,
+  // with the CUDA-core outputs on a side stream (joined back before the run
+  // ends); a handful of launches in all.  Each probe has its own workspace:
+  // all of their contractions are in flight at once.
   bool precision = false;
-  std::vector<cudaStream_t> lanes;
-  cudaEvent_t fork_ev = nullptr;
-  std::vector<cudaEvent_t> join_ev;
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int out_format = ALTHEA_IBL_FORMAT_RGBA32F;
   std::vector<void*> tc_ws;   // one per probe
-  std::vector<int> tc_lane;   // lane of each probe
   ibl::TcBatch* tcb = nullptr;
 };
 
@@ -318,8 +300,8 @@ void free_batch(althea_ibl_batch* b) {
   cudaFree(b->d_partial);
   tc_batch_destroy(b->tcb);
   for (void* p : b->tc_ws) cudaFree(p);
-  for (cudaStream_t l : b->lanes) cudaStreamDestroy(l);
-  for (cudaEvent_t e : b->join_ev) cudaEventDestroy(e);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->join_ev) cudaEventDestroy(b->join_ev);
   if (b->fork_ev) cudaEventDestroy(b->fork_ev);
   delete b;
 }
@@ -464,8 +446,7 @@ int launch_irradiance_batch(althea_ibl_batch* b, cudaStream_t st) {
 }
 
 int launch_tc(althea_ibl_batch* b, cudaStream_t st) {
-  return tc_batch_run(b->tcb, st, b->lanes.data(), (int)b->lanes.size(), b->tc_lane.data(),
-                      b->fork_ev, b->join_ev.data());
+  return tc_batch_run(b->tcb, st, b->side, b->fork_ev, b->join_ev);
 }
 
 int launch_all(althea_ibl_batch* b, cudaStream_t st) {
@@ -657,39 +638,15 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
   // ---- precision path: one planned tensor-core bake per probe --------------
   if (precision) {
     // Lanes: longest-processing-time assignment by level-0 area.
-    const int nl = std::min(kTcLanes, n);
-    for (int l = 0; l < nl; ++l) {
-      cudaStream_t ls = nullptr;
-      cudaEvent_t ev = nullptr;
-      cudaError_t e = cudaStreamCreateWithFlags(&ls, cudaStreamNonBlocking);
-      if (e == cudaSuccess) b->lanes.push_back(ls);
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-      if (e == cudaSuccess) b->join_ev.push_back(ev);
-      if (e != cudaSuccess) {
-        free_batch(b);
-        return cuda_status(e, "precision lanes");
-      }
-    }
     {
-      cudaError_t e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+      cudaError_t e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming);
       if (e != cudaSuccess) {
         free_batch(b);
-        return cuda_status(e, "precision lanes");
+        return cuda_status(e, "precision side stream");
       }
     }
-    std::vector<int> order(n), lane_of(n, 0);
-    for (int i = 0; i < n; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
-      return (double)probes[a].env_width * probes[a].env_height >
-             (double)probes[c].env_width * probes[c].env_height;
-    });
-    std::vector<double> load(nl, 0.0);
-    for (int i : order) {
-      const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-      lane_of[i] = l;
-      load[l] += (double)probes[i].env_width * probes[i].env_height;
-    }
-    b->tc_lane = lane_of;
     std::vector<TcBatchProbe> tp(n);
     for (int i = 0; i < n; ++i) {
       const althea_ibl_probe& p = probes[i];
@@ -726,7 +683,7 @@ extern "C" int althea_ibl_batch_create(const althea_ibl_probe* probes, int n,
       b->tc_ws.push_back(ws);
       t.ws = ws;
     }
-    int r = tc_batch_create(tp.data(), n, b->out_format, &b->tcb);
+    int r = tc_batch_create(tp.data(), n, b->out_format, st, &b->tcb);
     if (r) {
       free_batch(b);
       return r;

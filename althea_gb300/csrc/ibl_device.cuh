@@ -62,6 +62,22 @@ __host__ __device__ inline void make_table(int w, int h, ChainTable* t) {
   }
 }
 
+// Job tables of batched launches: the index of the last range whose begin
+// <= key (begins ascending, begins[0] = 0), so block b of a launch belongs to
+// job find_range(begins, n, b) as its block b - begins[job].
+__device__ __forceinline__ int find_range(const long long* __restrict__ begins, int n,
+                                          long long key) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (begins[mid] <= key)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 // Index wrap for REPEAT.  Texel coordinates normally lie in [-1, n]; the
 // general branch keeps any input (even from NaN) in bounds.
 __device__ __forceinline__ int wrap_repeat(int i, int n) {

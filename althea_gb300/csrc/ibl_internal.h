@@ -49,6 +49,17 @@ int launch_irradiance(const float* chain, int w, int h, float* out, int ow, int 
 // out_half: RGBA16F output (8-byte texels) instead of RGBA32F.
 int launch_delta_mip(const float* chain, int w, int h, const althea_ibl_mip_target* mip,
                      int out_half, cudaStream_t st);
+// Delta mips of many probes in one launch (ibl_plain.cu): job k covers
+// blocks [begins[k], begins[k + 1]) of 32 x 8 texels, blocks_x per row.
+struct DeltaJob {
+  const float* chain;
+  int w, h;
+  void* out;
+  long long pitch;  // texels
+  int ow, oh, out_half, blocks_x;
+};
+int launch_delta_batch(const DeltaJob* d_jobs, const long long* d_begins, int njobs,
+                       long long blocks, cudaStream_t st);
 
 // A second stream for work that does not feed the tensor-core contractions
 // (the outputs summed on the CUDA cores): forked from the bake's stream after
@@ -70,10 +81,12 @@ size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n
                           const int* levels, int irr_w, int irr_h, int irr_level);
 
 // Precision batches (ibl_tc.cu): every probe planned with the planner's
-// levels into its own workspace; a run launches each probe's split planes and
-// tables on its lane, then ONE persistent contraction kernel over a queue of
-// (job, row tile, column block, split) work items of every probe, then each
-// probe's finish on its lane.  The results equal the probes' single bakes.
+// levels into its own workspace, its tables computed once at creation.  A
+// run launches the split passes of every probe (one launch), ONE persistent
+// contraction kernel over a queue of (job, row tile, column block, split)
+// work items of every probe, then every probe's finish (one launch); the
+// narrow outputs and roughness-0 mips go to `side` beside them (one launch
+// each).  The results equal the probes' single bakes.
 struct TcBatchProbe {
   const float* chain;
   int w, h;
@@ -85,9 +98,12 @@ struct TcBatchProbe {
   size_t ws_bytes;
 };
 struct TcBatch;
-int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, TcBatch** out);
-int tc_batch_run(TcBatch* b, cudaStream_t st, const cudaStream_t* lanes, int nlanes,
-                 const int* lane_of, cudaEvent_t fork_ev, const cudaEvent_t* join_ev);
+// Builds the plan and the device job tables, and computes every probe's
+// tables on `st` (synchronised before it returns).
+int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, cudaStream_t st,
+                    TcBatch** out);
+int tc_batch_run(TcBatch* b, cudaStream_t st, cudaStream_t side, cudaEvent_t fork_ev,
+                 cudaEvent_t join_ev);
 int tc_batch_items(const TcBatch* b);
 // Synchronises `st` and reports a work item whose bounded wait gave up.
 int tc_batch_error(const TcBatch* b, cudaStream_t st);

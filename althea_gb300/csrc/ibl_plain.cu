@@ -126,15 +126,11 @@ __global__ void __launch_bounds__(kPfTileX* kPfTileY) prefilter_kernel(const Pre
 // that every kept sample of PreFilterEnvMap.comp:147-167 repeats (H = N, first
 // Hammersley point), without repeating its accumulation.  The precision path
 // uses it for roughness-0 mips (its quadrature of a delta).
-__global__ void __launch_bounds__(256) delta_mip_kernel(const float4* __restrict__ chain, int w,
-                                                        int h, void* __restrict__ out,
-                                                        long long pitch, int ow, int oh,
-                                                        int out_half) {
-  __shared__ ChainTable tab;
-  if (threadIdx.x == 0) make_table(w, h, &tab);
-  __syncthreads();
-  const int x = blockIdx.x * 32 + (int)(threadIdx.x & 31);
-  const int y = blockIdx.y * 8 + (int)(threadIdx.x >> 5);
+// Texel (x, y) of a delta mip (the caller's 32 x 8 block of 256 threads).
+__device__ __forceinline__ void delta_texel(const float4* __restrict__ chain,
+                                            const ChainTable& tab, void* __restrict__ out,
+                                            long long pitch, int ow, int oh, int out_half, int x,
+                                            int y) {
   if (x >= ow || y >= oh) return;
   Float3 n = texel_dir(x, y, ow, oh);
   Float3 t, b;
@@ -160,6 +156,36 @@ __global__ void __launch_bounds__(256) delta_mip_kernel(const float4* __restrict
   }
 }
 
+__global__ void __launch_bounds__(256) delta_mip_kernel(const float4* __restrict__ chain, int w,
+                                                        int h, void* __restrict__ out,
+                                                        long long pitch, int ow, int oh,
+                                                        int out_half) {
+  __shared__ ChainTable tab;
+  if (threadIdx.x == 0) make_table(w, h, &tab);
+  __syncthreads();
+  delta_texel(chain, tab, out, pitch, ow, oh, out_half,
+              blockIdx.x * 32 + (int)(threadIdx.x & 31), blockIdx.y * 8 + (int)(threadIdx.x >> 5));
+}
+
+// The delta mips of many probes in one launch: block b is block b - begins[k]
+// of job k's (ceil(ow / 32) x ceil(oh / 8)) grid, row-major.
+__global__ void __launch_bounds__(256) delta_batch_kernel(const DeltaJob* __restrict__ jobs,
+                                                          const long long* __restrict__ begins,
+                                                          int njobs) {
+  __shared__ ChainTable tab;
+  __shared__ int k_sh;
+  if (threadIdx.x == 0) {
+    k_sh = find_range(begins, njobs, blockIdx.x);
+    make_table(jobs[k_sh].w, jobs[k_sh].h, &tab);
+  }
+  __syncthreads();
+  const DeltaJob& j = jobs[k_sh];
+  const long long local = (long long)blockIdx.x - begins[k_sh];
+  const int bx = (int)(local % j.blocks_x), by = (int)(local / j.blocks_x);
+  delta_texel(reinterpret_cast<const float4*>(j.chain), tab, j.out, j.pitch, j.ow, j.oh,
+              j.out_half, bx * 32 + (int)(threadIdx.x & 31), by * 8 + (int)(threadIdx.x >> 5));
+}
+
 int launch_delta_mip(const float* chain, int w, int h, const althea_ibl_mip_target* mip,
                      int out_half, cudaStream_t st) {
   dim3 grid((mip->width + 31) / 32, (mip->height + 7) / 8);
@@ -168,6 +194,13 @@ int launch_delta_mip(const float* chain, int w, int h, const althea_ibl_mip_targ
                                          (long long)(mip->pitch_bytes / (out_half ? 8 : 16)),
                                          mip->width, mip->height, out_half);
   return cuda_status(cudaGetLastError(), "delta mip launch");
+}
+
+int launch_delta_batch(const DeltaJob* d_jobs, const long long* d_begins, int njobs,
+                       long long blocks, cudaStream_t st) {
+  if (njobs <= 0 || blocks <= 0) return ALTHEA_IBL_OK;
+  delta_batch_kernel<<<(unsigned)blocks, 256, 0, st>>>(d_jobs, d_begins, njobs);
+  return cuda_status(cudaGetLastError(), "delta batch launch");
 }
 
 int launch_prefilter(const float* chain, int w, int h, const althea_ibl_mip_target* mips,

@@ -82,9 +82,9 @@ constexpr int kNBMax = 128;       // MMA N (columns) per CTA
 constexpr int kACol = 3 * kNBMax; // first A stage column (accumulators before it)
 constexpr int kTmemCols = 512;
 constexpr int kProducerWarps = 16;  // four per TMEM lane quarter, 8 K each per stage
-constexpr int kMmaWarp0 = 16;       // MMA issuers: (colour channel, column half)
-constexpr int kMmaWarps = 6;
-constexpr int kLoaderWarp = 22;
+constexpr int kMmaWarp0 = 16;       // MMA issuers: one per colour channel
+constexpr int kMmaWarps = 3;
+constexpr int kLoaderWarp = 19;
 constexpr int kThreads = 32 * (kLoaderWarp + 1);
 static_assert(kMmaWarp0 == kProducerWarps && kLoaderWarp == kMmaWarp0 + kMmaWarps, "warp roles");
 static_assert(kACol + kStages * kKS <= kTmemCols, "TMEM columns");
@@ -94,6 +94,7 @@ constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr uint32_t kSleepNs = 200000;  // longest hardware suspension per try (0.2 ms)
 constexpr float kPiF = 3.14159265358979f;
 constexpr int kSmemLimit = 232448;  // opt-in shared memory per block
+constexpr int kCtN = 64;            // column tiles: weight rows (MMA N)
 
 // ---- PTX wrappers -------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -390,7 +391,6 @@ struct Job {
   int nres, nb, nblk;        // columns per residue x0, MMA N, column blocks per residue
   int rlen;                  // staged row length (bf16 elements, multiple of 8)
   int nslots;                // staged rows in flight (2..kMaxSlots)
-  int nsplit;                // MMA issuers per channel (column halves): 2 when nb % 32 == 0
   int kind;                  // 0 = GGX prefilter, 1 = irradiance
   float a2;                  // roughness^2
   int ksplit;                // source rows are split over this many CTAs
@@ -404,9 +404,10 @@ struct Job {
   int two_prod;              // 1: BF16 hi weights only (two products per channel), weight
                              // sum over the rounded weights; 0: hi/lo weights (three)
   // A second output of the same geometry (same source level, phase count,
-  // columns) in TMEM lanes 64-127, so that two outputs of <= 64 rows fill one
-  // M = 128 tile: they share every radiance operand, only the weights differ.
-  // K interleave (outputs of <= 32 rows): every lane quarter holds the same
+  // columns) in the same CTA: they share every radiance operand, only the
+  // weights differ.  Row tiles: TMEM lanes 64-127, so that two outputs of
+  // <= 64 rows fill one M = 128 tile.
+  // K interleave (row tiles of <= 32 rows): every lane quarter holds the same
   // rows and owns every fourth K stage (stage slot q), so the weight work of
   // one quarter spreads over the four SM sub-partitions; the CTA adds the
   // quarters' sums before writing one partial per split.
@@ -419,23 +420,36 @@ struct Job {
   const int* vis;
   int kinter;                // 1 or 4
   int nparts;                // partial sums the finish adds: ksplit
-  int pair;                  // 1: lanes 64-127 hold the second output
+  int pair;                  // 1: a second output (ho_b rows) is contracted too
   int ho_b, kind_b;
   float a2_b;
   const float* out_rows_b;   // [ho_b][2]
   float* partial_b;          // [ksplit][3][wo][ho_b]
   double* wsum_part_b;       // [ksplit][ho_b]  (kind_b 0)
+  // Column tiles (unpaired outputs of 33 to 64 rows): the staged radiance
+  // Hankel is the A operand (M = 128 output columns, nb = 128) and the
+  // weights the B operand (N = kCtN = 64 rows), written by the producers to
+  // shared memory.
+  int ct;
 };
 
+// Weight stages of a column-tile CTA: K-major, no swizzle; per stage and
+// plane, KS/8 groups of 8 K, each kCtN rows x 16 bytes (row i at
+// (i / 8) 128 + (i % 8) 16).  Three products: hi and lo planes of 32 K; two
+// products: the hi plane of 64 K.  Either way 128 kCtN bytes per stage.
+__host__ __device__ inline size_t ct_stage_bytes(const Job& J) { return (size_t)128 * kCtN; }
+
 struct SmemPlan {
-  size_t slots, cosd, total;
+  size_t slots, cosd, bst, total;
 };
 
 __host__ __device__ inline SmemPlan smem_plan(const Job& J) {
   SmemPlan p;
   p.slots = 0;
   p.cosd = p.slots + (size_t)J.nslots * 6 * J.rlen * 2;
-  p.total = p.cosd + (size_t)J.g * J.kpad * 4;
+  const size_t end = p.cosd + (size_t)J.g * J.kpad * 4;
+  p.bst = (end + 127) & ~(size_t)127;
+  p.total = J.ct ? p.bst + kStages * ct_stage_bytes(J) : end;
   return p;
 }
 
@@ -474,6 +488,127 @@ __device__ __forceinline__ bool settle(uint64_t* bar, uint32_t parity) {
   while (!mbar_try_wait(bar, parity))
     if (global_ns() - t0 > kWaitNs) return false;
   return true;
+}
+
+// Eight weights of one output row at K = kb .. kb + 7 of phase row cdrow:
+// w = k1 c D(c) (GGX, D = 1 / (alpha + beta c)^2) or k1 c (cosine), c =
+// ccq cos_d + ssq, clamped at 0 and zero past krow; packed FP32x2 arithmetic.
+__device__ __forceinline__ void weights8(const float* cdrow, int kb, int krow, float2 ccq2,
+                                         float2 ssq2, float2 k12, float2 alpha2, float2 beta2,
+                                         bool ggx, float2 (&w)[4]) {
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const float4 cd = *reinterpret_cast<const float4*>(cdrow + kb + 4 * e);
+    const float2 c01 = __ffma2_rn(ccq2, make_float2(cd.x, cd.y), ssq2);
+    const float2 c23 = __ffma2_rn(ccq2, make_float2(cd.z, cd.w), ssq2);
+    if (ggx) {
+      const float2 d01 = __ffma2_rn(c01, beta2, alpha2);
+      const float2 d23 = __ffma2_rn(c23, beta2, alpha2);
+      const float2 q01 = __fmul2_rn(d01, d01), q23 = __fmul2_rn(d23, d23);
+      const float2 r01 = make_float2(rcp_approx(q01.x), rcp_approx(q01.y));
+      const float2 r23 = make_float2(rcp_approx(q23.x), rcp_approx(q23.y));
+      w[2 * e] = __fmul2_rn(__fmul2_rn(k12, c01), r01);
+      w[2 * e + 1] = __fmul2_rn(__fmul2_rn(k12, c23), r23);
+    } else {
+      w[2 * e] = __fmul2_rn(k12, c01);
+      w[2 * e + 1] = __fmul2_rn(k12, c23);
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    w[e].x = fmaxf(w[e].x, 0.0f);
+    w[e].y = fmaxf(w[e].y, 0.0f);
+  }
+  if (kb + 8 > krow) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (kb + u >= krow) {
+        if (u & 1)
+          w[u >> 1].y = 0.0f;
+        else
+          w[u >> 1].x = 0.0f;
+      }
+  }
+}
+
+// Hankel row loader (one thread): for every source row of split `split`
+// with a visible chunk and every phase, slot[p][t] = P_ph[(t + 8 n0) mod
+// krow], t < rlen, by bulk copies completing on slot_full.  Waits (bounded)
+// for its last copies before returning.
+__device__ __forceinline__ void load_rows(const Job& job, __nv_bfloat16* slots,
+                                          uint64_t* slot_full, uint64_t* slot_empty, int split,
+                                          int ks, int kchunks, const int* vis_row, int n0,
+                                          volatile int* abort_flag) {
+  const int u0 = (8 * n0) % job.krow;
+  long long row_id = 0;
+  bool ok = true;
+  for (int j = split; j < job.hs && ok; j += job.ksplit) {
+    int ca, cb;
+    visible_chunks(vis_row[j], job.krow, ks, kchunks, ca, cb);
+    if (ca + kchunks - cb == 0) continue;  // no visible offset: the row is not staged
+    for (int ph = 0; ph < job.g && ok; ++ph, ++row_id) {
+      const int slot = (int)(row_id % job.nslots);
+      const long long use = row_id / job.nslots;
+      if (use >= 1 && !wait_bar(&slot_empty[slot], (uint32_t)((use - 1) & 1), abort_flag)) {
+        ok = false;
+        break;
+      }
+      __nv_bfloat16* dst = slots + (size_t)slot * 6 * job.rlen;
+      mbar_expect_tx(&slot_full[slot], (uint32_t)(6 * job.rlen * 2));
+      for (int p = 0; p < 6; ++p) {
+        const __nv_bfloat16* srcrow =
+            job.src + (((size_t)p * job.hs + j) * job.g + ph) * job.krow;
+        int t = 0, u = u0;
+        while (t < job.rlen) {
+          const int len = min(job.krow - u, job.rlen - t);
+          bulk_g2s(dst + (size_t)p * job.rlen + t, srcrow + u, (uint32_t)(len * 2),
+                   &slot_full[slot]);
+          t += len;
+          u = 0;
+        }
+      }
+    }
+  }
+  // After an abort, copies may still be in flight: they land before the CTA
+  // exits (in a normal run the MMA threads have already seen every fill).
+  for (long long r = row_id > job.nslots ? row_id - job.nslots : 0; r < row_id; ++r) {
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try_wait(&slot_full[r % job.nslots], (uint32_t)((r / job.nslots) & 1)))
+      if (global_ns() - t0 > kWaitNs) break;
+  }
+}
+
+// An MMA issuer's end: every MMA it issued has completed (done_bar, which
+// every issuer commits to) and the arrivals of its last commits on the stage
+// and slot barriers have landed, so that nothing is in flight on them.
+__device__ __forceinline__ void issuer_drain(CtaShared& sh, uint32_t gidx, uint32_t row_id,
+                                             int nslots, bool ok, volatile int* abort_flag) {
+  mma_commit(&sh.done_bar);
+  if (!settle(&sh.done_bar, 0u)) *abort_flag = 1;
+  for (uint32_t st = 0; ok && st < (uint32_t)kStages && st < gidx; ++st) {
+    const uint32_t last = st + kStages * ((gidx - 1 - st) / kStages);
+    if (!settle(&sh.a_empty[st], (last / kStages) & 1u)) *abort_flag = 1;
+  }
+  const uint32_t ns_ = (uint32_t)nslots;
+  for (uint32_t sl = 0; ok && sl < ns_ && sl < row_id; ++sl) {
+    const uint32_t last = sl + ns_ * ((row_id - 1 - sl) / ns_);
+    if (!settle(&sh.slot_empty[sl], (last / ns_) & 1u)) *abort_flag = 1;
+  }
+}
+
+// Invalidates every barrier of a quiescent CTA (thread 0), for the next item.
+__device__ __forceinline__ void inval_barriers(CtaShared& sh) {
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_inval(&sh.a_full[s]);
+      mbar_inval(&sh.a_empty[s]);
+    }
+    for (int s = 0; s < kMaxSlots; ++s) {
+      mbar_inval(&sh.slot_full[s]);
+      mbar_inval(&sh.slot_empty[s]);
+    }
+    mbar_inval(&sh.done_bar);
+  }
 }
 
 // One CTA of a contraction: output rows bx * 128 .., column block by, source
@@ -522,13 +657,13 @@ __device__ __forceinline__ bool contract_cta(const Job& job, int bx, int by, int
       // arrivals per stage: the four warps of every live quarter, or of the
       // owning quarter alone (K interleave)
       mbar_init(&a_full[s], kint ? 4 : 4 * live_count);
-      mbar_init(&a_empty[s], 3 * job.nsplit);
+      mbar_init(&a_empty[s], kMmaWarps);
     }
     for (int s = 0; s < kMaxSlots; ++s) {
       mbar_init(&slot_full[s], 1);
-      mbar_init(&slot_empty[s], 3 * job.nsplit);
+      mbar_init(&slot_empty[s], kMmaWarps);
     }
-    mbar_init(&done_bar, 3 * job.nsplit);
+    mbar_init(&done_bar, kMmaWarps);
     abort_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -638,41 +773,8 @@ __device__ __forceinline__ bool contract_cta(const Job& job, int bx, int by, int
 #pragma unroll
            for (int gq = 0; gq < NG; ++gq) {
             const int kb = kc * KS + KW * h + 8 * gq;
-            // four pairs of weights with packed FP32x2 arithmetic
             float2 w[4];
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-              const float4 cd = *reinterpret_cast<const float4*>(cdrow + kb + 4 * e);
-              const float2 c01 = __ffma2_rn(ccq2, make_float2(cd.x, cd.y), ssq2);
-              const float2 c23 = __ffma2_rn(ccq2, make_float2(cd.z, cd.w), ssq2);
-              if (ggx) {
-                const float2 d01 = __ffma2_rn(c01, beta2, alpha2);
-                const float2 d23 = __ffma2_rn(c23, beta2, alpha2);
-                const float2 q01 = __fmul2_rn(d01, d01), q23 = __fmul2_rn(d23, d23);
-                const float2 r01 = make_float2(rcp_approx(q01.x), rcp_approx(q01.y));
-                const float2 r23 = make_float2(rcp_approx(q23.x), rcp_approx(q23.y));
-                w[2 * e] = __fmul2_rn(__fmul2_rn(k12, c01), r01);
-                w[2 * e + 1] = __fmul2_rn(__fmul2_rn(k12, c23), r23);
-              } else {
-                w[2 * e] = __fmul2_rn(k12, c01);
-                w[2 * e + 1] = __fmul2_rn(k12, c23);
-              }
-            }
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              w[e].x = fmaxf(w[e].x, 0.0f);
-              w[e].y = fmaxf(w[e].y, 0.0f);
-            }
-            if (kb + 8 > job.krow) {
-#pragma unroll
-              for (int u = 0; u < 8; ++u)
-                if (kb + u >= job.krow) {
-                  if (u & 1)
-                    w[u >> 1].y = 0.0f;
-                  else
-                    w[u >> 1].x = 0.0f;
-                }
-            }
+            weights8(cdrow, kb, job.krow, ccq2, ssq2, k12, alpha2, beta2, ggx, w);
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
               const __nv_bfloat162 h2 = __floats2bfloat162_rn(w[e].x, w[e].y);
@@ -733,19 +835,18 @@ __device__ __forceinline__ bool contract_cta(const Job& job, int bx, int by, int
     }
     wsum_sh[h][row] = wacc;
   } else if (warp < kMmaWarp0 + kMmaWarps) {
-    // ---- MMA issuers: one thread per (colour channel, column half) --------------
-    const int u = warp - kMmaWarp0;
-    const int ch = u / job.nsplit, hf = u - ch * job.nsplit;
-    if (lane == 0 && total > 0 && u < 3 * job.nsplit) {
-      const int nm = job.nb / job.nsplit;
-      const uint32_t idesc = idesc_bf16(kM, nm);
+    // ---- MMA issuers: one thread per colour channel -----------------------------
+    // (two issuers per channel, on column halves, measured slower)
+    const int ch = warp - kMmaWarp0;
+    if (lane == 0 && total > 0) {
+      const uint32_t idesc = idesc_bf16(kM, job.nb);
       // B descriptors differ only in the start-address field (16-byte units;
       // every staged address stays below 2^18 bytes, so no carry out of it).
       const uint64_t bdesc0 = smem_desc(smem_u32(slots), 16, 128);
       const uint32_t r8 = (uint32_t)(job.rlen >> 3);
-      const uint32_t d = tmem + (uint32_t)(ch * job.nb + hf * nm);
+      const uint32_t d = tmem + (uint32_t)(ch * job.nb);
       // this issuer's hi plane rows within a slot, in 16-byte units
-      const uint32_t plane16 = 2u * (uint32_t)ch * r8 + (uint32_t)(hf * nm);
+      const uint32_t plane16 = 2u * (uint32_t)ch * r8;
       const uint32_t slot16 = 6u * r8;
       uint32_t gidx = 0, row_id = 0;
       bool ok = true;
@@ -782,61 +883,12 @@ __device__ __forceinline__ bool contract_cta(const Job& job, int bx, int by, int
         }
       }
       // every MMA issued by all issuers has completed before the accumulators
-      // are read and TMEM is released
-      mma_commit(&done_bar);
-      if (!settle(&done_bar, 0u)) *abort_flag = 1;
-      // The last commits' arrivals on the stage and slot barriers land too,
-      // before anything invalidates the barriers for reuse.
-      for (uint32_t st = 0; ok && st < (uint32_t)kStages && st < gidx; ++st) {
-        const uint32_t last = st + kStages * ((gidx - 1 - st) / kStages);
-        if (!settle(&a_empty[st], (last / kStages) & 1u)) *abort_flag = 1;
-      }
-      const uint32_t ns_ = (uint32_t)job.nslots;
-      for (uint32_t sl = 0; ok && sl < ns_ && sl < row_id; ++sl) {
-        const uint32_t last = sl + ns_ * ((row_id - 1 - sl) / ns_);
-        if (!settle(&slot_empty[sl], (last / ns_) & 1u)) *abort_flag = 1;
-      }
+      // are read and TMEM is released; the barriers are quiescent
+      issuer_drain(sh, gidx, row_id, job.nslots, ok, abort_flag);
     }
-  } else if (lane == 0) {
-    // ---- Hankel row loader: slot[p][t] = P_ph[(t + 8 n0) mod krow], t < rlen ----
-    const int u0 = (8 * n0) % job.krow;
-    long long row_id = 0;
-    bool ok = true;
-    for (int j = split; j < job.hs && ok; j += jstep) {
-      int ca, cb;
-      visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
-      if (ca + kchunks - cb == 0) continue;  // no visible offset: the row is not staged
-      for (int ph = 0; ph < job.g && ok; ++ph, ++row_id) {
-        const int slot = (int)(row_id % job.nslots);
-        const long long use = row_id / job.nslots;
-        if (use >= 1 &&
-            !wait_bar(&slot_empty[slot], (uint32_t)((use - 1) & 1), abort_flag)) {
-          ok = false;
-          break;
-        }
-        __nv_bfloat16* dst = slots + (size_t)slot * 6 * job.rlen;
-        mbar_expect_tx(&slot_full[slot], (uint32_t)(6 * job.rlen * 2));
-        for (int p = 0; p < 6; ++p) {
-          const __nv_bfloat16* srcrow =
-              job.src + (((size_t)p * job.hs + j) * job.g + ph) * job.krow;
-          int t = 0, u = u0;
-          while (t < job.rlen) {
-            const int len = min(job.krow - u, job.rlen - t);
-            bulk_g2s(dst + (size_t)p * job.rlen + t, srcrow + u, (uint32_t)(len * 2),
-                     &slot_full[slot]);
-            t += len;
-            u = 0;
-          }
-        }
-      }
-    }
-    // After an abort, copies may still be in flight: they land before the CTA
-    // exits (in a normal run the MMA threads have already seen every fill).
-    for (long long r = row_id > job.nslots ? row_id - job.nslots : 0; r < row_id; ++r) {
-      const unsigned long long t0 = global_ns();
-      while (!mbar_try_wait(&slot_full[r % job.nslots], (uint32_t)((r / job.nslots) & 1)))
-        if (global_ns() - t0 > kWaitNs) break;
-    }
+  } else if (warp == kLoaderWarp && lane == 0) {
+    // ---- Hankel row loader ----
+    load_rows(job, slots, slot_full, slot_empty, split, KS, kchunks, vis_row, n0, abort_flag);
   }
 
   tc_fence_before();
@@ -919,19 +971,263 @@ __device__ __forceinline__ bool contract_cta(const Job& job, int bx, int by, int
   __syncthreads();
   tc_fence_after();
   if (failed) return false;
-  // quiescent: every arrival has landed (the MMA issuer settled the last
+  // quiescent: every arrival has landed (the MMA issuers settled the last
   // phases), so the barriers can be invalidated for the next work item
+  inval_barriers(sh);
+  return true;
+}
+
+// One CTA of a column-tile contraction (Job::ct): output columns n0 ..
+// n0 + 127 of residue x0 (column block by), every row of the output, source
+// rows of split bz.  A = the staged Hankel
+// rows (M = 128 columns: the descriptor of the row tiles' B), B = the weights
+// of the kCtN rows in shared memory; accumulator lane = column, TMEM column =
+// channel * kCtN + row.  Producer warps form G groups, group g owning the
+// stage slots st with st % G == g; each warp writes 8 K of 32 rows per stage
+// (one 16-byte store per lane).  Same contract as contract_cta: false when a bounded wait
+// gave up, else every barrier quiescent and invalidated.
+template <int KIND, bool TWO>
+__device__ __forceinline__ bool contract_cta_ct(const Job& job, int by, int bz, uint32_t tmem,
+                                                unsigned char* smem, CtaShared& sh) {
+  uint64_t* const a_full = sh.a_full;
+  uint64_t* const a_empty = sh.a_empty;
+  uint64_t* const slot_full = sh.slot_full;
+  uint64_t* const slot_empty = sh.slot_empty;
+  double* const wsum_sh = &sh.wsum[0][0];  // [producer warp][lane]
+  static_assert(sizeof(CtaShared::wsum) >= sizeof(double) * kProducerWarps * 32, "weight sums");
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int x0 = by / job.nblk;
+  const int n0 = (by - x0 * job.nblk) * kM;
+  const int split = bz;
+  const SmemPlan sp = smem_plan(job);
+  __nv_bfloat16* slots = reinterpret_cast<__nv_bfloat16*>(smem + sp.slots);
+  float* cosd_sm = reinterpret_cast<float*>(smem + sp.cosd);
+  unsigned char* bst = smem + sp.bst;
+  volatile int* abort_flag = &sh.abort;
+
+  constexpr int KS = TWO ? 64 : kKS;  // K per stage
+  constexpr int KG = KS / 8;          // groups of 8 K per stage
+  constexpr int N = kCtN;             // weight rows (MMA N)
+  constexpr int R = N / 32;           // row groups of 32 lanes
+  constexpr int T = R * KG;           // producer tasks per stage: 8 or 16
+  constexpr int G = kProducerWarps / T;  // producer groups: 2 or 1
+  constexpr int TW = T;               // warps per group, one task each
+  static_assert(kProducerWarps % T == 0 && kStages % G == 0, "producer groups");
+  constexpr uint32_t stage_bytes = 128u * N;
+  constexpr uint32_t group_bytes = 16u * N;               // 8 K of all N rows
+  constexpr uint32_t plane_bytes = (uint32_t)KG * group_bytes;  // lo plane after hi
+
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_inval(&a_full[s]);
-      mbar_inval(&a_empty[s]);
+      mbar_init(&a_full[s], TW);  // the warps of the owning group
+      mbar_init(&a_empty[s], kMmaWarps);  // the issuers' commits
     }
     for (int s = 0; s < kMaxSlots; ++s) {
-      mbar_inval(&slot_full[s]);
-      mbar_inval(&slot_empty[s]);
+      mbar_init(&slot_full[s], 1);
+      mbar_init(&slot_empty[s], kMmaWarps);
     }
-    mbar_inval(&done_bar);
+    mbar_init(&sh.done_bar, kMmaWarps);
+    sh.abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  {
+    const int shf = (job.s / job.g) * x0 % job.krow;
+    for (int e = tid; e < job.g * job.kpad; e += kThreads) {
+      int ph = e / job.kpad, k = e - ph * job.kpad;
+      int kk = k - shf;
+      if (kk < 0) kk += job.krow;
+      cosd_sm[e] = k < job.krow ? job.cos_d[job.g * kk + ph] : 0.0f;
+    }
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+
+  const int jstep = job.ksplit;
+  const int kchunks = job.kpad / KS;
+  const int* vis_row = job.vis;  // the one row tile
+  long long total = 0;
+  for (int j = split; j < job.hs; j += jstep) {
+    int ca, cb;
+    visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
+    total += (long long)job.g * (ca + kchunks - cb);
+  }
+  const bool by0 = by == 0;
+
+  if (warp < kProducerWarps) {
+    // ---- weight producers: B row i = 32 rg + lane, 8 K (group kg) of the stage
+    const int gw = warp / TW, wi = warp - gw * TW;
+    const int rg = wi % R, kg = wi / R;
+    const int i = 32 * rg + lane;  // output row
+    const bool real = i < job.ho;
+    float cp = 0.0f, sp_ = 0.0f;
+    if (real) {
+      cp = job.out_rows[2 * i];
+      sp_ = job.out_rows[2 * i + 1];
+    }
+    const float a2 = job.a2;
+    constexpr bool ggx = KIND == 0;
+    const bool want = real && ggx && by0;
+    const float alpha = 0.5f * (1.0f + a2), beta = 0.5f * (a2 - 1.0f), ka = a2 / kPiF;
+    const float2 alpha2 = make_float2(alpha, alpha), beta2 = make_float2(beta, beta);
+    const float2 minus1 = make_float2(-1.0f, -1.0f);
+    const uint32_t row_off = (uint32_t)((i >> 3) * 128 + (i & 7) * 16);
+    double wacc = 0.0;
+    uint32_t gidx = 0;
+    bool ok = true;
+    for (int j = split; j < job.hs && ok; j += jstep) {
+      int ca, cb;
+      visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
+      const int nvis = ca + kchunks - cb;
+      const float cq = job.src_rows[3 * j], sq = job.src_rows[3 * j + 1];
+      const float om = job.src_rows[3 * j + 2];
+      const float ccq = cp * cq, ssq = sp_ * sq;
+      const float k1 = real ? (ggx ? ka * om : om) : 0.0f;  // padded rows: zero weights
+      const float2 ccq2 = make_float2(ccq, ccq), ssq2 = make_float2(ssq, ssq);
+      const float2 k12 = make_float2(k1, k1);
+      for (int ph = 0; ph < job.g && ok; ++ph) {
+        const float* cdrow = cosd_sm + ph * job.kpad;
+        float2 rowsum2 = make_float2(0.0f, 0.0f);
+        for (int v = 0; v < nvis; ++v, ++gidx) {
+          const int st = (int)(gidx & (kStages - 1));
+          if (st % G != gw) continue;  // another group's stage slot
+          const uint32_t use = gidx / kStages;
+          const int kc = v < ca ? v : cb + (v - ca);
+          uint32_t hw[4], lw[4];
+          {
+            float2 w[4];
+            weights8(cdrow, kc * KS + 8 * kg, job.krow, ccq2, ssq2, k12, alpha2, beta2, ggx, w);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const __nv_bfloat162 h2 = __floats2bfloat162_rn(w[e].x, w[e].y);
+              hw[e] = *reinterpret_cast<const uint32_t*>(&h2);
+              if (TWO) {
+                w[e] = __bfloat1622float2(h2);  // the weight the MMAs use
+              } else {
+                const float2 lo = __ffma2_rn(__bfloat1622float2(h2), minus1, w[e]);
+                const __nv_bfloat162 l2 = __floats2bfloat162_rn(lo.x, lo.y);
+                lw[e] = *reinterpret_cast<const uint32_t*>(&l2);
+              }
+            }
+            if (want)
+              rowsum2 = __fadd2_rn(__fadd2_rn(rowsum2, w[0]), __fadd2_rn(__fadd2_rn(w[1], w[2]), w[3]));
+          }
+          if (use >= 1 && !wait_bar(&a_empty[st], (uint32_t)((use - 1) & 1), abort_flag)) {
+            ok = false;
+            break;
+          }
+          {
+            unsigned char* g8 = bst + (size_t)st * stage_bytes + row_off + (size_t)kg * group_bytes;
+            *reinterpret_cast<uint4*>(g8) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+            if (!TWO)
+              *reinterpret_cast<uint4*>(g8 + plane_bytes) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+          }
+          // the stores are read by the tensor cores (async proxy)
+          fence_async_smem();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&a_full[st]);
+        }
+        wacc += (double)(rowsum2.x + rowsum2.y);
+      }
+    }
+    wsum_sh[warp * 32 + lane] = wacc;
+  } else if (warp < kMmaWarp0 + kMmaWarps) {
+    // ---- MMA issuers: one thread per colour channel ------------------------------
+    const int ch = warp - kMmaWarp0;
+    if (lane == 0 && total > 0) {
+      const uint32_t idesc = idesc_bf16(kM, N);
+      // descriptors differ only in the start-address field (16-byte units;
+      // every address stays below 2^18 bytes, so no carry out of it)
+      const uint64_t adesc0 = smem_desc(smem_u32(slots), 16, 128);
+      const uint64_t bdesc0 = smem_desc(smem_u32(bst), group_bytes, 128);
+      const uint32_t r8 = (uint32_t)(job.rlen >> 3);
+      const uint32_t plane16 = 2u * (uint32_t)ch * r8;  // this channel's hi plane
+      const uint32_t slot16 = 6u * r8;
+      const uint32_t stage16 = stage_bytes >> 4, lo16 = plane_bytes >> 4;
+      const uint32_t bk = 2u * (group_bytes >> 4);  // B units per K = 16
+      const uint32_t d = tmem + (uint32_t)(ch * N);
+      uint32_t gidx = 0, row_id = 0;
+      bool ok = true;
+      for (int j = split; j < job.hs && ok; j += jstep) {
+        int ca, cb;
+        visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
+        const int nvis = ca + kchunks - cb;
+        if (nvis == 0) continue;  // not staged by the loader either
+        for (int ph = 0; ph < job.g && ok; ++ph, ++row_id) {
+          const uint32_t slot = row_id % (uint32_t)job.nslots;
+          if (!wait_bar(&slot_full[slot], (row_id / (uint32_t)job.nslots) & 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          const uint64_t arow = adesc0 + (uint64_t)(slot * slot16 + plane16);
+          for (int v = 0; v < nvis; ++v, ++gidx) {
+            const int kc = v < ca ? v : cb + (v - ca);
+            const uint32_t st = gidx & (kStages - 1);
+            if (!wait_bar(&a_full[st], (gidx / kStages) & 1u, abort_flag)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint64_t ah = arow + (uint64_t)(kc * (KS * 2 / 16));
+            const uint64_t bh = bdesc0 + (uint64_t)(st * stage16);
+            if (TWO)
+              mma_stage64_ss2(d, ah, ah + r8, bh, bk, idesc, gidx != 0, &a_empty[st]);
+            else
+              mma_stage_ss(d, ah, ah + r8, bh, bh + lo16, bk, idesc, gidx != 0, &a_empty[st]);
+          }
+          if (ok) mma_commit(&slot_empty[slot]);  // the row's slot is free once its MMAs are done
+        }
+      }
+      issuer_drain(sh, gidx, row_id, job.nslots, ok, abort_flag);
+    }
+  } else if (warp == kLoaderWarp && lane == 0) {
+    // ---- Hankel row loader (rows of 8 * 128 + kpad elements) ----
+    load_rows(job, slots, slot_full, slot_empty, split, KS, kchunks, vis_row, n0, abort_flag);
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const bool failed = sh.abort != 0;
+  if (failed) {
+    if (tid == 0) atomicExch(job.error, 1);
+  } else {
+    if (warp < kProducerWarps) {
+      // accumulators -> partial sums: lane quarter q holds columns 32 q ..;
+      // its four warps take every fourth 16-column chunk (16 rows of one channel)
+      const int q = warp & 3;
+      const int n = 32 * q + lane;
+      const int x = x0 + job.m * (n0 + n);
+      const bool col_ok = n0 + n < job.nres && x < job.wo;
+      for (int c0 = 16 * (warp >> 2); c0 < 3 * N; c0 += 16 * (kProducerWarps / 4)) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+        const int ch = c0 / N, i0 = c0 - ch * N;
+        if (!col_ok) continue;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int i = i0 + u;
+          const float val = total > 0 ? v[u] : 0.0f;
+          if (i < job.ho) job.partial[(((size_t)split * 3 + ch) * job.wo + x) * job.ho + i] = val;
+        }
+      }
+    }
+    if (KIND == 0 && by0 && tid < job.ho) {
+      // weight sums of row i: the warps of row group i / 32, in warp order
+      const int i = tid, rg = i >> 5, l = i & 31;
+      double ws = 0.0;
+      for (int w = 0; w < kProducerWarps; ++w)
+        if ((w % TW) % R == rg) ws += wsum_sh[w * 32 + l];  // every group, in warp order
+      job.wsum_part[(size_t)split * job.ho + i] = ws;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (failed) return false;
+  inval_barriers(sh);
   return true;
 }
 
@@ -966,6 +1262,17 @@ __global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
   __shared__ uint32_t tmem_base_sh;
   const uint32_t tmem = tmem_alloc_all(&tmem_base_sh);
   contract_cta<KIND, TWO>(job, blockIdx.x, blockIdx.y, blockIdx.z, tmem, smem, sh);
+  tmem_free_all(tmem);
+}
+
+// The contraction kernel of one column-tile job.  Grid: (1, m * nblk, ksplit).
+template <int KIND, bool TWO>
+__global__ void __launch_bounds__(kThreads, 1) contract_ct_kernel(const Job job) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ CtaShared sh;
+  __shared__ uint32_t tmem_base_sh;
+  const uint32_t tmem = tmem_alloc_all(&tmem_base_sh);
+  contract_cta_ct<KIND, TWO>(job, blockIdx.y, blockIdx.z, tmem, smem, sh);
   tmem_free_all(tmem);
 }
 
@@ -1004,7 +1311,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     bool ok;
-    if (job_sh.kind == 1)
+    if (job_sh.ct) {
+      if (job_sh.kind == 1)
+        ok = contract_cta_ct<1, false>(job_sh, wi.by, wi.bz, tmem, smem, sh);
+      else if (job_sh.two_prod)
+        ok = contract_cta_ct<0, true>(job_sh, wi.by, wi.bz, tmem, smem, sh);
+      else
+        ok = contract_cta_ct<0, false>(job_sh, wi.by, wi.bz, tmem, smem, sh);
+    } else if (job_sh.kind == 1)
       ok = contract_cta<1, false>(job_sh, wi.bx, wi.by, wi.bz, tmem, smem, sh);
     else if (job_sh.two_prod)
       ok = contract_cta<0, true>(job_sh, wi.bx, wi.by, wi.bz, tmem, smem, sh);
@@ -1060,7 +1374,7 @@ __host__ __device__ inline size_t narrow_smem_bytes(int ws, int wo) {
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(kNarrowThreads) narrow_kernel(const NarrowJob J) {
+__device__ __forceinline__ void narrow_block(const NarrowJob& J, int i, int band) {
   extern __shared__ __align__(16) unsigned char nsm[];
   const int ws = J.ws, wo = J.wo, s = J.s;
   float4* row = reinterpret_cast<float4*>(nsm);        // staged L_j
@@ -1070,7 +1384,6 @@ __global__ void __launch_bounds__(kNarrowThreads) narrow_kernel(const NarrowJob 
   __shared__ float red[kNarrowWarps];
   __shared__ double wsum_sh;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int i = blockIdx.x;
   // lane -> (output column x, sub-range r of the warp's source columns)
   const int R = 32 / wo, x = lane % wo, r = lane / wo;
   const bool lane_live = r < R;
@@ -1081,7 +1394,7 @@ __global__ void __launch_bounds__(kNarrowThreads) narrow_kernel(const NarrowJob 
   const float cp = J.out_rows[2 * i], sp = J.out_rows[2 * i + 1];
   const float alpha = 0.5f * (1.0f + J.a2), beta = 0.5f * (J.a2 - 1.0f), ka = J.a2 / kPiF;
   const int j_per = (J.hs + J.ksplit - 1) / J.ksplit;
-  const int j0 = blockIdx.y * j_per, j1 = min(J.hs, j0 + j_per);
+  const int j0 = band * j_per, j1 = min(J.hs, j0 + j_per);
   const int sx = (int)(((long long)s * x) % ws);
   double a0 = 0.0, a1 = 0.0, a2 = 0.0, wsum = 0.0;
   for (int j = j0; j < j1; ++j) {
@@ -1151,7 +1464,7 @@ __global__ void __launch_bounds__(kNarrowThreads) narrow_kernel(const NarrowJob 
         t1 += fin[3 * src_t + 1];
         t2 += fin[3 * src_t + 2];
       }
-    double* dst = J.partial + ((size_t)blockIdx.y * wo * J.ho + (size_t)i * wo + tid) * 4;
+    double* dst = J.partial + ((size_t)band * wo * J.ho + (size_t)i * wo + tid) * 4;
     dst[0] = t0;
     dst[1] = t1;
     dst[2] = t2;
@@ -1159,11 +1472,31 @@ __global__ void __launch_bounds__(kNarrowThreads) narrow_kernel(const NarrowJob 
   }
 }
 
-// One warp per output texel: the splits in a fixed order (lane k takes k,
+// Output row i, band of source rows `band`: grid (ho, ksplit).
+template <int KIND>
+__global__ void __launch_bounds__(kNarrowThreads) narrow_kernel(const NarrowJob J) {
+  narrow_block<KIND>(J, blockIdx.x, blockIdx.y);
+}
+
+// The narrow jobs of many probes (one kind) in one launch: block b is block
+// b - begins[k] = band * ho + i of job k.  Dynamic shared memory: the largest
+// job's.
+template <int KIND>
+__global__ void __launch_bounds__(kNarrowThreads)
+    narrow_batch_kernel(const NarrowJob* __restrict__ jobs, const long long* __restrict__ begins,
+                        int njobs) {
+  const int k = find_range(begins, njobs, blockIdx.x);
+  const NarrowJob& J = jobs[k];
+  const int local = (int)((long long)blockIdx.x - begins[k]);
+  narrow_block<KIND>(J, local % J.ho, local / J.ho);
+}
+
+// One warp per output texel o: the splits in a fixed order (lane k takes k,
 // k + 32, ...; then a fixed shuffle tree), normalised, written.
-__global__ void narrow_finish_kernel(const NarrowJob J, int kind, void* __restrict__ out,
-                                     long long pitch, int out_half) {
-  const int o = blockIdx.x, lane = threadIdx.x;
+__device__ __forceinline__ void narrow_finish_warp(const NarrowJob& J, int kind,
+                                                   void* __restrict__ out, long long pitch,
+                                                   int out_half, int o) {
+  const int lane = threadIdx.x & 31;
   const int n_out = J.wo * J.ho;
   double t[4] = {0.0, 0.0, 0.0, 0.0};
   for (int k = lane; k < J.ksplit; k += 32) {
@@ -1185,6 +1518,30 @@ __global__ void narrow_finish_kernel(const NarrowJob J, int kind, void* __restri
   } else {
     reinterpret_cast<float4*>(out)[(long long)i * pitch + x] = make_float4(r, g, b, 1.0f);
   }
+}
+
+__global__ void narrow_finish_kernel(const NarrowJob J, int kind, void* __restrict__ out,
+                                     long long pitch, int out_half) {
+  narrow_finish_warp(J, kind, out, pitch, out_half, blockIdx.x);
+}
+
+// A narrow output of a batch: its job, kind and destination.
+struct NarrowOut {
+  NarrowJob J;
+  int kind;
+  void* out;
+  long long pitch;
+  int out_half;
+};
+
+// Every narrow output of a batch: block b (one warp) is texel b - begins[k]
+// of output k.
+__global__ void narrow_finish_batch_kernel(const NarrowOut* __restrict__ outs,
+                                           const long long* __restrict__ begins, int n) {
+  const int k = find_range(begins, n, blockIdx.x);
+  const NarrowOut& o = outs[k];
+  narrow_finish_warp(o.J, o.kind, o.out, o.pitch, o.out_half,
+                     (int)((long long)blockIdx.x - begins[k]));
 }
 
 // Direction tables in FP64, stored as FP32: cos of the column offsets
@@ -1302,11 +1659,10 @@ struct RowsArgs {
   __nv_bfloat16* out[kMaxRowsOut];
 };
 
-__global__ void rows_kernel(const RowsArgs a) {
+__device__ __forceinline__ void rows_block(const RowsArgs& a, int j) {
   extern __shared__ __nv_bfloat16 row_sm[];
   const float4* __restrict__ src = a.src;
   const int ws = a.ws, hs = a.hs;
-  const int j = blockIdx.x;
   for (int x = threadIdx.x; x < ws; x += blockDim.x) {
     const float4 v = src[(size_t)j * ws + x];
     const float c[3] = {v.x, v.y, v.z};
@@ -1342,6 +1698,17 @@ __global__ void rows_kernel(const RowsArgs a) {
       }
     }
   }
+}
+
+__global__ void rows_kernel(const RowsArgs a) { rows_block(a, blockIdx.x); }
+
+// The split passes of many levels (of many probes) in one launch: block b is
+// source row b - begins[k] of level job k.  Dynamic shared memory: the widest
+// level's.
+__global__ void rows_batch_kernel(const RowsArgs* __restrict__ jobs,
+                                  const long long* __restrict__ begins, int njobs) {
+  const int k = find_range(begins, njobs, blockIdx.x);
+  rows_block(jobs[k], (int)((long long)blockIdx.x - begins[k]));
 }
 
 // Sum the K splits (FP32, fixed order), normalise by the FP64 weight sum,
@@ -1482,6 +1849,23 @@ __global__ void __launch_bounds__(kFinishThreads) finish_all_kernel(
   int k = 0;
   while (k + 1 < a.n && b >= a.begin[k + 1]) ++k;
   finish_block(a.job[k], a.out[k], a.pitch[k], (long long)(b - a.begin[k]) * 32);
+}
+
+// A contracted output of a batch: its job and destination.
+struct FinishOut {
+  Job job;
+  void* out;
+  long long pitch;
+};
+
+// Every contracted output of a batch: block b is block b - begins[k] (32
+// slots) of output k.
+__global__ void __launch_bounds__(kFinishThreads)
+    finish_batch_kernel(const FinishOut* __restrict__ outs, const long long* __restrict__ begins,
+                        int n) {
+  const int k = find_range(begins, n, blockIdx.x);
+  const FinishOut& o = outs[k];
+  finish_block(o.job, o.out, o.pitch, ((long long)blockIdx.x - begins[k]) * 32);
 }
 
 }  // namespace tc
@@ -1645,7 +2029,6 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   J.nb = ((J.nres + 15) / 16) * 16;
   if (J.nb > kNBMax) J.nb = kNBMax;
   J.nblk = (J.nres + J.nb - 1) / J.nb;
-  J.nsplit = 1;  // two issuers per channel (N/2 each) measured slower
   J.rlen = ((8 * J.nb + J.kpad + 7) / 8) * 8;
   J.kind = kind;
   J.a2 = roughness * roughness;
@@ -1681,7 +2064,7 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
   J.ksplit = ks;
   J.kinter = 1;
   J.nparts = ks;
-  // one partial sum per split (a K interleave adds its quarters in the CTA)
+  // one partial sum per split
   const int parts = ks;
   jp.level = li;
   jp.cosd_off = off;
@@ -1758,12 +2141,37 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
       if (x.ws != y.ws || x.hs != y.hs || x.wo != y.wo || x.g != y.g || x.m != y.m ||
           x.krow != y.krow || x.kpad != y.kpad || x.nres != y.nres || x.nb != y.nb ||
           x.nblk != y.nblk || x.rlen != y.rlen || x.nslots != y.nslots ||
-          x.nsplit != y.nsplit || x.ksplit != y.ksplit || x.two_prod != y.two_prod)
+          x.ksplit != y.ksplit || x.two_prod != y.two_prod)
         continue;
       A.pair_with = (int)b;
       B.paired = true;
       break;
     }
+  }
+  // Unpaired tensor outputs of 33 to 64 rows: column tiles.  An M = 128 tile
+  // of their rows would be half or more padding; their columns fill it
+  // instead (the operands swap roles: N = 64 rows).  With both operands in
+  // shared memory the MMAs read 4 KB of radiance per K = 16 whatever N is,
+  // which only pays at N = 64 (about 6 KB per 37-cycle MMA, near the
+  // shared-memory rate): smaller outputs keep row tiles (pairs, K
+  // interleave).  Same grid and splits (one row tile; column blocks of 128
+  // either way), so the workspace layout is unchanged.
+  for (auto& jp : P.jobs) {
+    if (jp.level < 0 || jp.narrow || jp.paired || jp.pair_with >= 0 || jp.J.ho <= 32 ||
+        jp.J.ho > 64)
+      continue;
+    Job& J = jp.J;
+    J.ct = 1;
+    J.nb = kM;
+    J.nblk = (J.nres + kM - 1) / kM;
+    J.rlen = 8 * kM + J.kpad;
+    for (J.nslots = kMaxSlots; J.nslots > 2; --J.nslots)
+      if (smem_plan(J).total + 4096 <= (size_t)kSmemLimit) break;
+    if (smem_plan(J).total + 4096 > (size_t)kSmemLimit)
+      return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
+                       "tensor path: a %dx%d output against a %d-wide level needs too much "
+                       "shared memory",
+                       J.wo, J.ho, J.ws);
   }
   // Unpaired tensor outputs of at most 32 rows: K interleave over the four
   // lane quarters.
@@ -1811,8 +2219,9 @@ extern "C" int althea_ibl_tc_stats(int w, int h, const althea_ibl_mip_target* mi
     const int KS = J.two_prod ? 2 * kKS : kKS;
     const int kchunks = J.kpad / KS, products = J.two_prod ? 2 : 3;
     const int ntiles = (J.ho + kM - 1) / kM, gy = J.m * J.nblk;
-    // flops of one stage's MMAs: 3 channels x products x K/16 MMAs of M = 128, N = nb, K = 16
-    const double stage_flops = 3.0 * products * (KS / 16) * 2.0 * kM * J.nb * 16;
+    // flops of one stage's MMAs: 3 channels x products x K/16 MMAs of M = 128,
+    // K = 16 and N = nb (row tiles) or kCtN (column tiles)
+    const double stage_flops = 3.0 * products * (KS / 16) * 2.0 * kM * (J.ct ? kCtN : J.nb) * 16;
     for (int tile = 0; tile < ntiles; ++tile) {
       const int ia = tile * kM, ib = std::min(J.ho, ia + kM) - 1;
       const int rows = ib - ia + 1 + ho_b;
@@ -1947,19 +2356,11 @@ int tc_setup(const float* chain, int w, int h, const althea_ibl_mip_target* mips
   return ALTHEA_IBL_OK;
 }
 
-int tc_launch_narrow(const TcBake& B, cudaStream_t ns);
-
-// Split planes and tables; with `narrow`, the CUDA-core outputs too (on the
-// side stream when there is one, returned in *ns_out).
-int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream_t* ns_out,
-                   bool narrow = true) {
+// The split passes of a bake: one per source level, writing every phase
+// decomposition of it (up to kMaxRowsOut per pass).
+std::vector<RowsArgs> rows_jobs(const TcBake& B) {
   const TcPlan& P = B.P;
-  char* base = B.base;
-  *ns_out = s;
-  cudaError_t e = cudaMemsetAsync(base, 0, 256, s);
-  if (e != cudaSuccess) return cuda_status(e, "tc error flag");
-  // One split pass per source level, writing every phase decomposition of it
-  // (up to kMaxRowsOut per pass).
+  std::vector<RowsArgs> out;
   std::vector<char> done(P.levels.size(), 0);
   for (size_t a0 = 0; a0 < P.levels.size(); ++a0) {
     if (done[a0]) continue;
@@ -1972,45 +2373,86 @@ int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream
     for (size_t a1 = a0; a1 < P.levels.size() && ra.n < kMaxRowsOut; ++a1) {
       if (done[a1] || P.levels[a1].level != L.level) continue;
       ra.g[ra.n] = P.levels[a1].g;
-      ra.out[ra.n] = reinterpret_cast<__nv_bfloat16*>(base + P.levels[a1].offset);
+      ra.out[ra.n] = reinterpret_cast<__nv_bfloat16*>(B.base + P.levels[a1].offset);
       ++ra.n;
       done[a1] = 1;
     }
-    const int sm = 6 * L.ws * 2;
+    out.push_back(ra);
+  }
+  return out;
+}
+
+// Direction tables and visible-offset windows of every job of a bake, one
+// launch (FP64 transcendentals spread over many SMs).  They depend on the
+// sizes only.
+int tc_launch_tables(const TcBake& B, cudaStream_t s) {
+  const TcPlan& P = B.P;
+  TableArgs ta;
+  memset(&ta, 0, sizeof(ta));
+  int nt = 0, nmax = 1;
+  for (size_t k = 0; k < P.jobs.size(); ++k) {
+    const JobPlan& jp = P.jobs[k];
+    if (jp.level < 0 && !jp.narrow) continue;
+    const Job& J = jp.J;
+    ta.ws[nt] = J.ws;
+    ta.hs[nt] = J.hs;
+    ta.ho[nt] = J.ho;
+    ta.cosd[nt] = const_cast<float*>(J.cos_d);
+    ta.srows[nt] = const_cast<float*>(J.src_rows);
+    ta.orows[nt] = const_cast<float*>(J.out_rows);
+    if (!jp.narrow && !jp.paired) {  // a tensor launch: its visible-offset windows
+      ta.vis[nt] = const_cast<int*>(J.vis);
+      ta.ntiles[nt] = (J.ho + kM - 1) / kM;
+      ta.ho_b[nt] = jp.pair_with >= 0 ? P.jobs[jp.pair_with].J.ho : 0;
+      ta.g[nt] = J.g;
+      ta.krow[nt] = J.krow;
+    }
+    nmax = std::max(nmax, std::max(J.ws, std::max(J.hs, J.ho)));
+    ++nt;
+  }
+  if (nt > 0) tables_kernel<<<dim3((nmax + 31) / 32, nt), 32, 0, s>>>(ta);
+  return cuda_status(cudaGetLastError(), "tc tables launch");
+}
+
+// The CUDA-core job of a narrow output.
+NarrowJob narrow_job(const TcBake& B, const JobPlan& jp) {
+  const Job& J = jp.J;
+  NarrowJob nj;
+  nj.src = reinterpret_cast<const float4*>(B.chain) + B.tab.off[jp.src_level];
+  nj.ws = J.ws;
+  nj.hs = J.hs;
+  nj.wo = J.wo;
+  nj.ho = J.ho;
+  nj.s = J.ws / J.wo;
+  nj.ksplit = J.ksplit;
+  nj.a2 = J.a2;
+  nj.cos_d = J.cos_d;
+  nj.src_rows = J.src_rows;
+  nj.out_rows = J.out_rows;
+  nj.partial = reinterpret_cast<double*>(B.base + jp.partial_off);
+  return nj;
+}
+
+int tc_launch_narrow(const TcBake& B, cudaStream_t ns);
+
+// Error flag, split planes and tables; with `narrow`, the CUDA-core outputs
+// too (on the side stream when there is one, returned in *ns_out).
+int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream_t* ns_out,
+                   bool narrow = true) {
+  const TcPlan& P = B.P;
+  *ns_out = s;
+  cudaError_t e = cudaMemsetAsync(B.base, 0, 256, s);
+  if (e != cudaSuccess) return cuda_status(e, "tc error flag");
+  for (const RowsArgs& ra : rows_jobs(B)) {
+    const int sm = 6 * ra.ws * 2;
     if (sm > 48 * 1024) {
       e = cudaFuncSetAttribute(rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
       if (e != cudaSuccess) return cuda_status(e, "tc rows smem attribute");
     }
-    rows_kernel<<<L.hs, 256, sm, s>>>(ra);
+    rows_kernel<<<ra.hs, 256, sm, s>>>(ra);
   }
-  // Direction tables of every job, one launch (FP64 transcendentals spread
-  // over many SMs).
-  {
-    TableArgs ta;
-    memset(&ta, 0, sizeof(ta));
-    int nt = 0, nmax = 1;
-    for (size_t k = 0; k < P.jobs.size(); ++k) {
-      const JobPlan& jp = P.jobs[k];
-      if (jp.level < 0 && !jp.narrow) continue;
-      const Job& J = jp.J;
-      ta.ws[nt] = J.ws;
-      ta.hs[nt] = J.hs;
-      ta.ho[nt] = J.ho;
-      ta.cosd[nt] = const_cast<float*>(J.cos_d);
-      ta.srows[nt] = const_cast<float*>(J.src_rows);
-      ta.orows[nt] = const_cast<float*>(J.out_rows);
-      if (!jp.narrow && !jp.paired) {  // a tensor launch: its visible-offset windows
-        ta.vis[nt] = const_cast<int*>(J.vis);
-        ta.ntiles[nt] = (J.ho + kM - 1) / kM;
-        ta.ho_b[nt] = jp.pair_with >= 0 ? P.jobs[jp.pair_with].J.ho : 0;
-        ta.g[nt] = J.g;
-        ta.krow[nt] = J.krow;
-      }
-      nmax = std::max(nmax, std::max(J.ws, std::max(J.hs, J.ho)));
-      ++nt;
-    }
-    if (nt > 0) tables_kernel<<<dim3((nmax + 31) / 32, nt), 32, 0, s>>>(ta);
-  }
+  int r = tc_launch_tables(B, s);
+  if (r) return r;
   // The outputs summed on the CUDA cores go to the side stream when there is
   // one (they need the tables, nothing else of the tensor path).
   bool any_narrow = false;
@@ -2029,25 +2471,11 @@ int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream
 
 // The outputs summed on the CUDA cores (after the prep launches' tables).
 int tc_launch_narrow(const TcBake& B, cudaStream_t ns) {
-  const TcPlan& P = B.P;
-  char* base = B.base;
   cudaError_t e;
-  for (const JobPlan& jp : P.jobs) {
+  for (const JobPlan& jp : B.P.jobs) {
     if (!jp.narrow) continue;
     const Job& J = jp.J;
-    NarrowJob nj;
-    nj.src = reinterpret_cast<const float4*>(B.chain) + B.tab.off[jp.src_level];
-    nj.ws = J.ws;
-    nj.hs = J.hs;
-    nj.wo = J.wo;
-    nj.ho = J.ho;
-    nj.s = J.ws / J.wo;
-    nj.ksplit = J.ksplit;
-    nj.a2 = J.a2;
-    nj.cos_d = J.cos_d;
-    nj.src_rows = J.src_rows;
-    nj.out_rows = J.out_rows;
-    nj.partial = reinterpret_cast<double*>(base + jp.partial_off);
+    const NarrowJob nj = narrow_job(B, jp);
     // dynamic part; with the 8 KB static reduction buffer it can pass the
     // 48 KB default, so the limit is always raised to what this job needs
     const int smem = (int)narrow_smem_bytes(J.ws, J.wo);
@@ -2072,9 +2500,10 @@ int tc_launch_narrow(const TcBake& B, cudaStream_t ns) {
   return cuda_status(cudaGetLastError(), "tensor path prep launch");
 }
 
-// Dynamic shared memory of a contraction CTA of job J: its staging slots and
-// cos table, at least 120 KB so that no two CTAs share an SM (each allocates
-// all of TMEM), and room for a K interleave's quarter sums.
+// Dynamic shared memory of a contraction CTA of job J: its staging slots,
+// cos table and (column tiles) weight stages, at least 120 KB so that no two
+// CTAs share an SM (each allocates all of TMEM), and room for a K
+// interleave's quarter sums.
 int contract_smem(const Job& J) {
   int smem = (int)smem_plan(J).total;
   if (smem < 120 * 1024) smem = 120 * 1024;
@@ -2082,13 +2511,21 @@ int contract_smem(const Job& J) {
   return smem;
 }
 
+// The one-shot kernel of job J.
+void (*contract_kernel_for(const Job& J))(Job) {
+  if (J.ct)
+    return J.kind == 1 ? contract_ct_kernel<1, false>
+                       : (J.two_prod ? contract_ct_kernel<0, true> : contract_ct_kernel<0, false>);
+  return J.kind == 1 ? contract_kernel<1, false>
+                     : (J.two_prod ? contract_kernel<0, true> : contract_kernel<0, false>);
+}
+
 int tc_launch_contract(const TcBake& B, cudaStream_t s) {
   for (int k : B.launch_jobs) {
     const Job& J = B.P.jobs[k].J;
     const int smem = contract_smem(J);
-    dim3 grid((J.ho + kM - 1) / kM, J.m * J.nblk, J.ksplit);
-    auto kern = J.kind == 1 ? contract_kernel<1, false>
-                            : (J.two_prod ? contract_kernel<0, true> : contract_kernel<0, false>);
+    dim3 grid(J.ct ? 1 : (J.ho + kM - 1) / kM, J.m * J.nblk, J.ksplit);
+    auto kern = contract_kernel_for(J);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
     kern<<<grid, kThreads, smem, s>>>(J);
@@ -2149,6 +2586,17 @@ size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n
 }
 
 // ---- precision batches: one persistent contraction for every probe --------------
+// A device job table with its block offsets: job k owns blocks
+// [begins[k], begins[k + 1]) of one launch.
+template <typename T>
+struct DevTable {
+  T* jobs = nullptr;
+  long long* begins = nullptr;
+  int n = 0;
+  long long blocks = 0;
+  int smem = 0;  // dynamic shared memory of the launch (the largest job's)
+};
+
 struct TcBatch {
   std::vector<TcBake*> bakes;   // one per probe
   Job* d_jobs = nullptr;        // every contraction launch of every probe
@@ -2156,19 +2604,53 @@ struct TcBatch {
   unsigned int* d_next = nullptr;
   int* d_error = nullptr;       // set by any work item whose bounded wait gave up
   int nitems = 0, njobs = 0, smem = 0, ctas = 0;
+  // the rest of every probe's bake, one launch per kind of work
+  DevTable<RowsArgs> rows;
+  DevTable<NarrowJob> narrow[2];  // GGX, cosine
+  DevTable<NarrowOut> narrow_out;
+  DevTable<FinishOut> finish;
+  DevTable<DeltaJob> delta;
+  std::vector<void*> allocs;
 };
 
 void tc_batch_destroy(TcBatch* b) {
   if (!b) return;
   for (TcBake* B : b->bakes) delete B;
-  if (b->d_jobs) cudaFree(b->d_jobs);
-  if (b->d_items) cudaFree(b->d_items);
-  if (b->d_next) cudaFree(b->d_next);
-  if (b->d_error) cudaFree(b->d_error);
+  for (void* p : b->allocs) cudaFree(p);
   delete b;
 }
 
-int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, TcBatch** out) {
+namespace {
+
+// Copies a host job table and its block offsets to the device.
+template <typename T>
+cudaError_t upload(TcBatch* b, const std::vector<T>& jobs, const std::vector<long long>& blocks,
+                   DevTable<T>& t) {
+  t.n = (int)jobs.size();
+  if (t.n == 0) return cudaSuccess;
+  std::vector<long long> begins(jobs.size());
+  long long acc = 0;
+  for (size_t k = 0; k < jobs.size(); ++k) {
+    begins[k] = acc;
+    acc += blocks[k];
+  }
+  t.blocks = acc;
+  cudaError_t e = cudaMalloc(&t.jobs, sizeof(T) * jobs.size());
+  if (e == cudaSuccess) b->allocs.push_back(t.jobs);
+  if (e == cudaSuccess) e = cudaMalloc(&t.begins, sizeof(long long) * begins.size());
+  if (e == cudaSuccess) b->allocs.push_back(t.begins);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(t.jobs, jobs.data(), sizeof(T) * jobs.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(t.begins, begins.data(), sizeof(long long) * begins.size(),
+                   cudaMemcpyHostToDevice);
+  return e;
+}
+
+}  // namespace
+
+int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, cudaStream_t st,
+                    TcBatch** out) {
   *out = nullptr;
   TcBatch* b = new (std::nothrow) TcBatch();
   if (!b) return set_error(ALTHEA_IBL_ERR_OUT_OF_MEMORY, "host allocation");
@@ -2178,6 +2660,12 @@ int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, TcBatch**
     long long k;  // K this CTA sums (its source rows x phase rows), for the order
   };
   std::vector<Cand> items;
+  std::vector<RowsArgs> rows;
+  std::vector<NarrowJob> narrow[2];
+  std::vector<NarrowOut> nouts;
+  std::vector<FinishOut> fins;
+  std::vector<DeltaJob> deltas;
+  std::vector<long long> rows_blk, narrow_blk[2], nout_blk, fin_blk, delta_blk;
   for (int i = 0; i < n; ++i) {
     const TcBatchProbe& p = probes[i];
     TcBake* B = new (std::nothrow) TcBake();
@@ -2186,24 +2674,61 @@ int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, TcBatch**
       return set_error(ALTHEA_IBL_ERR_OUT_OF_MEMORY, "host allocation");
     }
     b->bakes.push_back(B);
-    int st = tc_setup(p.chain, p.w, p.h, p.mips.data(), (int)p.mips.size(), nullptr, p.irr,
-                      p.irr_w, p.irr_h, p.irr_pitch, -1, p.ws, p.ws_bytes, out_format, *B);
-    if (st) {
+    int r = tc_setup(p.chain, p.w, p.h, p.mips.data(), (int)p.mips.size(), nullptr, p.irr,
+                     p.irr_w, p.irr_h, p.irr_pitch, -1, p.ws, p.ws_bytes, out_format, *B);
+    // the tables depend on the sizes only: computed once, here
+    if (!r) r = tc_launch_tables(*B, st);
+    if (r) {
       tc_batch_destroy(b);
-      return st;
+      return r;
     }
     for (int k : B->launch_jobs) {
       const Job& J = B->P.jobs[k].J;
       const int jid = (int)jobs.size();
       jobs.push_back(J);
       b->smem = std::max(b->smem, contract_smem(J));
-      const int gx = (J.ho + kM - 1) / kM, gy = J.m * J.nblk, gz = J.ksplit;
+      const int gx = J.ct ? 1 : (J.ho + kM - 1) / kM, gy = J.m * J.nblk, gz = J.ksplit;
       for (int bz = 0; bz < gz; ++bz) {
-        const long long rows = (J.hs - bz + gz - 1) / gz;  // rows bz, bz + gz, ...
+        const long long rws = (J.hs - bz + gz - 1) / gz;  // rows bz, bz + gz, ...
         for (int by = 0; by < gy; ++by)
           for (int bx = 0; bx < gx; ++bx)
-            items.push_back(Cand{WorkItem{jid, bx, by, bz}, rows * J.g * J.kpad});
+            items.push_back(Cand{WorkItem{jid, bx, by, bz}, rws * J.g * J.kpad});
       }
+    }
+    for (const RowsArgs& ra : rows_jobs(*B)) {
+      rows.push_back(ra);
+      rows_blk.push_back(ra.hs);
+      b->rows.smem = std::max(b->rows.smem, 6 * ra.ws * 2);
+    }
+    for (const JobPlan& jp : B->P.jobs) {
+      if (!jp.narrow) continue;
+      const int kind = jp.J.kind;
+      const NarrowJob nj = narrow_job(*B, jp);
+      narrow[kind].push_back(nj);
+      narrow_blk[kind].push_back((long long)nj.ho * nj.ksplit);
+      b->narrow[kind].smem = std::max(b->narrow[kind].smem, (int)narrow_smem_bytes(nj.ws, nj.wo));
+      nouts.push_back(NarrowOut{nj, kind, jp.out, jp.pitch, B->out_half});
+      nout_blk.push_back((long long)nj.wo * nj.ho);
+    }
+    for (int k = 0; k < B->fa.n; ++k) {
+      fins.push_back(FinishOut{B->fa.job[k], B->fa.out[k], B->fa.pitch[k]});
+      fin_blk.push_back(B->fa.begin[k + 1] - B->fa.begin[k]);
+    }
+    for (int m = 0; m < B->n; ++m) {
+      if (B->P.jobs[m].level >= 0 || B->P.jobs[m].narrow) continue;  // roughness 0 only
+      const althea_ibl_mip_target& t = B->mips[m];
+      DeltaJob d;
+      d.chain = B->chain;
+      d.w = B->w;
+      d.h = B->h;
+      d.out = t.out_dev;
+      d.pitch = (long long)(t.pitch_bytes / (B->out_half ? 8 : 16));
+      d.ow = t.width;
+      d.oh = t.height;
+      d.out_half = B->out_half;
+      d.blocks_x = (t.width + 31) / 32;
+      deltas.push_back(d);
+      delta_blk.push_back((long long)d.blocks_x * ((t.height + 7) / 8));
     }
   }
   std::stable_sort(items.begin(), items.end(),
@@ -2216,20 +2741,41 @@ int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, TcBatch**
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   b->ctas = sms > 0 ? sms : 1;
+  auto track = [&](void* p) { b->allocs.push_back(p); };
   if (e == cudaSuccess && b->njobs > 0) e = cudaMalloc(&b->d_jobs, sizeof(Job) * jobs.size());
+  if (e == cudaSuccess && b->d_jobs) track(b->d_jobs);
   if (e == cudaSuccess && b->nitems > 0)
     e = cudaMalloc(&b->d_items, sizeof(WorkItem) * wi.size());
+  if (e == cudaSuccess && b->d_items) track(b->d_items);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_next, sizeof(unsigned int));
+  if (e == cudaSuccess) track(b->d_next);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_error, sizeof(int));
+  if (e == cudaSuccess) track(b->d_error);
   if (e == cudaSuccess) e = cudaMemset(b->d_error, 0, sizeof(int));
   for (Job& J : jobs) J.error = b->d_error;  // one status word for the whole batch
   if (e == cudaSuccess && b->njobs > 0)
     e = cudaMemcpy(b->d_jobs, jobs.data(), sizeof(Job) * jobs.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && b->nitems > 0)
     e = cudaMemcpy(b->d_items, wi.data(), sizeof(WorkItem) * wi.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = upload(b, rows, rows_blk, b->rows);
+  for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind)
+    e = upload(b, narrow[kind], narrow_blk[kind], b->narrow[kind]);
+  if (e == cudaSuccess) e = upload(b, nouts, nout_blk, b->narrow_out);
+  if (e == cudaSuccess) e = upload(b, fins, fin_blk, b->finish);
+  if (e == cudaSuccess) e = upload(b, deltas, delta_blk, b->delta);
   if (e == cudaSuccess && b->smem > 0)
     e = cudaFuncSetAttribute(contract_persistent_kernel,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem);
+  if (e == cudaSuccess && b->rows.smem > 48 * 1024)
+    e = cudaFuncSetAttribute(rows_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             b->rows.smem);
+  if (e == cudaSuccess && b->narrow[0].n)
+    e = cudaFuncSetAttribute(narrow_batch_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             b->narrow[0].smem);
+  if (e == cudaSuccess && b->narrow[1].n)
+    e = cudaFuncSetAttribute(narrow_batch_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             b->narrow[1].smem);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the tables are in place
   if (e != cudaSuccess) {
     tc_batch_destroy(b);
     return cuda_status(e, "precision batch plan");
@@ -2250,68 +2796,45 @@ int tc_batch_error(const TcBatch* b, cudaStream_t st) {
   return ALTHEA_IBL_OK;
 }
 
-int tc_batch_run(TcBatch* b, cudaStream_t st, const cudaStream_t* lanes, int nlanes,
-                 const int* lane_of, cudaEvent_t fork_ev, const cudaEvent_t* join_ev) {
+int tc_batch_run(TcBatch* b, cudaStream_t st, cudaStream_t side, cudaEvent_t fork_ev,
+                 cudaEvent_t join_ev) {
   ibl::NvtxRange nvtx_range("precision batch");
-  auto fork = [&]() -> cudaError_t {
-    cudaError_t e = cudaEventRecord(fork_ev, st);
-    for (int l = 0; l < nlanes && e == cudaSuccess; ++l)
-      e = cudaStreamWaitEvent(lanes[l], fork_ev, 0);
-    return e;
-  };
-  auto join = [&]() -> cudaError_t {
-    cudaError_t r = cudaSuccess;
-    for (int l = 0; l < nlanes; ++l) {
-      cudaError_t e = cudaEventRecord(join_ev[l], lanes[l]);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, join_ev[l], 0);
-      if (e != cudaSuccess && r == cudaSuccess) r = e;
-    }
-    return r;
-  };
-  // each probe's split planes and tables, on lanes
-  cudaError_t e = fork();
+  // The CUDA-core work (narrow outputs, roughness-0 mips) needs the chain and
+  // the tables only: it runs on the side stream beside the split passes and
+  // the contraction.
+  cudaError_t e = cudaEventRecord(fork_ev, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork_ev, 0);
   if (e != cudaSuccess) return cuda_status(e, "precision batch fork");
-  int r = ALTHEA_IBL_OK;
-  for (size_t i = 0; i < b->bakes.size() && !r; ++i) {
-    cudaStream_t ns;
-    r = tc_launch_prep(*b->bakes[i], lanes[lane_of[i]], nullptr, &ns, false);
-  }
-  e = join();  // also after an error, so that a stream capture can end cleanly
-  if (r) return r;
-  if (e != cudaSuccess) return cuda_status(e, "precision batch join");
-  // Every contraction of every probe: one persistent launch over the queue.
-  // The CUDA-core outputs go to the lanes after it is launched (its CTAs are
-  // placed first; a contraction CTA leaves no registers for another block),
-  // and take the SMs that the persistent kernel leaves as its queue drains.
-  e = cudaEventRecord(fork_ev, st);
-  if (e != cudaSuccess) return cuda_status(e, "precision batch fork");
+  if (b->rows.n)
+    rows_batch_kernel<<<(unsigned)b->rows.blocks, 256, b->rows.smem, st>>>(
+        b->rows.jobs, b->rows.begins, b->rows.n);
   if (b->nitems > 0) {
     e = cudaMemsetAsync(b->d_next, 0, sizeof(unsigned int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_error, 0, sizeof(int), st);
-    if (e != cudaSuccess) return cuda_status(e, "precision batch queue reset");
-    contract_persistent_kernel<<<b->ctas, kThreads, b->smem, st>>>(b->d_jobs, b->d_items,
-                                                                   b->nitems, b->d_next);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_status(e, "precision batch contraction launch");
+    if (e == cudaSuccess) {
+      contract_persistent_kernel<<<b->ctas, kThreads, b->smem, st>>>(b->d_jobs, b->d_items,
+                                                                     b->nitems, b->d_next);
+      e = cudaGetLastError();
+    }
   }
-  for (int l = 0; l < nlanes && e == cudaSuccess; ++l)
-    e = cudaStreamWaitEvent(lanes[l], fork_ev, 0);
-  if (e != cudaSuccess) return cuda_status(e, "precision batch fork");
-  for (size_t i = 0; i < b->bakes.size() && !r; ++i)
-    r = tc_launch_narrow(*b->bakes[i], lanes[lane_of[i]]);
-  if (r) {
-    join();
-    return r;
-  }
-  // each probe's split sums and roughness-0 mips, on lanes (after its
-  // CUDA-core outputs there and the contraction)
-  e = fork();
-  if (e != cudaSuccess) return cuda_status(e, "precision batch fork");
-  for (size_t i = 0; i < b->bakes.size() && !r; ++i) {
-    cudaStream_t l = lanes[lane_of[i]];
-    r = tc_launch_finish(*b->bakes[i], l, l, nullptr);
-  }
-  e = join();
+  if (e == cudaSuccess && b->finish.n)
+    finish_batch_kernel<<<(unsigned)b->finish.blocks, kFinishThreads, 0, st>>>(
+        b->finish.jobs, b->finish.begins, b->finish.n);
+  if (e == cudaSuccess && b->narrow[0].n)
+    narrow_batch_kernel<0><<<(unsigned)b->narrow[0].blocks, kNarrowThreads, b->narrow[0].smem,
+                             side>>>(b->narrow[0].jobs, b->narrow[0].begins, b->narrow[0].n);
+  if (e == cudaSuccess && b->narrow[1].n)
+    narrow_batch_kernel<1><<<(unsigned)b->narrow[1].blocks, kNarrowThreads, b->narrow[1].smem,
+                             side>>>(b->narrow[1].jobs, b->narrow[1].begins, b->narrow[1].n);
+  if (e == cudaSuccess && b->narrow_out.n)
+    narrow_finish_batch_kernel<<<(unsigned)b->narrow_out.blocks, 32, 0, side>>>(
+        b->narrow_out.jobs, b->narrow_out.begins, b->narrow_out.n);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  int r = e == cudaSuccess ? ALTHEA_IBL_OK : cuda_status(e, "precision batch launch");
+  if (!r) r = launch_delta_batch(b->delta.jobs, b->delta.begins, b->delta.n, b->delta.blocks, side);
+  // join (also after an error, so that a stream capture can end cleanly)
+  e = cudaEventRecord(join_ev, side);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, join_ev, 0);
   if (r) return r;
   return cuda_status(e, "precision batch join");
 }
