@@ -1736,7 +1736,14 @@ __device__ __forceinline__ void store_texel(void* out, long long pitch, int i, i
   }
 }
 
-__device__ __forceinline__ void finish_block(const Job& job, void* __restrict__ out,
+// What the finish of one contracted output reads.
+struct FinishJob {
+  const float* partial;      // [nparts][3][wo][ho]
+  const double* wsum_part;   // [nparts][ho] (kind 0)
+  int wo, ho, nparts, kind, out_half;
+};
+
+__device__ __forceinline__ void finish_block(const FinishJob& job, void* __restrict__ out,
                                              long long pitch, long long slot0) {
   __shared__ float red[kFinishWarps][3][kFinishRows][32];
   __shared__ double redw[kFinishWarps][kFinishRows][32];
@@ -1757,7 +1764,7 @@ __device__ __forceinline__ void finish_block(const Job& job, void* __restrict__ 
   }
   const float* base = job.partial + (size_t)x * job.ho + i0;
   if (live && vec) {
-    constexpr int kU = 2;
+    constexpr int kU = 1;
     for (int k0 = w; k0 < job.nparts; k0 += kU * kFinishWarps) {
       float4 v[kU][3];
       double2 wv[kU][2];
@@ -1836,14 +1843,14 @@ __device__ __forceinline__ void finish_block(const Job& job, void* __restrict__ 
 // begin[k] <= b < begin[k + 1] and covers 32 slots (four rows, one column) of it.
 constexpr int kMaxFinishJobs = ALTHEA_IBL_MAX_MIPS + 1;
 struct FinishArgs {
-  Job job[kMaxFinishJobs];
+  FinishJob job[kMaxFinishJobs];
   void* out[kMaxFinishJobs];
   long long pitch[kMaxFinishJobs];
   int begin[kMaxFinishJobs + 1];
   int n;
 };
 
-__global__ void __launch_bounds__(kFinishThreads) finish_all_kernel(
+__global__ void __launch_bounds__(kFinishThreads, 4) finish_all_kernel(
     const __grid_constant__ FinishArgs a) {
   const int b = blockIdx.x;
   int k = 0;
@@ -1853,19 +1860,25 @@ __global__ void __launch_bounds__(kFinishThreads) finish_all_kernel(
 
 // A contracted output of a batch: its job and destination.
 struct FinishOut {
-  Job job;
+  FinishJob job;
   void* out;
   long long pitch;
 };
 
 // Every contracted output of a batch: block b is block b - begins[k] (32
 // slots) of output k.
-__global__ void __launch_bounds__(kFinishThreads)
+__global__ void __launch_bounds__(kFinishThreads, 4)
     finish_batch_kernel(const FinishOut* __restrict__ outs, const long long* __restrict__ begins,
                         int n) {
-  const int k = find_range(begins, n, blockIdx.x);
-  const FinishOut& o = outs[k];
-  finish_block(o.job, o.out, o.pitch, ((long long)blockIdx.x - begins[k]) * 32);
+  __shared__ FinishOut o;
+  __shared__ long long slot0;
+  if (threadIdx.x == 0) {
+    const int k = find_range(begins, n, blockIdx.x);
+    o = outs[k];
+    slot0 = ((long long)blockIdx.x - begins[k]) * 32;
+  }
+  __syncthreads();
+  finish_block(o.job, o.out, o.pitch, slot0);
 }
 
 }  // namespace tc
@@ -2349,9 +2362,18 @@ int tc_setup(const float* chain, int w, int h, const althea_ibl_mip_target* mips
     }
     B.launch_jobs.push_back((int)k);
   }
-  // the paired jobs' pointers are set above too: copy every job into its slot
+  // the paired jobs' pointers are set above too: every job's finish record
   for (const JobPlan& jp : P.jobs)
-    if (jp.finish_slot >= 0) B.fa.job[jp.finish_slot] = jp.J;
+    if (jp.finish_slot >= 0) {
+      FinishJob& f = B.fa.job[jp.finish_slot];
+      f.partial = jp.J.partial;
+      f.wsum_part = jp.J.wsum_part;
+      f.wo = jp.J.wo;
+      f.ho = jp.J.ho;
+      f.nparts = jp.J.nparts;
+      f.kind = jp.J.kind;
+      f.out_half = jp.J.out_half;
+    }
   B.fa.begin[B.fa.n] = B.finish_blocks;
   return ALTHEA_IBL_OK;
 }
