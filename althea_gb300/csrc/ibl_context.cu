@@ -34,19 +34,26 @@ struct althea_ibl_context {
   // forked from and joined back into the caller's stream inside each bake.
   cudaStream_t lut_stream, narrow_stream;
   cudaEvent_t lut_fork, lut_join, narrow_fork, narrow_join;
+  // Precision path: the workspace's direction tables and windows depend on
+  // the sizes only, so the first bake computes them and `tables_done` (an
+  // event after that bake) orders every later bake, on any stream, after it.
+  bool tables_ready;
+  cudaEvent_t tables_done;
 };
 
 static void free_side_streams(althea_ibl_context* c) {
   if (c->lut_stream) cudaStreamDestroy(c->lut_stream);
   if (c->narrow_stream) cudaStreamDestroy(c->narrow_stream);
-  for (cudaEvent_t ev : {c->lut_fork, c->lut_join, c->narrow_fork, c->narrow_join})
+  for (cudaEvent_t ev : {c->lut_fork, c->lut_join, c->narrow_fork, c->narrow_join,
+                         c->tables_done})
     if (ev) cudaEventDestroy(ev);
 }
 
 static cudaError_t make_side_streams(althea_ibl_context* c) {
   cudaError_t e = cudaStreamCreateWithFlags(&c->lut_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->narrow_stream, cudaStreamNonBlocking);
-  for (cudaEvent_t* ev : {&c->lut_fork, &c->lut_join, &c->narrow_fork, &c->narrow_join})
+  for (cudaEvent_t* ev : {&c->lut_fork, &c->lut_join, &c->narrow_fork, &c->narrow_join,
+                          &c->tables_done})
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   return e;
 }
@@ -282,9 +289,21 @@ extern "C" int althea_ibl_bake(althea_ibl_context* c, const althea_ibl_outputs* 
   if (precision) {
     // the planner's source levels (-1), the workspace sized at create
     const SideStream side{c->narrow_stream, c->narrow_fork, c->narrow_join};
-    r = tc_bake(c->chain, w, h, mips, c->cfg.mip_count, nullptr, o->irradiance_dev, c->irr_w,
-                c->irr_h, o->irradiance_pitch_bytes, -1, c->tc_ws, c->tc_ws_bytes,
-                c->cfg.out_format, st, &side);
+    if (c->tables_ready) {
+      const cudaError_t e = cudaStreamWaitEvent(st, c->tables_done, 0);
+      if (e != cudaSuccess) r = cuda_status(e, "tables event wait");
+    }
+    if (!r)
+      r = tc_bake(c->chain, w, h, mips, c->cfg.mip_count, nullptr, o->irradiance_dev, c->irr_w,
+                  c->irr_h, o->irradiance_pitch_bytes, -1, c->tc_ws, c->tc_ws_bytes,
+                  c->cfg.out_format, st, &side, !c->tables_ready);
+    if (!r && !c->tables_ready) {
+      const cudaError_t e = cudaEventRecord(c->tables_done, st);
+      if (e == cudaSuccess)
+        c->tables_ready = true;
+      else
+        r = cuda_status(e, "tables event record");
+    }
     if (lut_side) {  // join even when the bake failed, so no fork is left open
       const cudaError_t e = cudaStreamWaitEvent(st, c->lut_join, 0);
       if (!r && e != cudaSuccess) r = cuda_status(e, "LUT side-stream join");

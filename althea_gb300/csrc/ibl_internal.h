@@ -72,11 +72,13 @@ struct SideStream {
 
 // Precision path (ibl_tc.cu): the bake behind althea_ibl_bake_tc_ex, and its
 // workspace size (0 when the plan is unsupported).  side may be null (one
-// stream).
+// stream).  tables = false: the workspace already holds this plan's direction
+// tables and windows (they depend on the sizes only), from an earlier bake
+// ordered before this one.
 int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
             const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
             int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream,
-            const SideStream* side = nullptr);
+            const SideStream* side = nullptr, bool tables = true);
 size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n,
                           const int* levels, int irr_w, int irr_h, int irr_level);
 

@@ -2460,7 +2460,7 @@ int tc_launch_narrow(const TcBake& B, cudaStream_t ns);
 // Error flag, split planes and tables; with `narrow`, the CUDA-core outputs
 // too (on the side stream when there is one, returned in *ns_out).
 int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream_t* ns_out,
-                   bool narrow = true) {
+                   bool narrow = true, bool tables = true) {
   const TcPlan& P = B.P;
   *ns_out = s;
   cudaError_t e = cudaMemsetAsync(B.base, 0, 256, s);
@@ -2473,8 +2473,10 @@ int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream
     }
     rows_kernel<<<ra.hs, 256, sm, s>>>(ra);
   }
-  int r = tc_launch_tables(B, s);
-  if (r) return r;
+  if (tables) {
+    const int r = tc_launch_tables(B, s);
+    if (r) return r;
+  }
   // The outputs summed on the CUDA cores go to the side stream when there is
   // one (they need the tables, nothing else of the tensor path).
   bool any_narrow = false;
@@ -2581,14 +2583,14 @@ int tc_launch_finish(TcBake& B, cudaStream_t s, cudaStream_t ns, const SideStrea
 int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
             const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
             int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream,
-            const SideStream* side) {
+            const SideStream* side, bool tables) {
   ibl::NvtxRange nvtx_range("precision bake");
   TcBake B;
   int st = tc_setup(chain, w, h, mips, n, levels, irr_out, irr_w, irr_h, irr_pitch, irr_level,
                     ws, ws_bytes, out_format, B);
   if (st) return st;
   cudaStream_t ns = stream;
-  st = tc_launch_prep(B, stream, side, &ns);
+  st = tc_launch_prep(B, stream, side, &ns, true, tables);
   if (!st) st = tc_launch_contract(B, stream);
   if (!st) st = tc_launch_finish(B, stream, ns, side);
   return st;
