@@ -30,27 +30,31 @@
 // The column residue x0 shifts the weights, not the row, so every staged row
 // is the phase row rotated by a multiple of 16 bytes: TMA bulk copies.
 //
-// Kernel (warp-specialised, one CTA per SM, 736 threads):
+// Kernel (warp-specialised, one CTA per SM, 640 threads):
 //   warps 0-15  weight producers: generate A (hi and lo BF16) for one K = 32
 //               stage and write it straight into TMEM with tcgen05.st (four
 //               stages in flight), so no shared-memory bandwidth goes to A;
-//   warps 16-21 one thread each issues the MMAs of one colour channel and one
-//               half of the columns (A from TMEM, B from shared memory; one
-//               channel per thread when N < 32).  A single issuing thread
-//               cannot keep the tensor core busy: on sm_103a one thread issues
-//               a tcgen05.mma about every 64 cycles, while an N = 64 MMA
+//   warps 16-18 one thread each issues the MMAs of one colour channel (A from
+//               TMEM, B from shared memory).  A single issuing thread cannot
+//               keep the tensor core busy: on sm_103a one thread issues a
+//               tcgen05.mma about every 64 cycles, while an N = 64 MMA
 //               executes in 32;
-//   warp 22     one thread stages the Hankel radiance rows with TMA bulk
+//   warp 19     one thread stages the Hankel radiance rows with TMA bulk
 //               copies (up to four slots in flight).
-// Each CTA owns at most kMaxK = 16384 of K (the source rows are split over the
+// Unpaired outputs of 33 to 64 rows run as column tiles instead: the staged
+// Hankel is the A operand (M = 128 output columns) and the weights, written
+// by the producers to shared memory, the B operand (N = 64 rows).
+// Each CTA owns at most kMaxK = 32768 of K (the source rows are split over the
 // grid to guarantee it), so each accumulator is one tensor-core FP32
 // accumulation chain of bounded length; the producer warps move it to the
-// partial sums at the end.  16384 against 8192: half the partial sums to
-// write and add, 7 % faster bakes, and the worst error over the accuracy
-// reports unchanged (the FP32 chain adds about 2e-5 to the mean of the
-// 1024x512 mip).  All hand-offs are mbarriers; every wait is bounded by the
-// global timer and an abort flag, after which the kernel records an error,
-// waits (bounded) for its own MMAs and copies, frees its TMEM and returns.
+// partial sums at the end.  32768 against 16384: half the partial sums to
+// write and add again, 3 % faster bakes, the worst error over the production
+// test unchanged (mean errors of the 1024x512 and 512x256 mips up by 2e-5 to
+// 4e-5).  All hand-offs are mbarriers; every wait is bounded by the global
+// timer and an abort flag, after which the kernel records an error, waits
+// (bounded) for its own MMAs and copies, frees its TMEM and returns.
+// A batch runs every CTA of every probe's contractions as work items of one
+// persistent kernel (contract_persistent_kernel).
 //
 // Precision.  Radiance and weights are each split x = hi + lo (hi = bf16(x),
 // lo = bf16(x - hi)); three MMAs per channel (hi*hi + hi*lo + lo*hi) give
@@ -89,7 +93,7 @@ constexpr int kThreads = 32 * (kLoaderWarp + 1);
 static_assert(kMmaWarp0 == kProducerWarps && kLoaderWarp == kMmaWarp0 + kMmaWarps, "warp roles");
 static_assert(kACol + kStages * kKS <= kTmemCols, "TMEM columns");
 constexpr int kMaxSlots = 4;      // staged radiance rows in flight
-constexpr int kMaxK = 16384;      // K per CTA: one TMEM accumulation chain
+constexpr int kMaxK = 32768;      // K per CTA: one TMEM accumulation chain
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr uint32_t kSleepNs = 200000;  // longest hardware suspension per try (0.2 ms)
 constexpr float kPiF = 3.14159265358979f;
