@@ -208,7 +208,7 @@ void load_tune_file_locked() {
   if (!f) return;
   char key[4096];
   int tx, ty, irr;
-  // Lines naming a tile shape or irradiance target this build does not have
+  // Lines naming a tile shape or irradiance target this library does not have
   // (an edited or stale file) are skipped.
   while (fscanf(f, "%4095s %d %d %d", key, &tx, &ty, &irr) == 4) {
     bool known_irr = false;

@@ -69,6 +69,10 @@ def workload():
 NCU_PREFILTER_TRAFFIC = 156.4e6
 # Warp instructions (smsp__inst_executed.sum) of the same launch, same capture.
 NCU_PREFILTER_WARP_INSTRUCTIONS = 13.95e9
+# DRAM bytes of the precision bake's largest contraction launch (mip 1, 1024x512
+# from level 2) from an ncu capture of the default line: the 19 splits' partial
+# sums are most of it; the operands stay on chip.
+NCU_MIP1_TRAFFIC = 65.5e6
 GB300_SMS = 152
 ISSUE_SLOTS_PER_SM_CYCLE = 4  # one warp instruction per sub-partition per cycle
 
@@ -868,7 +872,12 @@ def run_tc(args):
                              "issued_note": "tcgen05.mma flops issued per bake (split "
                                             "products, visible stages only, M = 128 tiles with "
                                             "padding) over the contraction stage",
-                             "jobs": [list(j) for j in tc_jobs(levels, irr_level)]},
+                             "jobs": [list(j) for j in tc_jobs(levels, irr_level)],
+                             "mip1_launch_dram_bytes": NCU_MIP1_TRAFFIC,
+                             "traffic_note": "per-stage DRAM traffic not captured (traffic "
+                                             "null); the mip-1 launch, 42 % of the stage, "
+                                             "moves 65.5 MB (ncu), against 2.2e12 "
+                                             "algorithmic flops"},
                 "clocks": clk.summary(),
                 "cpu_baseline": cpu}
         print(json.dumps(line))
