@@ -2481,20 +2481,31 @@ int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream
     const int r = tc_launch_tables(B, s);
     if (r) return r;
   }
-  // The outputs summed on the CUDA cores go to the side stream when there is
-  // one (they need the tables, nothing else of the tensor path).
-  bool any_narrow = false;
-  for (const JobPlan& jp : P.jobs) any_narrow |= jp.narrow;
+  // The outputs summed on the CUDA cores and the roughness-0 mips go to the
+  // side stream when there is one (they need the tables and the chain,
+  // nothing else of the tensor path), where they fill the gaps between the
+  // contraction launches.
+  bool any_side = false;
+  for (int k = 0; k < (int)P.jobs.size(); ++k)
+    any_side |= P.jobs[k].narrow || (k < B.n && P.jobs[k].level < 0);
   if (!narrow) return cuda_status(cudaGetLastError(), "tensor path prep launch");
   cudaStream_t ns = s;
-  if (side && any_narrow) {
+  if (side && any_side) {
     e = cudaEventRecord(side->fork, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(side->stream, side->fork, 0);
     if (e != cudaSuccess) return cuda_status(e, "tc side-stream fork");
     ns = side->stream;
   }
   *ns_out = ns;
-  return tc_launch_narrow(B, ns);
+  const int r = tc_launch_narrow(B, ns);
+  if (r) return r;
+  // Roughness-0 mips are a delta (no contraction): the reflected sample itself.
+  for (int m = 0; m < B.n; ++m) {
+    if (P.jobs[m].level >= 0 || P.jobs[m].narrow) continue;
+    const int st = launch_delta_mip(B.chain, B.w, B.h, &B.mips[m], B.out_half, ns);
+    if (st) return st;
+  }
+  return ALTHEA_IBL_OK;
 }
 
 // The outputs summed on the CUDA cores (after the prep launches' tables).
@@ -2569,12 +2580,6 @@ int tc_launch_finish(TcBake& B, cudaStream_t s, cudaStream_t ns, const SideStrea
     finish_all_kernel<<<B.finish_blocks, kFinishThreads, 0, s>>>(B.fa);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "tc finish launch");
-  }
-  // Roughness-0 mips are a delta (no contraction): the reflected sample itself.
-  for (int m = 0; m < B.n; ++m) {
-    if (B.P.jobs[m].level >= 0 || B.P.jobs[m].narrow) continue;
-    const int st = launch_delta_mip(B.chain, B.w, B.h, &B.mips[m], B.out_half, s);
-    if (st) return st;
   }
   if (ns != s) {  // join the side stream
     e = cudaEventRecord(side->join, ns);
