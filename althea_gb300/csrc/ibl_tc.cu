@@ -435,6 +435,10 @@ struct Job {
   // weights the B operand (N = kCtN = 64 rows), written by the producers to
   // shared memory.
   int ct;
+  // Weight sums of a cosine (kind 1) output too -- an irradiance from which a
+  // roughness-1 mip is derived (wsum1: the first output; wsum1_b: the second
+  // of a pair).
+  int wsum1, wsum1_b;
 };
 
 // Weight stages of a column-tile CTA: K-major, no swizzle; per stage and
@@ -725,8 +729,8 @@ __device__ __forceinline__ bool contract_cta(const Job& job, int bx, int by, int
     visible_chunks(vis_row[j], job.krow, KS, kchunks, ca, cb);
     total += (long long)job.g * (ca + kchunks - cb);
   }
-  const bool want_wsum = KIND == 0 && by == 0;
-  const bool want_wsum_b = job.pair && job.kind_b == 0 && by == 0;
+  const bool want_wsum = (KIND == 0 || job.wsum1) && by == 0;
+  const bool want_wsum_b = job.pair && (job.kind_b == 0 || job.wsum1_b) && by == 0;
 
   if (warp < kProducerWarps) {
     // ---- weight producers: rows 32q + lane, K sub-range [8h, 8h + 8) of each stage
@@ -1073,7 +1077,7 @@ __device__ __forceinline__ bool contract_cta_ct(const Job& job, int by, int bz, 
     }
     const float a2 = job.a2;
     constexpr bool ggx = KIND == 0;
-    const bool want = real && ggx && by0;
+    const bool want = real && (ggx || job.wsum1) && by0;
     const float alpha = 0.5f * (1.0f + a2), beta = 0.5f * (a2 - 1.0f), ka = a2 / kPiF;
     const float2 alpha2 = make_float2(alpha, alpha), beta2 = make_float2(beta, beta);
     const float2 minus1 = make_float2(-1.0f, -1.0f);
@@ -1218,7 +1222,7 @@ __device__ __forceinline__ bool contract_cta_ct(const Job& job, int by, int bz, 
         }
       }
     }
-    if (KIND == 0 && by0 && tid < job.ho) {
+    if ((KIND == 0 || job.wsum1) && by0 && tid < job.ho) {
       // weight sums of row i: the warps of row group i / 32, in warp order
       const int i = tid, rg = i >> 5, l = i & 31;
       double ws = 0.0;
@@ -1743,8 +1747,13 @@ __device__ __forceinline__ void store_texel(void* out, long long pitch, int i, i
 // What the finish of one contracted output reads.
 struct FinishJob {
   const float* partial;      // [nparts][3][wo][ho]
-  const double* wsum_part;   // [nparts][ho] (kind 0)
+  const double* wsum_part;   // [nparts][ho] (kind 0, or a kind 1 output with a derived mip)
   int wo, ho, nparts, kind, out_half;
+  // An irradiance's derived roughness-1 mip: texel (x / df, i / df) for
+  // every x and i divisible by df is the normalised cosine sum there.
+  void* dout;
+  long long dpitch;
+  int df;
 };
 
 __device__ __forceinline__ void finish_block(const FinishJob& job, void* __restrict__ out,
@@ -1767,6 +1776,7 @@ __device__ __forceinline__ void finish_block(const FinishJob& job, void* __restr
     sw[r] = 0.0;
   }
   const float* base = job.partial + (size_t)x * job.ho + i0;
+  const bool sums = job.kind == 0 || job.df > 0;  // weight sums to read
   if (live && vec) {
     constexpr int kU = 1;
     for (int k0 = w; k0 < job.nparts; k0 += kU * kFinishWarps) {
@@ -1779,7 +1789,7 @@ __device__ __forceinline__ void finish_block(const FinishJob& job, void* __restr
           const float* p = base + (size_t)k * 3 * plane;
 #pragma unroll
           for (int c = 0; c < 3; ++c) v[u][c] = *reinterpret_cast<const float4*>(p + c * plane);
-          if (job.kind == 0) {
+          if (sums) {
             const double* wp = job.wsum_part + (size_t)k * job.ho + i0;
             wv[u][0] = *reinterpret_cast<const double2*>(wp);
             wv[u][1] = *reinterpret_cast<const double2*>(wp + 2);
@@ -1796,7 +1806,7 @@ __device__ __forceinline__ void finish_block(const FinishJob& job, void* __restr
             s[c][2] += v[u][c].z;
             s[c][3] += v[u][c].w;
           }
-          if (job.kind == 0) {
+          if (sums) {
             sw[0] += wv[u][0].x;
             sw[1] += wv[u][0].y;
             sw[2] += wv[u][1].x;
@@ -1813,7 +1823,7 @@ __device__ __forceinline__ void finish_block(const FinishJob& job, void* __restr
         if (i0 + r < job.ho) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) s[c][r] += p[c * plane + r];
-          if (job.kind == 0) sw[r] += job.wsum_part[(size_t)k * job.ho + i0 + r];
+          if (sums) sw[r] += job.wsum_part[(size_t)k * job.ho + i0 + r];
         }
       }
     }
@@ -1840,6 +1850,11 @@ __device__ __forceinline__ void finish_block(const FinishJob& job, void* __restr
     const double norm = job.kind == 1 ? (1.0 / 3.14159265358979323846) : (1.0 / tw);
     store_texel(out, pitch, i0 + r, x, job.out_half, (float)(t0 * norm), (float)(t1 * norm),
                 (float)(t2 * norm));
+    if (job.df > 0 && x % job.df == 0 && (i0 + r) % job.df == 0) {
+      const double dn = 1.0 / tw;
+      store_texel(job.dout, job.dpitch, (i0 + r) / job.df, x / job.df, job.out_half,
+                  (float)(t0 * dn), (float)(t1 * dn), (float)(t2 * dn));
+    }
   }
 }
 
@@ -1941,6 +1956,11 @@ struct JobPlan {
   void* out = nullptr;   // the output image and its pitch (texels), set at setup
   long long pitch = 0;
   int finish_slot = -1;  // this job's entry in the finish arguments
+  // A roughness-1 GGX mip is the irradiance's normalised cosine sum (D = 1/pi):
+  // written by the irradiance's finish at every derived_factor-th texel, no
+  // work of its own.
+  bool derived = false;
+  int derived_factor = 0;
 };
 
 struct TcPlan {
@@ -2110,6 +2130,16 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
   // A source level named by the caller must exist in the chain (the planner's
   // own choices always do).
   const int nlevels = chain_levels(w, h);
+  // The irradiance's level, and whether it is contracted on the tensor cores:
+  // a roughness-1 mip on the same level whose texel corners are a subset of
+  // the irradiance's is derived from it.  With a2 = 1 the GGX weight is
+  // D cos Omega = cos Omega / pi, the irradiance's weight over pi, so the mip
+  // is the irradiance's sum over its weight sum: the same quadrature.
+  const int irr_lv = irr_w > 0 ? (irr_level >= 0 ? irr_level : planned_level(w, irr_w, 1.0f, true))
+                               : -1;
+  const bool irr_tensor =
+      irr_w > 0 && !(irr_w * irr_h <= kNarrowMax && irr_w <= kNarrowMaxW && 32 % irr_w == 0);
+  bool any_derived = false;
   for (int m = 0; m < n; ++m) {
     if (mips[m].roughness == 0.0f) {  // a delta: handled by the plain path
       P.jobs.push_back(JobPlan{});
@@ -2117,6 +2147,16 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
     }
     const bool planned = !(levels && levels[m] >= 0);
     int lv = planned ? planned_level(w, mips[m].width, mips[m].roughness, false) : levels[m];
+    if (mips[m].roughness == 1.0f && irr_tensor && lv == irr_lv && irr_w % mips[m].width == 0 &&
+        irr_h % mips[m].height == 0 && irr_w / mips[m].width == irr_h / mips[m].height) {
+      JobPlan d;
+      d.level = -3;
+      d.derived = true;
+      d.derived_factor = irr_w / mips[m].width;
+      P.jobs.push_back(d);
+      any_derived = true;
+      continue;
+    }
     if (lv >= nlevels)
       return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT,
                        "tensor path: mip %d source level %d; the chain has levels 0..%d", m, lv,
@@ -2143,6 +2183,7 @@ int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int*
                        irr_w, irr_h, lv);
     int st = add_job(P, w, h, irr_w, irr_h, 1.0f, 1, lv, irr_level < 0, off);
     if (st) return st;
+    if (any_derived) P.jobs.back().J.wsum1 = 1;
   }
   // Pair tensor jobs of at most 64 rows that share every radiance operand
   // (same source level and phase decomposition, same columns): one launch
@@ -2320,6 +2361,11 @@ int tc_setup(const float* chain, int w, int h, const althea_ibl_mip_target* mips
   B.launch_jobs.clear();
   for (size_t k = 0; k < P.jobs.size(); ++k) {
     JobPlan& jp = P.jobs[k];
+    if (jp.derived) {  // written by the irradiance's finish
+      jp.out = mips[k].out_dev;
+      jp.pitch = (long long)(mips[k].pitch_bytes / texel);
+      continue;
+    }
     if (jp.level < 0 && !jp.narrow) continue;  // roughness 0: the delta pass
     Job& J = jp.J;
     J.cos_d = reinterpret_cast<float*>(base + jp.cosd_off);
@@ -2359,6 +2405,7 @@ int tc_setup(const float* chain, int w, int h, const althea_ibl_mip_target* mips
       J.pair = 1;
       J.ho_b = bp.J.ho;
       J.kind_b = bp.J.kind;
+      J.wsum1_b = bp.J.wsum1;
       J.a2_b = bp.J.a2;
       J.out_rows_b = reinterpret_cast<const float*>(base + bp.orows_off);
       J.partial_b = reinterpret_cast<float*>(base + bp.partial_off);
@@ -2377,6 +2424,17 @@ int tc_setup(const float* chain, int w, int h, const althea_ibl_mip_target* mips
       f.nparts = jp.J.nparts;
       f.kind = jp.J.kind;
       f.out_half = jp.J.out_half;
+      f.dout = nullptr;
+      f.dpitch = 0;
+      f.df = 0;
+    }
+  // a derived roughness-1 mip rides on the irradiance's finish (the last job)
+  for (const JobPlan& jp : P.jobs)
+    if (jp.derived && P.jobs.back().finish_slot >= 0) {
+      FinishJob& f = B.fa.job[P.jobs.back().finish_slot];
+      f.dout = jp.out;
+      f.dpitch = jp.pitch;
+      f.df = jp.derived_factor;
     }
   B.fa.begin[B.fa.n] = B.finish_blocks;
   return ALTHEA_IBL_OK;
@@ -2487,7 +2545,7 @@ int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream
   // contraction launches.
   bool any_side = false;
   for (int k = 0; k < (int)P.jobs.size(); ++k)
-    any_side |= P.jobs[k].narrow || (k < B.n && P.jobs[k].level < 0);
+    any_side |= P.jobs[k].narrow || (k < B.n && P.jobs[k].level < 0 && !P.jobs[k].derived);
   if (!narrow) return cuda_status(cudaGetLastError(), "tensor path prep launch");
   cudaStream_t ns = s;
   if (side && any_side) {
@@ -2501,7 +2559,7 @@ int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream
   if (r) return r;
   // Roughness-0 mips are a delta (no contraction): the reflected sample itself.
   for (int m = 0; m < B.n; ++m) {
-    if (P.jobs[m].level >= 0 || P.jobs[m].narrow) continue;
+    if (P.jobs[m].level >= 0 || P.jobs[m].narrow || P.jobs[m].derived) continue;
     const int st = launch_delta_mip(B.chain, B.w, B.h, &B.mips[m], B.out_half, ns);
     if (st) return st;
   }
@@ -2748,7 +2806,8 @@ int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, cudaStrea
       fin_blk.push_back(B->fa.begin[k + 1] - B->fa.begin[k]);
     }
     for (int m = 0; m < B->n; ++m) {
-      if (B->P.jobs[m].level >= 0 || B->P.jobs[m].narrow) continue;  // roughness 0 only
+      if (B->P.jobs[m].level >= 0 || B->P.jobs[m].narrow || B->P.jobs[m].derived)
+        continue;  // roughness 0 only
       const althea_ibl_mip_target& t = B->mips[m];
       DeltaJob d;
       d.chain = B->chain;

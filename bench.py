@@ -510,13 +510,28 @@ def run_ours(args):
     return 0
 
 
+def derived_from_irradiance(w, h, r, lv, irr_level):
+    """The library derives a roughness-1 mip from the irradiance's sums (the
+    GGX weight at a2 = 1 is the cosine weight over pi) when both use one level,
+    the irradiance is contracted on the tensor cores and the mip's texel
+    corners are a subset of the irradiance's."""
+    return (r == 1.0 and lv == irr_level and IRR_W * IRR_H > TC_NARROW_MAX and
+            IRR_W % w == 0 and IRR_H % h == 0 and IRR_W // w == IRR_H // h)
+
+
 def tc_jobs(levels, irr_level):
     """(output width, output height, source width, source height, phase count g)
     of every contraction of one precision bake (the planner's decomposition:
-    g = 1 when 8 % s == 0, s / 8 when s % 8 == 0, else s; s = source / output width)."""
+    g = 1 when 8 % s == 0, s / 8 when s % 8 == 0, else s; s = source / output width).
+    A mip derived from the irradiance's sums adds no job (and no algorithmic
+    flops of its own)."""
     jobs = []
-    for (w, h), lv in list(zip(mip_sizes(), levels)) + [((IRR_W, IRR_H), irr_level)]:
+    rough = roughness() + [None]
+    for ((w, h), lv), r in zip(list(zip(mip_sizes(), levels)) + [((IRR_W, IRR_H), irr_level)],
+                               rough):
         if lv < 0:
+            continue
+        if r is not None and derived_from_irradiance(w, h, r, lv, irr_level):
             continue
         ws, hs = max(ENV_W >> lv, 1), max(ENV_H >> lv, 1)
         s = ws // w

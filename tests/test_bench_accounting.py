@@ -35,7 +35,9 @@ def test_precision_flops_and_jobs():
     pairs = executed_pairs = 0
     for m, ((w, h), lv) in enumerate(list(zip(bench.mip_sizes(), levels)) +
                                      [((128, 64), irr_level)]):
-        if lv >= 0:
+        # mip 8 (8x4, roughness 1, level 1 like the irradiance) is the
+        # irradiance's normalised sum: no pairs of its own
+        if lv >= 0 and m != 8:
             p = w * h * (4096 >> lv) * (2048 >> lv)
             pairs += p
             # mip 1 (roughness 1/8) takes two BF16 products per channel, the rest three
@@ -60,10 +62,11 @@ def test_precision_flops_and_jobs():
 def test_precision_launches_per_bake():
     """12 chain blits, 2 split passes (levels 1 and 2), 1 tables pass,
     6 contractions (mips 1-6 and the irradiance, mip 4 and the irradiance
-    paired in one launch), 1 finish, 2 x 2 for the 16x8 and 8x4 mips on the
-    CUDA cores, 1 delta mip, 1 LUT: 28."""
+    paired in one launch), 1 finish, 2 for the 16x8 mip on the CUDA cores
+    (the 8x4 roughness-1 mip comes out of the irradiance's finish), 1 delta
+    mip, 1 LUT: 26."""
     levels, irr_level = _plan()
-    assert bench.tc_launches(levels, irr_level) == 12 + 2 + 1 + 6 + 1 + 4 + 1 + 1 == 28
+    assert bench.tc_launches(levels, irr_level) == 12 + 2 + 1 + 6 + 1 + 2 + 1 + 1 == 26
 
 
 def test_cpu_strata_cover_every_texel_once():

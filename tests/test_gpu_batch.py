@@ -123,6 +123,35 @@ def test_precision_batch_equals_probes_alone(half):
     batch.close()
 
 
+def test_precision_batch_of_the_batching_configuration_equals_solo_bakes():
+    """Probes of the batching configuration's widths (2048 down to 256, log2(W)-3
+    mips, 32x16 irradiance): their plans hold every kind of work item of the
+    persistent contraction -- two-product row tiles (mip 1), three-product row
+    tiles, column tiles (128x64 outputs), paired and K-interleaved outputs --
+    and CUDA-core narrow outputs.  Every output equals the probe's solo bake."""
+    sizes = [(2048, 1024), (1024, 512), (512, 256), (256, 128)]
+    specs = [ibl.spec_for(w, h) for w, h in sizes]
+    envs = [torch.from_numpy(synth.make_env(w, h, seed=80 + i, sun_max=1e6)).cuda()
+            for i, (w, h) in enumerate(sizes)]
+    stream = torch.cuda.Stream()
+    batch = ibl.ProbeBatch(specs, envs, graph=True, stream=stream, precision=True)
+    batch.run(stream)
+    batch.status(stream)
+    assert batch.info().contraction_items > 0
+    for i, (s, env) in enumerate(zip(specs, envs)):
+        chain = ibl.build_env_chain(env)
+        mips = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+                for w, h in s.mip_sizes]
+        iw, ih = s.irradiance_size
+        irr = torch.empty((ih, iw, 4), dtype=torch.float32, device="cuda")
+        ibl.bake_tc(chain, s.env_width, s.env_height, mips, s.roughness, irradiance=irr)
+        torch.cuda.synchronize()
+        for m in range(len(mips)):
+            assert torch.equal(batch.mips[i][m], mips[m]), (s.env_width, m)
+        assert torch.equal(batch.irradiance[i], irr), s.env_width
+    batch.close()
+
+
 def test_half_outputs_need_the_precision_path():
     spec = ibl.spec_for(64, 32)
     env = torch.from_numpy(synth.make_env(64, 32, seed=3)).cuda()
