@@ -53,8 +53,10 @@
 // 4e-5).  All hand-offs are mbarriers; every wait is bounded by the global
 // timer and an abort flag, after which the kernel records an error, waits
 // (bounded) for its own MMAs and copies, frees its TMEM and returns.
-// A batch runs every CTA of every probe's contractions as work items of one
-// persistent kernel (contract_persistent_kernel).
+// A bake runs every CTA of its contractions as work items of one queue launch
+// (contract_queue_kernel); a batch, those of every probe in one persistent
+// kernel (contract_persistent_kernel).  Either way one CTA per SM pulls
+// items largest first, so a job is split only to bound K per CTA.
 //
 // Precision.  Radiance and weights are each split x = hi + lo (hi = bf16(x),
 // lo = bf16(x - hi)); three MMAs per channel (hi*hi + hi*lo + lo*hi) give
@@ -1262,25 +1264,66 @@ __device__ __forceinline__ void tmem_free_all(uint32_t tmem) {
                  "r"((uint32_t)kTmemCols));
 }
 
-// The contraction kernel of one job.  Grid: (ceil(ho/128), m * nblk, ksplit).
-template <int KIND, bool TWO>
-__global__ void __launch_bounds__(kThreads, 1) contract_kernel(const Job job) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ CtaShared sh;
-  __shared__ uint32_t tmem_base_sh;
-  const uint32_t tmem = tmem_alloc_all(&tmem_base_sh);
-  contract_cta<KIND, TWO>(job, blockIdx.x, blockIdx.y, blockIdx.z, tmem, smem, sh);
-  tmem_free_all(tmem);
+// One work item: the CTA (bx, by, bz) of the grid a job would have as a
+// launch of its own -- the row tile bx (row tiles; column tiles have one),
+// the column block and residue by, the split bz -- run on this CTA, with all
+// of TMEM at `tmem` and the job's record in shared memory.
+__device__ __forceinline__ bool run_item(const Job& job, int bx, int by, int bz, uint32_t tmem,
+                                         unsigned char* smem, CtaShared& sh) {
+  if (job.ct) {
+    if (job.kind == 1) return contract_cta_ct<1, false>(job, by, bz, tmem, smem, sh);
+    if (job.two_prod) return contract_cta_ct<0, true>(job, by, bz, tmem, smem, sh);
+    return contract_cta_ct<0, false>(job, by, bz, tmem, smem, sh);
+  }
+  if (job.kind == 1) return contract_cta<1, false>(job, bx, by, bz, tmem, smem, sh);
+  if (job.two_prod) return contract_cta<0, true>(job, bx, by, bz, tmem, smem, sh);
+  return contract_cta<0, false>(job, bx, by, bz, tmem, smem, sh);
 }
 
-// The contraction kernel of one column-tile job.  Grid: (1, m * nblk, ksplit).
-template <int KIND, bool TWO>
-__global__ void __launch_bounds__(kThreads, 1) contract_ct_kernel(const Job job) {
+__device__ __forceinline__ void copy_job(Job& dst, const Job& src) {
+  static_assert(sizeof(Job) % 8 == 0, "job copy in 8-byte words");
+  const unsigned long long* s = reinterpret_cast<const unsigned long long*>(&src);
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(&dst);
+  for (int e = threadIdx.x; e < (int)(sizeof(Job) / 8); e += blockDim.x) d[e] = s[e];
+}
+
+// The contractions of one bake as one queue: job k owns items
+// [begin[k], begin[k + 1]), item = bx + gx (by + gy bz) within the job.  The
+// jobs come in the order of their items' K, largest first, and one CTA per SM
+// pulls items from a counter until the queue is empty: the jobs need no
+// splits to fill the GPU on their own, and no launch waits for another's tail.
+constexpr int kMaxQueueJobs = ALTHEA_IBL_MAX_MIPS + 1;
+struct QueueArgs {
+  Job jobs[kMaxQueueJobs];
+  int begin[kMaxQueueJobs + 1];
+  int gx[kMaxQueueJobs], gy[kMaxQueueJobs];
+  int n;
+};
+static_assert(sizeof(QueueArgs) <= 4096, "queue arguments fit the kernel parameter space");
+
+__global__ void __launch_bounds__(kThreads, 1)
+    contract_queue_kernel(const __grid_constant__ QueueArgs a, unsigned int* __restrict__ next) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ CtaShared sh;
   __shared__ uint32_t tmem_base_sh;
+  __shared__ int item_sh;
+  __shared__ __align__(16) Job job_sh;
   const uint32_t tmem = tmem_alloc_all(&tmem_base_sh);
-  contract_cta_ct<KIND, TWO>(job, blockIdx.y, blockIdx.z, tmem, smem, sh);
+  for (;;) {
+    if (threadIdx.x == 0) item_sh = (int)atomicAdd(next, 1u);
+    __syncthreads();
+    const int it = item_sh;
+    if (it >= a.begin[a.n]) break;
+    int k = 0;
+    while (k + 1 < a.n && it >= a.begin[k + 1]) ++k;
+    copy_job(job_sh, a.jobs[k]);
+    __syncthreads();
+    const int local = it - a.begin[k], gx = a.gx[k], gy = a.gy[k];
+    const bool ok = run_item(job_sh, local % gx, (local / gx) % gy, local / (gx * gy), tmem,
+                             smem, sh);
+    if (!ok) break;  // uniform: every thread read the same abort flag
+    __syncthreads();  // item_sh and job_sh are rewritten next
+  }
   tmem_free_all(tmem);
 }
 
@@ -1304,7 +1347,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ uint32_t tmem_base_sh;
   __shared__ int item_sh;
   __shared__ __align__(16) Job job_sh;
-  static_assert(sizeof(Job) % 8 == 0, "job copy in 8-byte words");
   const uint32_t tmem = tmem_alloc_all(&tmem_base_sh);
   for (;;) {
     if (threadIdx.x == 0) item_sh = (int)atomicAdd(next, 1u);
@@ -1312,26 +1354,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int it = item_sh;
     if (it >= nitems) break;
     const WorkItem wi = items[it];
-    {
-      const unsigned long long* src = reinterpret_cast<const unsigned long long*>(jobs + wi.job);
-      unsigned long long* dst = reinterpret_cast<unsigned long long*>(&job_sh);
-      for (int e = threadIdx.x; e < (int)(sizeof(Job) / 8); e += blockDim.x) dst[e] = src[e];
-    }
+    copy_job(job_sh, jobs[wi.job]);
     __syncthreads();
-    bool ok;
-    if (job_sh.ct) {
-      if (job_sh.kind == 1)
-        ok = contract_cta_ct<1, false>(job_sh, wi.by, wi.bz, tmem, smem, sh);
-      else if (job_sh.two_prod)
-        ok = contract_cta_ct<0, true>(job_sh, wi.by, wi.bz, tmem, smem, sh);
-      else
-        ok = contract_cta_ct<0, false>(job_sh, wi.by, wi.bz, tmem, smem, sh);
-    } else if (job_sh.kind == 1)
-      ok = contract_cta<1, false>(job_sh, wi.bx, wi.by, wi.bz, tmem, smem, sh);
-    else if (job_sh.two_prod)
-      ok = contract_cta<0, true>(job_sh, wi.bx, wi.by, wi.bz, tmem, smem, sh);
-    else
-      ok = contract_cta<0, false>(job_sh, wi.bx, wi.by, wi.bz, tmem, smem, sh);
+    const bool ok = run_item(job_sh, wi.bx, wi.by, wi.bz, tmem, smem, sh);
     if (!ok) break;  // uniform: every thread read the same abort flag
     __syncthreads();  // item_sh and job_sh are rewritten next
   }
@@ -2084,18 +2109,18 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
                      "shared memory",
                      ow, oh, J.ws);
   // Split the source rows so that no CTA sums more than kMaxK of K (one
-  // source row at least: a phase row longer than kMaxK is one chain), then
-  // round the grid up towards whole waves of the 152 SMs.
-  const int ctas = ((oh + kM - 1) / kM) * J.m * J.nblk;
+  // source row at least: a phase row longer than kMaxK is one chain).  No
+  // more: the contractions of a bake run as one queue of work items (and a
+  // batch's as one persistent kernel), so a job need not fill the GPU alone.
+  // An FP32 tensor-core chain of K = 32768 (2048 MMAs) adds up to about
+  // 1.3e-4 of rounding against the FP64 quadrature at the same level
+  // (measured: 1.26e-4 on a 128x64 mip at K = 32768, 1.14e-4 on a 24x12 one
+  // at K = 14,600), well within the 1e-3 of the precision path.  Planned and
+  // caller-named levels split alike, so the two bake the same levels
+  // bit-identically.
   int rows_max = kMaxK / (J.g * J.kpad);
   if (rows_max < 1) rows_max = 1;
   int ks = (J.hs + rows_max - 1) / rows_max;
-  for (int t = ks; t <= J.hs && t <= 2 * ks; ++t)
-    if ((long long)ctas * t % 152 == 0) {
-      ks = t;
-      break;
-    }
-  if ((long long)ctas * ks < 152) ks = (152 + ctas - 1) / ctas;
   if (ks > J.hs) ks = J.hs;
   if (ks < 1) ks = 1;
   J.ksplit = ks;
@@ -2126,7 +2151,7 @@ constexpr int kMaxTcWidth = 1024;
 
 int make_plan(int w, int h, const althea_ibl_mip_target* mips, int n, const int* levels,
               int irr_w, int irr_h, int irr_level, TcPlan& P) {
-  size_t off = 256;  // error flag first
+  size_t off = 256;  // the error flag (byte 0) and the queue counter (byte 128) first
   // A source level named by the caller must exist in the chain (the planner's
   // own choices always do).
   const int nlevels = chain_levels(w, h);
@@ -2271,7 +2296,7 @@ extern "C" int althea_ibl_tc_stats(int w, int h, const althea_ibl_mip_target* mi
     }
     out->dense_pairs += dense;
     if (jp.paired) continue;  // contracted inside its partner's launch
-    out->tensor_launches += 1;
+    out->tensor_launches = 1;  // one queue launch for every contraction
     const bool pair = jp.pair_with >= 0;
     const int ho_b = pair ? P.jobs[jp.pair_with].J.ho : 0;
     const int KS = J.two_prod ? 2 * kKS : kKS;
@@ -2608,28 +2633,45 @@ int contract_smem(const Job& J) {
   return smem;
 }
 
-// The one-shot kernel of job J.
-void (*contract_kernel_for(const Job& J))(Job) {
-  if (J.ct)
-    return J.kind == 1 ? contract_ct_kernel<1, false>
-                       : (J.two_prod ? contract_ct_kernel<0, true> : contract_ct_kernel<0, false>);
-  return J.kind == 1 ? contract_kernel<1, false>
-                     : (J.two_prod ? contract_kernel<0, true> : contract_kernel<0, false>);
-}
+// K one item of job J sums: its source rows times the phase rows' length.
+long long item_k(const Job& J) { return (long long)((J.hs + J.ksplit - 1) / J.ksplit) * J.g * J.kpad; }
 
+// Every contraction of the bake: one queue launch (contract_queue_kernel).
+// The queue's counter sits in the workspace's first 256 bytes, which the prep
+// zeroes with the error flag.
 int tc_launch_contract(const TcBake& B, cudaStream_t s) {
-  for (int k : B.launch_jobs) {
+  if (B.launch_jobs.empty()) return ALTHEA_IBL_OK;
+  std::vector<int> order = B.launch_jobs;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+    return item_k(B.P.jobs[a].J) > item_k(B.P.jobs[c].J);
+  });
+  if ((int)order.size() > kMaxQueueJobs)
+    return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "tc: %d contraction jobs", (int)order.size());
+  QueueArgs qa;
+  memset(&qa, 0, sizeof(qa));
+  int items = 0, smem = 0;
+  for (int k : order) {
     const Job& J = B.P.jobs[k].J;
-    const int smem = contract_smem(J);
-    dim3 grid(J.ct ? 1 : (J.ho + kM - 1) / kM, J.m * J.nblk, J.ksplit);
-    auto kern = contract_kernel_for(J);
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return cuda_status(e, "tc smem attribute");
-    kern<<<grid, kThreads, smem, s>>>(J);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_status(e, "tc contraction launch");
+    const int gx = J.ct ? 1 : (J.ho + kM - 1) / kM, gy = J.m * J.nblk;
+    qa.jobs[qa.n] = J;
+    qa.gx[qa.n] = gx;
+    qa.gy[qa.n] = gy;
+    qa.begin[qa.n] = items;
+    items += gx * gy * J.ksplit;
+    smem = std::max(smem, contract_smem(J));
+    ++qa.n;
   }
-  return ALTHEA_IBL_OK;
+  qa.begin[qa.n] = items;
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(contract_queue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+  if (e != cudaSuccess) return cuda_status(e, "tc queue setup");
+  unsigned int* next = reinterpret_cast<unsigned int*>(B.base + 128);
+  contract_queue_kernel<<<std::min(std::max(sms, 1), items), kThreads, smem, s>>>(qa, next);
+  return cuda_status(cudaGetLastError(), "tc contraction launch");
 }
 
 int tc_launch_finish(TcBake& B, cudaStream_t s, cudaStream_t ns, const SideStream* side) {

@@ -587,10 +587,9 @@ TC_NARROW_MAX = 128
 
 def tc_launches(levels, irr_level):
     """Kernels of one precision probe step: chain blits, one split pass per
-    source level of a tensor-core job, one tables pass, one contraction per
-    tensor job (pairs share one) and one finish launch for all of them, the
-    narrow sum + its finish per CUDA-core job, one delta pass per roughness-0
-    mip, the LUT."""
+    source level of a tensor-core job, one tables pass, one queue launch for
+    every contraction and one finish launch for all of them, the narrow sum +
+    its finish per CUDA-core job, one delta pass per roughness-0 mip, the LUT."""
     from althea_gb300 import ibl
     jobs = tc_jobs(levels, irr_level)
     tensor = [j for j in jobs if j[0] * j[1] > TC_NARROW_MAX]
@@ -611,7 +610,7 @@ def tc_launches(levels, irr_level):
                 break
     narrow = len(jobs) - len(tensor)
     return ((ibl.chain_levels(ENV_W, ENV_H) - 1) + len(split_levels) + 1 +
-            (len(tensor) - pairs) + (1 if tensor else 0) + 2 * narrow + levels.count(-1) + 1)
+            (1 if tensor else 0) + (1 if tensor else 0) + 2 * narrow + levels.count(-1) + 1)
 
 
 def error_table(env, outs_by_path, irr_by_path, per_mip=128, seed=7):
@@ -875,10 +874,11 @@ def run_tc(args):
                 "gpu_launches": tc_launches(levels, irr_level) * args.steps,
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
                              "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                             "kernel": "contract_kernel (every contraction of one bake; the "
-                                       "timed stage also holds the split, tables, finish and "
-                                       "delta kernels, and the outputs of <= 128 texels, "
-                                       "summed on the CUDA cores)",
+                             "kernel": "contract_queue_kernel (every contraction of one "
+                                       "bake as work items of one launch); achieved over the "
+                                       "whole contraction stage, which also holds the split, "
+                                       "tables, finish and delta kernels and the outputs of "
+                                       "<= 128 texels summed on the CUDA cores",
                              "peak_source": peak_kind + " (bf16 burst)",
                              "algorithmic_flops_per_bake": alg_flops,
                              "rgb_frac": 0.75 * achieved / peak,
@@ -1059,6 +1059,9 @@ def run_batch(args):
                 "path": r["path"], "tile": r["tile"],
                 "persistent_blocks": r["persistent_blocks"],
                 "irradiance_target_blocks": r["irradiance_target_blocks"],
+                **({"contraction_items": r["contraction_items"],
+                    "outputs_equal_solo_bakes": r["outputs_equal_solo_bakes"]}
+                   if precision else {}),
                 "l2": "flushed (256 MB write) between timed steps"},
             "gpu_launches": (r["graph_kernels"] * args.steps if r["graph_kernels"] >= 0
                              else None),

@@ -52,7 +52,7 @@ def test_precision_flops_and_jobs():
     assert work["dense_pairs"] + work["cuda_core_pairs"] == pairs
     assert 0.5 * work["dense_pairs"] < work["visible_pairs"] < work["dense_pairs"]
     assert work["tensor_flops_issued"] >= 2 * 3 * 2 * work["visible_pairs"]
-    assert work["tensor_launches"] == 6
+    assert work["tensor_launches"] == 1  # one queue launch
     # phase counts: s = source / output width; g = 1, s / 8 or s
     for w, h, ws, hs, lv, g in bench.tc_jobs(levels, irr_level):
         s = ws // w
@@ -61,12 +61,11 @@ def test_precision_flops_and_jobs():
 
 def test_precision_launches_per_bake():
     """12 chain blits, 2 split passes (levels 1 and 2), 1 tables pass,
-    6 contractions (mips 1-6 and the irradiance, mip 4 and the irradiance
-    paired in one launch), 1 finish, 2 for the 16x8 mip on the CUDA cores
-    (the 8x4 roughness-1 mip comes out of the irradiance's finish), 1 delta
-    mip, 1 LUT: 26."""
+    1 queue launch for every contraction (mips 1-6 and the irradiance), 1
+    finish, 2 for the 16x8 mip on the CUDA cores (the 8x4 roughness-1 mip
+    comes out of the irradiance's finish), 1 delta mip, 1 LUT: 21."""
     levels, irr_level = _plan()
-    assert bench.tc_launches(levels, irr_level) == 12 + 2 + 1 + 6 + 1 + 2 + 1 + 1 == 26
+    assert bench.tc_launches(levels, irr_level) == 12 + 2 + 1 + 1 + 1 + 2 + 1 + 1 == 21
 
 
 def test_cpu_strata_cover_every_texel_once():
