@@ -39,6 +39,11 @@ struct althea_ibl_context {
   // event after that bake) orders every later bake, on any stream, after it.
   bool tables_ready;
   cudaEvent_t tables_done;
+  // Precision path: timing events around the contraction launch of the last
+  // kTimedBakes bakes (bake i uses pair i % kTimedBakes), read by
+  // althea_ibl_contraction_times.
+  cudaEvent_t timing[ALTHEA_IBL_TIMED_BAKES][2];
+  long long timed_bakes;
 };
 
 static void free_side_streams(althea_ibl_context* c) {
@@ -47,6 +52,9 @@ static void free_side_streams(althea_ibl_context* c) {
   for (cudaEvent_t ev : {c->lut_fork, c->lut_join, c->narrow_fork, c->narrow_join,
                          c->tables_done})
     if (ev) cudaEventDestroy(ev);
+  for (auto& pair : c->timing)
+    for (cudaEvent_t ev : pair)
+      if (ev) cudaEventDestroy(ev);
 }
 
 static cudaError_t make_side_streams(althea_ibl_context* c) {
@@ -55,6 +63,10 @@ static cudaError_t make_side_streams(althea_ibl_context* c) {
   for (cudaEvent_t* ev : {&c->lut_fork, &c->lut_join, &c->narrow_fork, &c->narrow_join,
                           &c->tables_done})
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  if (c->cfg.path == ALTHEA_IBL_PATH_PRECISION)
+    for (auto& pair : c->timing)
+      for (cudaEvent_t& ev : pair)
+        if (e == cudaSuccess) e = cudaEventCreate(&ev);
   return e;
 }
 
@@ -296,7 +308,9 @@ extern "C" int althea_ibl_bake(althea_ibl_context* c, const althea_ibl_outputs* 
     if (!r)
       r = tc_bake(c->chain, w, h, mips, c->cfg.mip_count, nullptr, o->irradiance_dev, c->irr_w,
                   c->irr_h, o->irradiance_pitch_bytes, -1, c->tc_ws, c->tc_ws_bytes,
-                  c->cfg.out_format, st, &side, !c->tables_ready);
+                  c->cfg.out_format, st, &side, !c->tables_ready,
+                  c->timing[c->timed_bakes % ALTHEA_IBL_TIMED_BAKES]);
+    if (!r) ++c->timed_bakes;
     if (!r && !c->tables_ready) {
       const cudaError_t e = cudaEventRecord(c->tables_done, st);
       if (e == cudaSuccess)
@@ -331,6 +345,27 @@ extern "C" int althea_ibl_bake_status(const althea_ibl_context* c, void* stream)
   if (r) return r;
   if (c->cfg.path == ALTHEA_IBL_PATH_PRECISION) return althea_ibl_tc_error(c->tc_ws, stream);
   return cuda_status(cudaStreamSynchronize((cudaStream_t)stream), "bake status");
+}
+
+extern "C" int althea_ibl_contraction_times(const althea_ibl_context* c, float* ms,
+                                            int max_count, int* count) {
+  if (!c || !count || max_count < 0 || (max_count > 0 && !ms))
+    return set_error(ALTHEA_IBL_ERR_INVALID_ARGUMENT, "contraction times: null or negative");
+  *count = 0;
+  if (c->cfg.path != ALTHEA_IBL_PATH_PRECISION)
+    return set_error(ALTHEA_IBL_ERR_UNSUPPORTED, "contraction times: plain-path context");
+  int r = check_device(c);
+  if (r) return r;
+  long long n = c->timed_bakes < ALTHEA_IBL_TIMED_BAKES ? c->timed_bakes : ALTHEA_IBL_TIMED_BAKES;
+  if (n > max_count) n = max_count;
+  for (long long k = 0; k < n; ++k) {  // oldest first
+    const cudaEvent_t* pair = c->timing[(c->timed_bakes - n + k) % ALTHEA_IBL_TIMED_BAKES];
+    cudaError_t e = cudaEventSynchronize(pair[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[k], pair[0], pair[1]);
+    if (e != cudaSuccess) return cuda_status(e, "contraction times");
+  }
+  *count = (int)n;
+  return ALTHEA_IBL_OK;
 }
 
 extern "C" size_t althea_ibl_context_device_bytes(const althea_ibl_context* c) {

@@ -74,11 +74,13 @@ struct SideStream {
 // workspace size (0 when the plan is unsupported).  side may be null (one
 // stream).  tables = false: the workspace already holds this plan's direction
 // tables and windows (they depend on the sizes only), from an earlier bake
-// ordered before this one.
+// ordered before this one.  timing, when not null, is a pair of timing events
+// recorded on `stream` just before and just after the contraction launch.
 int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
             const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
             int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream,
-            const SideStream* side = nullptr, bool tables = true);
+            const SideStream* side = nullptr, bool tables = true,
+            const cudaEvent_t* timing = nullptr);
 size_t tc_workspace_bytes(int w, int h, const althea_ibl_mip_target* mips, int n,
                           const int* levels, int irr_w, int irr_h, int irr_level);
 

@@ -2692,7 +2692,7 @@ int tc_launch_finish(TcBake& B, cudaStream_t s, cudaStream_t ns, const SideStrea
 int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips, int n,
             const int* levels, float* irr_out, int irr_w, int irr_h, size_t irr_pitch,
             int irr_level, void* ws, size_t ws_bytes, int out_format, cudaStream_t stream,
-            const SideStream* side, bool tables) {
+            const SideStream* side, bool tables, const cudaEvent_t* timing) {
   ibl::NvtxRange nvtx_range("precision bake");
   TcBake B;
   int st = tc_setup(chain, w, h, mips, n, levels, irr_out, irr_w, irr_h, irr_pitch, irr_level,
@@ -2700,7 +2700,9 @@ int tc_bake(const float* chain, int w, int h, const althea_ibl_mip_target* mips,
   if (st) return st;
   cudaStream_t ns = stream;
   st = tc_launch_prep(B, stream, side, &ns, true, tables);
+  if (!st && timing) st = cuda_status(cudaEventRecord(timing[0], stream), "timing event");
   if (!st) st = tc_launch_contract(B, stream);
+  if (!st && timing) st = cuda_status(cudaEventRecord(timing[1], stream), "timing event");
   if (!st) st = tc_launch_finish(B, stream, ns, side);
   return st;
 }

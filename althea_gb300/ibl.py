@@ -102,6 +102,7 @@ PATH_PLAIN = 0
 PATH_PRECISION = 1
 FORMAT_RGBA32F = 0
 FORMAT_RGBA16F = 1
+TIMED_BAKES = 64  # contraction launches a context keeps the device time of
 
 
 class ServerConfig(ctypes.Structure):
@@ -180,6 +181,8 @@ def load(build_if_missing: bool = True):
         "althea_ibl_bake": (i, [vp, ctypes.POINTER(Outputs), vp]),
         "althea_ibl_bake_status": (i, [vp, vp]),
         "althea_ibl_context_device_bytes": (sz, [vp]),
+        "althea_ibl_contraction_times": (i, [vp, ctypes.POINTER(ctypes.c_float), i,
+                                             ctypes.POINTER(i)]),
         "althea_ibl_irradiance_noalloc": (i, [vp, i, i, vp, i, i, sz, vp]),
         "althea_ibl_batch_create": (i, [ctypes.POINTER(Probe), i, ctypes.POINTER(BatchParams), vp,
                                         ctypes.POINTER(vp)]),
@@ -557,6 +560,16 @@ class BakeContext:
         """Synchronises the stream; raises IBLError if a precision bake's
         kernels gave up on a bounded wait."""
         _check(load().althea_ibl_bake_status(self._ctx, _stream_ptr(stream)))
+
+    def contraction_times(self) -> List[float]:
+        """Device ms of the contraction launch of the last (up to
+        TIMED_BAKES) precision bakes, oldest first (CUDA events the context
+        records around that launch on the bake's stream)."""
+        buf = (ctypes.c_float * TIMED_BAKES)()
+        n = ctypes.c_int(0)
+        _check(load().althea_ibl_contraction_times(self._ctx, buf, TIMED_BAKES,
+                                                   ctypes.byref(n)))
+        return [float(buf[k]) for k in range(n.value)]
 
 
 def _device_view(ptr: int, nfloats: int):

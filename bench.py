@@ -69,10 +69,11 @@ def workload():
 NCU_PREFILTER_TRAFFIC = 156.4e6
 # Warp instructions (smsp__inst_executed.sum) of the same launch, same capture.
 NCU_PREFILTER_WARP_INSTRUCTIONS = 13.95e9
-# DRAM bytes of the precision bake's largest contraction launch (mip 1, 1024x512
-# from level 2) from an ncu capture of the default line: the 19 splits' partial
-# sums are most of it; the operands stay on chip.
-NCU_MIP1_TRAFFIC = 65.5e6
+# DRAM bytes of one contract_queue_kernel launch (every contraction of the
+# 4096x2048 precision bake) from an ncu capture of the default line: 83.6 MB
+# read (the split radiance planes and the direction tables), 121.3 MB written
+# (the splits' partial sums); the operands are reused on chip.
+NCU_QUEUE_TRAFFIC = 204.9e6
 GB300_SMS = 152
 ISSUE_SLOTS_PER_SM_CYCLE = 4  # one warp instruction per sub-partition per cycle
 
@@ -730,6 +731,11 @@ def run_tc(args):
     with ClockSampler(local) as clk:
         vevs = timed(product_step, 2)
     vctx.status(stream)
+    # the dominant kernel's own device time over the same timed steps: the
+    # context records CUDA events around its contraction launch (one
+    # contract_queue_kernel per bake) on the bake's stream
+    kernel_times = vctx.contraction_times()[-args.steps:]
+    kernel_ms = adist.allreduce_max(float(np.mean(kernel_times)), dev)
     total_ms = adist.allreduce_max(float(np.sum([e[0].elapsed_time(e[1]) for e in vevs])), dev)
     value = args.steps * world / (total_ms / 1e3)
     # stage times (for the roofline): the same kernels through the stateless
@@ -837,9 +843,9 @@ def run_tc(args):
     if rank == 0:
         peak, peak_kind = read_tensor_peak()
         alg_flops, split_flops = tc_flops(levels, irr_level)
-        achieved = alg_flops / (tc_ms / 1e3) / 1e12
+        achieved = alg_flops / (kernel_ms / 1e3) / 1e12
         work = tc_work()
-        issued = work["tensor_flops_issued"] / (tc_ms / 1e3) / 1e12
+        issued = work["tensor_flops_issued"] / (kernel_ms / 1e3) / 1e12
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
             cpu = cpu_baseline_line(env)
@@ -856,7 +862,8 @@ def run_tc(args):
                                   "path = precision): contractions on the caller's stream, "
                                   "LUT and CUDA-core outputs on the context's side streams",
                            "outputs_equal_stateless_calls": bool(product_same),
-                           "stage_ms": {"chain": chain_ms, "contraction": tc_ms, "lut": lut_ms,
+                           "stage_ms": {"chain": chain_ms, "contraction": tc_ms,
+                                        "contract_queue_kernel": kernel_ms, "lut": lut_ms,
                                         "serial_step": serial_ms},
                            "plain_same_map": {"value": 1e3 / plain_ms, "unit": "probes/s",
                                               "ms_per_step": plain_ms,
@@ -873,12 +880,17 @@ def run_tc(args):
                         "outputs_equal_device_path": bool(e2e_same)},
                 "gpu_launches": tc_launches(levels, irr_level) * args.steps,
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
-                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                             "unit": "TFLOP/s", "frac": achieved / peak,
+                             "traffic": NCU_QUEUE_TRAFFIC,
                              "kernel": "contract_queue_kernel (every contraction of one "
-                                       "bake as work items of one launch); achieved over the "
-                                       "whole contraction stage, which also holds the split, "
-                                       "tables, finish and delta kernels and the outputs of "
-                                       "<= 128 texels summed on the CUDA cores",
+                                       "bake as work items of one launch), timed by CUDA events "
+                                       "around it on the bake's stream over the timed steps",
+                             "kernel_ms": kernel_ms,
+                             "stage_frac": alg_flops / (tc_ms / 1e3) / 1e12 / peak,
+                             "stage_note": "stage_frac: the same flops over the whole "
+                                           "contraction stage (split passes, tables, the queue "
+                                           "launch, finish, the outputs summed on the CUDA "
+                                           "cores), timed on one stream",
                              "peak_source": peak_kind + " (bf16 burst)",
                              "algorithmic_flops_per_bake": alg_flops,
                              "rgb_frac": 0.75 * achieved / peak,
@@ -886,13 +898,13 @@ def run_tc(args):
                              "issued_tflops": issued, "issued_frac": issued / peak,
                              "issued_note": "tcgen05.mma flops issued per bake (split "
                                             "products, visible stages only, M = 128 tiles with "
-                                            "padding) over the contraction stage",
+                                            "padding) over the queue kernel's time",
                              "jobs": [list(j) for j in tc_jobs(levels, irr_level)],
-                             "mip1_launch_dram_bytes": NCU_MIP1_TRAFFIC,
-                             "traffic_note": "per-stage DRAM traffic not captured (traffic "
-                                             "null); the mip-1 launch, 42 % of the stage, "
-                                             "moves 65.5 MB (ncu), against 2.2e12 "
-                                             "algorithmic flops"},
+                             "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum "
+                                             "of one contract_queue_kernel launch (ncu): "
+                                             "205 MB against 3.2e12 algorithmic flops, so "
+                                             "DRAM is about 1 % busy and the roofline class "
+                                             "is the tensor pipe"},
                 "clocks": clk.summary(),
                 "cpu_baseline": cpu}
         print(json.dumps(line))

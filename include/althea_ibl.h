@@ -205,6 +205,15 @@ int althea_ibl_bake(althea_ibl_context* ctx, const althea_ibl_outputs* outs, voi
  * (Src/SingleTimeCommandBuffer.cpp:28-54) for callers that want the result
  * checked. */
 int althea_ibl_bake_status(const althea_ibl_context* ctx, void* stream);
+/* Device time of the contraction launch (every tcgen05 contraction of a
+ * bake, one launch) of the last min(bakes, ALTHEA_IBL_TIMED_BAKES, max_count)
+ * precision bakes, oldest first, in ms: from timing events the context
+ * records on the bake's stream around that launch.  Synchronises on those
+ * events.  No counterpart in the reference (its bake is timed nowhere);
+ * for rooflines and monitoring.  ALTHEA_IBL_ERR_UNSUPPORTED on the plain path. */
+#define ALTHEA_IBL_TIMED_BAKES 64
+int althea_ibl_contraction_times(const althea_ibl_context* ctx, float* ms, int max_count,
+                                 int* count);
 /* Device bytes the context holds (chain + workspaces), as allocated at create. */
 size_t althea_ibl_context_device_bytes(const althea_ibl_context* ctx);
 
@@ -247,7 +256,8 @@ typedef struct {
   double tensor_flops;       /* flops of the tcgen05.mma instructions issued (M = 128 tiles,
                                 padding rows and columns included) */
   double cuda_core_pairs;    /* pairs of the outputs summed on the CUDA cores */
-  int tensor_launches;       /* contraction launches (a paired launch counts once) */
+  int tensor_launches;       /* contraction launches: 1 (every contraction of a bake runs
+                                as work items of one queue launch) */
 } althea_ibl_tc_work;
 int althea_ibl_tc_stats(int env_width, int env_height, const althea_ibl_mip_target* mips,
                         int mip_count, const int* levels, int irradiance_width,

@@ -82,6 +82,9 @@ def test_argument_checks_without_gpu():
     assert L.althea_ibl_bake(None, None, None) == ibl.ERR_INVALID_ARGUMENT
     assert L.althea_ibl_bake_status(None, None) == ibl.ERR_INVALID_ARGUMENT
     assert L.althea_ibl_context_device_bytes(None) == 0
+    n = ctypes.c_int(7)
+    assert L.althea_ibl_contraction_times(None, None, 0, ctypes.byref(n)) == \
+        ibl.ERR_INVALID_ARGUMENT
 
 
 def test_context_path_and_format_checks_without_gpu():
