@@ -84,11 +84,13 @@ def test_autotune_choice_is_cached_per_shape():
 
 @pytest.mark.parametrize("half", [False, True])
 def test_precision_batch_equals_probes_alone(half):
-    """The precision path in a batch (one graph: every probe's prep on four
-    streams, one persistent contraction kernel over the work items of every
+    """The precision path in a batch (one graph: the split passes of every
+    probe, one persistent contraction kernel over the work items of every
     probe, every probe's finish) gives every probe exactly its solo
-    tensor-core bake, whose contractions are one launch per output; RGBA16F
-    outputs are the RGBA32F results rounded to half."""
+    tensor-core bake (whose contractions are one queue launch of the same
+    work items); RGBA16F outputs are the RGBA32F results rounded to half.
+    The graph is replayed, then run again on new maps written into the same
+    input buffers: the queue counter and error word restart each run."""
     sizes = [(256, 128), (64, 32), (256, 128), (128, 64), (512, 256)]
     specs = [ibl.spec_for(w, h) for w, h in sizes]
     specs[3].irradiance_size = None
@@ -103,6 +105,17 @@ def test_precision_batch_equals_probes_alone(half):
     info = batch.info()
     assert info.graph == 1
     assert info.contraction_items > 0
+    _check_precision_batch(batch, specs, envs, half)
+    for i, (w, h) in enumerate(sizes):  # new maps in the same buffers
+        envs[i].copy_(torch.from_numpy(synth.make_env(w, h, seed=70 + i, sun_max=1e6)))
+    torch.cuda.synchronize()
+    batch.run(stream)
+    batch.status(stream)
+    _check_precision_batch(batch, specs, envs, half)
+    batch.close()
+
+
+def _check_precision_batch(batch, specs, envs, half):
     for i, (s, env) in enumerate(zip(specs, envs)):
         chain = ibl.build_env_chain(env)
         mips = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
@@ -120,7 +133,6 @@ def test_precision_batch_equals_probes_alone(half):
             assert torch.equal(batch.mips[i][m], want), (i, m)
         if irr is not None:
             assert torch.equal(batch.irradiance[i], irr.half() if half else irr), i
-    batch.close()
 
 
 def test_precision_batch_of_the_batching_configuration_equals_solo_bakes():

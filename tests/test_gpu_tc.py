@@ -248,6 +248,29 @@ def test_context_precision_bake_equals_stateless_bake(fmt):
     assert torch.equal(res.irradianceMap, ref_irr.to(want))
 
 
+def test_context_rebake_with_another_map_equals_stateless_bake():
+    """A context re-baked with a different map (its queue counter, error word
+    and tables reused from the first bake) writes the second map's stateless
+    bake bit for bit, not the first map's."""
+    w, h = 512, 256
+    cfg = ibl.make_config(w, h, irradiance_size=(32, 16), mip_count=6, path=ibl.PATH_PRECISION)
+    ctx = ibl.BakeContext(cfg)
+    irr, mips, _ = ctx.allocate_outputs()
+    envs = [torch.from_numpy(synth.make_env(w, h, seed=20 + k, sun_max=1e6)).cuda()
+            for k in range(2)]
+    rough = [ctx.mip_info(m)[2] for m in range(6)]
+    for env_d in envs:
+        ctx.upload_env(env_d)
+        ctx.bake(irr, mips, None, check=True)
+        ref_mips = [torch.empty_like(m) for m in mips]
+        ref_irr = torch.empty_like(irr)
+        ibl.bake_tc(ibl.build_env_chain(env_d), w, h, ref_mips, rough, irradiance=ref_irr)
+        torch.cuda.synchronize()
+        assert all(torch.equal(a, b) for a, b in zip(mips, ref_mips))
+        assert torch.equal(irr, ref_irr)
+    ctx.close()
+
+
 def test_context_times_its_contraction_launch():
     """A precision context records CUDA events around its contraction launch
     (one queue launch per bake): one positive device time per bake, oldest
