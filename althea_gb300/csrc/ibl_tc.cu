@@ -1692,18 +1692,27 @@ struct RowsArgs {
   __nv_bfloat16* out[kMaxRowsOut];
 };
 
+// The staged row in shared memory: element x of a plane at x + 2 (x / 64).
+// The phase-row pass below has lane c read elements 4 g c + ph, 4 g apart:
+// unswizzled that is a 2g-word stride (a 16-way bank conflict at g = 8, 32-way
+// from g = 16); the extra word every 64 elements spreads the lanes over
+// distinct banks for g <= 16 (two-way at g = 32).
+__host__ __device__ constexpr int rows_swz(int x) { return x + 2 * (x >> 6); }
+__host__ __device__ constexpr int rows_plane(int ws) { return rows_swz(ws) + 2; }
+constexpr int rows_smem_bytes(int ws) { return 6 * rows_plane(ws) * 2; }
+
 __device__ __forceinline__ void rows_block(const RowsArgs& a, int j) {
   extern __shared__ __nv_bfloat16 row_sm[];
   const float4* __restrict__ src = a.src;
-  const int ws = a.ws, hs = a.hs;
+  const int ws = a.ws, hs = a.hs, pl = rows_plane(ws);
   for (int x = threadIdx.x; x < ws; x += blockDim.x) {
     const float4 v = src[(size_t)j * ws + x];
     const float c[3] = {v.x, v.y, v.z};
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
       const __nv_bfloat16 h = __float2bfloat16_rn(c[ch]);
-      row_sm[(2 * ch) * ws + x] = h;
-      row_sm[(2 * ch + 1) * ws + x] = __float2bfloat16_rn(c[ch] - __bfloat162float(h));
+      row_sm[(2 * ch) * pl + rows_swz(x)] = h;
+      row_sm[(2 * ch + 1) * pl + rows_swz(x)] = __float2bfloat16_rn(c[ch] - __bfloat162float(h));
     }
   }
   __syncthreads();
@@ -1713,16 +1722,16 @@ __device__ __forceinline__ void rows_block(const RowsArgs& a, int j) {
     const int g = a.g[q], krow = ws / g, quads = krow >> 2;
     __nv_bfloat16* __restrict__ out = a.out[q];
     for (int p = 0; p < 6; ++p) {
-      const __nv_bfloat16* rp = row_sm + p * ws;
+      const __nv_bfloat16* rp = row_sm + p * pl;
       __nv_bfloat16* op = out + ((size_t)p * hs + j) * ws;
       for (int ph = 0; ph < g; ++ph) {
         for (int c = threadIdx.x; c < quads; c += blockDim.x) {
           const int u = 4 * c;
           __nv_bfloat162 v01, v23;
-          v01.x = rp[g * u + ph];
-          v01.y = rp[g * (u + 1) + ph];
-          v23.x = rp[g * (u + 2) + ph];
-          v23.y = rp[g * (u + 3) + ph];
+          v01.x = rp[rows_swz(g * u + ph)];
+          v01.y = rp[rows_swz(g * (u + 1) + ph)];
+          v23.x = rp[rows_swz(g * (u + 2) + ph)];
+          v23.y = rp[rows_swz(g * (u + 3) + ph)];
           uint2 w;
           w.x = *reinterpret_cast<const uint32_t*>(&v01);
           w.y = *reinterpret_cast<const uint32_t*>(&v23);
@@ -2103,7 +2112,7 @@ int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, 
                      ow, oh, J.ws, J.krow);
   for (J.nslots = kMaxSlots; J.nslots > 2; --J.nslots)
     if (smem_plan(J).total + 4096 <= (size_t)kSmemLimit) break;
-  if (smem_plan(J).total + 4096 > (size_t)kSmemLimit)
+  if (smem_plan(J).total + 4096 > (size_t)kSmemLimit || rows_smem_bytes(J.ws) > kSmemLimit)
     return set_error(ALTHEA_IBL_ERR_UNSUPPORTED,
                      "tensor path: a %dx%d output against a %d-wide level needs too much "
                      "shared memory",
@@ -2553,7 +2562,7 @@ int tc_launch_prep(TcBake& B, cudaStream_t s, const SideStream* side, cudaStream
   cudaError_t e = cudaMemsetAsync(B.base, 0, 256, s);
   if (e != cudaSuccess) return cuda_status(e, "tc error flag");
   for (const RowsArgs& ra : rows_jobs(B)) {
-    const int sm = 6 * ra.ws * 2;
+    const int sm = rows_smem_bytes(ra.ws);
     if (sm > 48 * 1024) {
       e = cudaFuncSetAttribute(rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
       if (e != cudaSuccess) return cuda_status(e, "tc rows smem attribute");
@@ -2833,7 +2842,7 @@ int tc_batch_create(const TcBatchProbe* probes, int n, int out_format, cudaStrea
     for (const RowsArgs& ra : rows_jobs(*B)) {
       rows.push_back(ra);
       rows_blk.push_back(ra.hs);
-      b->rows.smem = std::max(b->rows.smem, 6 * ra.ws * 2);
+      b->rows.smem = std::max(b->rows.smem, rows_smem_bytes(ra.ws));
     }
     for (const JobPlan& jp : B->P.jobs) {
       if (!jp.narrow) continue;
