@@ -763,7 +763,7 @@ def run_tc(args):
                           lut_samples=LUT_SAMPLES, path=ibl.PATH_PRECISION)
     host_env = torch.from_numpy(env).pin_memory()
     lanes = []
-    for _ in range(2):
+    for _ in range(args.e2e_lanes):
         ctx = ibl.BakeContext(cfg)
         e_irr, e_mips, e_lut = ctx.allocate_outputs(device=dev)
         dev_outs = e_mips + [e_irr, e_lut]
@@ -772,7 +772,7 @@ def run_tc(args):
                       torch.cuda.Stream(device=dev)))
 
     def e2e_step(i):
-        ctx, e_irr, e_mips, e_lut, dev_outs, host_outs, st = lanes[i % 2]
+        ctx, e_irr, e_mips, e_lut, dev_outs, host_outs, st = lanes[i % len(lanes)]
         ctx.upload_env(host_env, st)
         ctx.bake(e_irr, e_mips, e_lut, st)
         for hdst, dsrc in zip(host_outs, dev_outs):
@@ -781,19 +781,21 @@ def run_tc(args):
 
     def e2e_run(nsteps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0, s1 = lanes[0][6], lanes[1][6]
+        s0 = lanes[0][6]
         a.record(s0)
-        s1.wait_event(a)
+        for ln in lanes[1:]:
+            ln[6].wait_event(a)
         for i in range(nsteps):
             e2e_step(i)
-        done1 = torch.cuda.Event()
-        done1.record(s1)
-        s0.wait_event(done1)
+        for ln in lanes[1:]:
+            done = torch.cuda.Event()
+            done.record(ln[6])
+            s0.wait_event(done)
         b.record(s0)
         torch.cuda.synchronize()
         return a.elapsed_time(b)
 
-    e2e_run(max(2, args.warmup))
+    e2e_run(max(len(lanes), args.warmup))  # every lane bakes before its outputs are checked
     for ln in lanes:
         ln[0].status(ln[6])  # no bounded wait gave up
     # the context's bake is the stateless bake above: same kernels, same bits
@@ -875,8 +877,8 @@ def run_tc(args):
                 "e2e": {"value": world * 1e3 / e2e_ms, "unit": "probes/s",
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "api": "BakeContext (althea_ibl_create / upload_env / bake, "
-                               "path = precision), two contexts on two streams taking "
-                               "alternate steps",
+                               f"path = precision), {args.e2e_lanes} contexts on their own "
+                               "streams taking steps in turn",
                         "outputs_equal_device_path": bool(e2e_same)},
                 "gpu_launches": tc_launches(levels, irr_level) * args.steps,
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
@@ -1391,6 +1393,8 @@ def main():
     ap.add_argument("--rates", type=float, nargs="+", default=[50, 200, 500, 1000, 2000])
     ap.add_argument("--requests", type=int, default=10000, help="serving: requests per rate")
     ap.add_argument("--budget-gb", type=float, default=40.0)
+    ap.add_argument("--e2e-lanes", type=int, default=2,
+                    help="e2e: bake contexts on their own streams taking steps in turn")
     ap.add_argument("--inflight", type=int, default=16)
     ap.add_argument("--pool", type=int, default=64, help="serving: resident skies")
     ap.add_argument("--no-sub", action="store_true",
