@@ -503,6 +503,11 @@ __device__ __forceinline__ bool settle(uint64_t* bar, uint32_t parity) {
 // Eight weights of one output row at K = kb .. kb + 7 of phase row cdrow:
 // w = k1 c D(c) (GGX, D = 1 / (alpha + beta c)^2) or k1 c (cosine), c =
 // ccq cos_d + ssq, clamped at 0 and zero past krow; packed FP32x2 arithmetic.
+__device__ __forceinline__ __nv_bfloat162 bf16_zero2() { return __float2bfloat162_rn(0.0f); }
+
+// CLAMP = false leaves the negative weights (beyond a row's horizon) to the
+// caller, which clamps them after rounding to BF16 (two per instruction).
+template <bool CLAMP = true>
 __device__ __forceinline__ void weights8(const float* cdrow, int kb, int krow, float2 ccq2,
                                          float2 ssq2, float2 k12, float2 alpha2, float2 beta2,
                                          bool ggx, float2 (&w)[4]) {
@@ -524,10 +529,12 @@ __device__ __forceinline__ void weights8(const float* cdrow, int kb, int krow, f
       w[2 * e + 1] = __fmul2_rn(k12, c23);
     }
   }
+  if (CLAMP) {
 #pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    w[e].x = fmaxf(w[e].x, 0.0f);
-    w[e].y = fmaxf(w[e].y, 0.0f);
+    for (int e = 0; e < 4; ++e) {
+      w[e].x = fmaxf(w[e].x, 0.0f);
+      w[e].y = fmaxf(w[e].y, 0.0f);
+    }
   }
   if (kb + 8 > krow) {
 #pragma unroll
@@ -784,21 +791,27 @@ __device__ __forceinline__ bool contract_cta(const Job& job, int bx, int by, int
            for (int gq = 0; gq < NG; ++gq) {
             const int kb = kc * KS + KW * h + 8 * gq;
             float2 w[4];
-            weights8(cdrow, kb, job.krow, ccq2, ssq2, k12, alpha2, beta2, ggx, w);
+            weights8<!TWO>(cdrow, kb, job.krow, ccq2, ssq2, k12, alpha2, beta2, ggx, w);
+            __nv_bfloat162 h2s[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-              const __nv_bfloat162 h2 = __floats2bfloat162_rn(w[e].x, w[e].y);
+              __nv_bfloat162 h2 = __floats2bfloat162_rn(w[e].x, w[e].y);
+              if (TWO) h2 = __hmax2(h2, bf16_zero2());  // max(bf16(w), 0) = bf16(max(w, 0))
+              h2s[e] = h2;
               hw[4 * gq + e] = *reinterpret_cast<const uint32_t*>(&h2);
-              if (TWO) {
-                w[e] = __bfloat1622float2(h2);  // the weight the MMAs use
-              } else {
+              if (!TWO) {
                 const float2 lo = __ffma2_rn(__bfloat1622float2(h2), minus1, w[e]);
                 const __nv_bfloat162 l2 = __floats2bfloat162_rn(lo.x, lo.y);
                 lw[e] = *reinterpret_cast<const uint32_t*>(&l2);
               }
             }
-            if (want)
+            if (want) {
+              if (TWO) {  // the weights the MMAs use
+#pragma unroll
+                for (int e = 0; e < 4; ++e) w[e] = __bfloat1622float2(h2s[e]);
+              }
               rowsum2 = __fadd2_rn(__fadd2_rn(rowsum2, w[0]), __fadd2_rn(__fadd2_rn(w[1], w[2]), w[3]));
+            }
            }
           }
           // Software pipeline: the previous stage's TMEM stores landed while
