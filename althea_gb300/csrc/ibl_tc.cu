@@ -628,9 +628,9 @@ __device__ __forceinline__ void inval_barriers(CtaShared& sh) {
   }
 }
 
-// One CTA of a contraction: output rows bx * 128 .., column block by, source
-// rows of split bz -- the grid coordinates of a one-shot launch, or one work
-// item of the persistent batch kernel.  Each CTA sums at most kMaxK of K in
+// One work item of a contraction: output rows bx * 128 .., column block by,
+// source rows of split bz (an item of a bake's queue launch or of a batch's
+// persistent kernel: the same body, so the same bits).  Each CTA sums at most kMaxK of K in
 // one TMEM accumulation chain per channel.  The caller holds all 512 TMEM
 // columns at `tmem`.  Returns false when a bounded wait gave up (the job's
 // error word is set).  Otherwise every barrier is quiescent and invalidated
@@ -1343,14 +1343,14 @@ __global__ void __launch_bounds__(kThreads, 1)
 // One CTA of some job of a batch.
 struct WorkItem {
   int job;         // index into the job table
-  int bx, by, bz;  // the CTA of that job's one-shot grid
+  int bx, by, bz;  // row tile, column block and split within the job
 };
 
 // The persistent contraction kernel of a batch: one CTA per SM (each holds
 // all of TMEM for its lifetime), pulling (job, tile, column block, split)
 // work items from a queue in the order given (largest first) until it is
-// empty.  Each item runs exactly the CTA of that job's one-shot launch, so
-// the results are the same bits.  A CTA whose bounded wait gave up stops
+// empty.  Each item runs exactly the body that the probe's single bake runs
+// for it (contract_queue_kernel), so the results are the same bits.  A CTA whose bounded wait gave up stops
 // taking items (the job's error word is set).
 __global__ void __launch_bounds__(kThreads, 1)
     contract_persistent_kernel(const Job* __restrict__ jobs, const WorkItem* __restrict__ items,
