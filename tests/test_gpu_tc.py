@@ -248,6 +248,32 @@ def test_context_precision_bake_equals_stateless_bake(fmt):
     assert torch.equal(res.irradianceMap, ref_irr.to(want))
 
 
+def test_queue_launch_with_the_most_contraction_jobs():
+    """The largest plan the C ABI admits: 16 mips and the irradiance, each a
+    contraction of its own (128 rows: no pairs, no K interleave), so the
+    bake's queue launch holds 17 jobs (136 work items).  Every output matches
+    the FP64 quadrature over level 0 within the same-level bound."""
+    w, h = 512, 256
+    env = synth.make_env(w, h, seed=12, sun_max=1e6)
+    chain_d = torch.from_numpy(oracle.build_chain(env)).cuda()
+    n = 16
+    rough = [0.2 + 0.05 * k for k in range(n)]
+    outs = [torch.empty((128, 256, 4), dtype=torch.float32, device="cuda") for _ in range(n)]
+    irr = torch.empty((128, 256, 4), dtype=torch.float32, device="cuda")
+    ibl.bake_tc(chain_d, w, h, outs, rough, irradiance=irr, levels=[0] * n, irradiance_level=0)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(12)
+    idx = rng.choice(256 * 128, size=32, replace=False)
+    xy = np.stack([idx % 256, idx // 256], 1).astype(np.int32)
+    for r, o in zip(rough, outs):
+        ref = oracle.quad_prefilter(env, 256, 128, r, xy)[:, :3]
+        got = o.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
+        assert _rel(got, ref).max() <= SAME_LEVEL_TOL, (r, _rel(got, ref).max())
+    ref = oracle.quad_irradiance(env, 256, 128, xy)[:, :3]
+    got = irr.cpu().numpy()[xy[:, 1], xy[:, 0], :3]
+    assert _rel(got, ref).max() <= SAME_LEVEL_TOL, _rel(got, ref).max()
+
+
 def test_context_rebake_with_another_map_equals_stateless_bake():
     """A context re-baked with a different map (its queue counter, error word
     and tables reused from the first bake) writes the second map's stateless
