@@ -2055,9 +2055,11 @@ int level_index(TcPlan& P, int w, int h, int level, int g, size_t& off) {
 // quadrature over level 0 on the 4096x2048 map with 1e6 suns (seeds 0-2,
 // every texel within 5 degrees of a sun, seams, poles and 512 random texels),
 // mip 1 (roughness 1/8 from a 1024-wide level) reaches 5.4e-4 with it against
-// 1.8e-4 without; the rougher mips already carry up to 7.6e-4 from their
-// source level and keep three products.
-constexpr float kTwoProdMaxRoughness = 0.2f;
+// 1.8e-4 without, and mip 2 (roughness 1/4, same level) 5.7e-4 against
+// 2.6e-4 over seeds 0-4 (the batch probes' mip 1 of roughness 1/4, and the
+// 512x256 probe's at every texel, are in the GPU tests).  The rougher mips
+// already carry up to 7.6e-4 from their source level and keep three products.
+constexpr float kTwoProdMaxRoughness = 0.25f;
 
 // Adds a contraction job (mip or irradiance) to the plan.
 int add_job(TcPlan& P, int w, int h, int ow, int oh, float roughness, int kind, int level,

@@ -543,12 +543,12 @@ def tc_jobs(levels, irr_level):
 
 # Glossy mips at most this rough take the library's two-product split (BF16
 # hi weights: hi*hi + hi*lo per channel) when the planner chose their level.
-TC_TWO_PRODUCT_MAX_ROUGHNESS = 0.2
+TC_TWO_PRODUCT_MAX_ROUGHNESS = 0.25
 
 
 def tc_products(w, h, lv):
     """BF16 products per channel and pair of one output of the default bake:
-    2 for a planned GGX mip of roughness <= 0.2, else 3 (hi*hi, hi*lo, lo*hi)."""
+    2 for a planned GGX mip of roughness <= 0.25, else 3 (hi*hi, hi*lo, lo*hi)."""
     for (mw, mh), r in zip(mip_sizes(), roughness()):
         if (mw, mh) == (w, h) and r > 0.0:
             return 2 if r <= TC_TWO_PRODUCT_MAX_ROUGHNESS else 3

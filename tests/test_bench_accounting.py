@@ -40,8 +40,9 @@ def test_precision_flops_and_jobs():
         if lv >= 0 and m != 8:
             p = w * h * (4096 >> lv) * (2048 >> lv)
             pairs += p
-            # mip 1 (roughness 1/8) takes two BF16 products per channel, the rest three
-            executed_pairs += p * (2 if m == 1 else 3)
+            # mips 1 and 2 (roughness 1/8 and 1/4) take two BF16 products per
+            # channel, the rest three
+            executed_pairs += p * (2 if m in (1, 2) else 3)
     alg, executed = bench.tc_flops(levels, irr_level)
     assert alg == 8 * pairs and executed == 6 * executed_pairs
     assert round(alg / 1e12, 2) == 3.21

@@ -4,8 +4,9 @@ quadrature over level 0 (the oracle's quad_prefilter / quad_irradiance).
 The benchmark map: 4096x2048, suns log-uniform up to 1e6 (seed 0), 9 mips
 from 2048x1024 (roughness m/8) and a 128x64 irradiance, baked by the tensor-core
 path with the planner's source levels -- the configuration the headline
-throughput is quoted on -- and a 2048x1024 probe of the batch configuration
-(6 mips from 1024x512, 32x16 irradiance).  Checked texels, per output with
+throughput is quoted on -- and probes of every width of the batch
+configuration (2048 down to 256 wide: log2(W) - 3 mips from W/2, 32x16
+irradiance).  Checked texels, per output with
 roughness > 0 and for the irradiance:
 
   * a seeded random sample;
@@ -76,7 +77,9 @@ def rel_errors(got, ref):
     return np.where(np.isfinite(got), e, np.inf)  # a missing output is a failure
 
 
-@pytest.mark.parametrize("env_w,per,cap", [(4096, 1024, 4096), (2048, 1024, 2048)])
+@pytest.mark.parametrize("env_w,per,cap", [(4096, 1024, 4096), (2048, 1024, 2048),
+                                           (1024, 1024, 1024), (512, 1024, 1024),
+                                           (256, 1024, 512)])
 def test_precision_path_within_1e3_of_fp64_at_production_size(env_w, per, cap):
     w, h, sizes, rough, (iw, ih) = probe_config(env_w)
     env = synth.make_env(w, h, seed=0, sun_max=SUN_MAX)
