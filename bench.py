@@ -70,10 +70,10 @@ NCU_PREFILTER_TRAFFIC = 156.4e6
 # Warp instructions (smsp__inst_executed.sum) of the same launch, same capture.
 NCU_PREFILTER_WARP_INSTRUCTIONS = 13.95e9
 # DRAM bytes of one contract_queue_kernel launch (every contraction of the
-# 4096x2048 precision bake) from an ncu capture of the default line: 83.6 MB
-# read (the split radiance planes and the direction tables), 121.9 MB written
+# 4096x2048 precision bake) from an ncu capture of the default line: 83.7 MB
+# read (the split radiance planes and the direction tables), 122.1 MB written
 # (the splits' partial sums); the operands are reused on chip.
-NCU_QUEUE_TRAFFIC = 205.5e6
+NCU_QUEUE_TRAFFIC = 205.8e6
 GB300_SMS = 152
 ISSUE_SLOTS_PER_SM_CYCLE = 4  # one warp instruction per sub-partition per cycle
 
