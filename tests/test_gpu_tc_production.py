@@ -77,13 +77,17 @@ def rel_errors(got, ref):
     return np.where(np.isfinite(got), e, np.inf)  # a missing output is a failure
 
 
-@pytest.mark.parametrize("env_w,per,cap", [(4096, 1024, 4096), (2048, 1024, 2048),
-                                           (1024, 1024, 1024), (512, 1024, 1024),
-                                           (256, 1024, 512)])
-def test_precision_path_within_1e3_of_fp64_at_production_size(env_w, per, cap):
+# (map width, random texels per output, cap on near-sun texels, map seed): seed 1
+# of the 2048-wide probe holds the closest approach to the bar measured (8.2e-4,
+# its two-product mip 1)
+@pytest.mark.parametrize("env_w,per,cap,seed", [(4096, 1024, 4096, 0), (2048, 1024, 2048, 0),
+                                                (2048, 1024, 2048, 1), (1024, 1024, 1024, 0),
+                                                (1024, 1024, 1024, 2), (512, 1024, 1024, 0),
+                                                (256, 1024, 512, 0)])
+def test_precision_path_within_1e3_of_fp64_at_production_size(env_w, per, cap, seed):
     w, h, sizes, rough, (iw, ih) = probe_config(env_w)
-    env = synth.make_env(w, h, seed=0, sun_max=SUN_MAX)
-    suns = synth.sun_params(w, h, seed=0, sun_max=SUN_MAX)
+    env = synth.make_env(w, h, seed=seed, sun_max=SUN_MAX)
+    suns = synth.sun_params(w, h, seed=seed, sun_max=SUN_MAX)
     chain = ibl.build_env_chain(torch.from_numpy(env).cuda())
     outs = [torch.full((mh, mw, 4), float("nan"), dtype=torch.float32, device="cuda")
             for mw, mh in sizes]
@@ -95,7 +99,7 @@ def test_precision_path_within_1e3_of_fp64_at_production_size(env_w, per, cap):
     irr = irr.cpu().numpy()
     for o in outs + [irr]:
         assert np.isfinite(o).all()
-    rng = np.random.default_rng(2024)
+    rng = np.random.default_rng(2024 + seed)
     nt = os.cpu_count() or 0
     worst, report = {}, {}
     targets = [(f"mip{m}", mw, mh, r, outs[m]) for m, ((mw, mh), r) in
@@ -110,6 +114,6 @@ def test_precision_path_within_1e3_of_fp64_at_production_size(env_w, per, cap):
         e = rel_errors(img[xy[:, 1], xy[:, 0], :3], ref)
         worst[name] = float(e.max())
         report[name] = {"texels": int(len(xy)), "max": float(e.max()), "mean": float(e.mean())}
-    print(json.dumps({"map": [w, h], "levels": levels, "irradiance_level": irr_level,
+    print(json.dumps({"map": [w, h], "seed": seed, "levels": levels, "irradiance_level": irr_level,
                       "outputs": report}))
     assert max(worst.values()) <= BAR, (levels, irr_level, worst)
