@@ -231,6 +231,31 @@ AGB_FN float agb_div_rcp(float a, float b, float r) {
   return a == 0.0f ? q0 : q;
 }
 
+/* Split-sum BRDF LUT (Karis 2013, IntegrateBRDF): one Hammersley sample's
+ * terms for a texel with view vector (vx, 0, vz), given the sample's half
+ * vector (hx, 0-plane, hz), 1 / NoH, omk = 1 - k, k = alpha / 2 and
+ * gv = G1(V) / NoV: adds (1 - Fc) G_vis to *sum_a and Fc G_vis to *sum_b,
+ * G_vis = G1(L) G1(V) VoH / (NoH NoV), Fc = (1 - VoH)^5.  Every product-sum
+ * is one explicit fma and 1 / (NoL (1 - k) + k) a correctly rounded
+ * reciprocal, so the LUT kernels and the CPU oracle, which both call this,
+ * compute the same bits. */
+AGB_FN void agb_lut_sample(float vx, float vz, float hx, float hz, float rnoh, float omk, float k,
+                           float gv, float* sum_a, float* sum_b) {
+  const float vdh = AGB_FMA(vx, hx, vz * hz);
+  const float lz = AGB_FMA(2.0f * vdh, hz, -vz);
+  const float nol = lz > 0.0f ? (lz < 1.0f ? lz : 1.0f) : 0.0f;
+  const float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
+  if (nol > 0.0f) {
+    const float g1l = nol * (1.0f / AGB_FMA(nol, omk, k));
+    const float g_vis = ((g1l * gv) * voh) * rnoh;
+    const float tt = 1.0f - voh;
+    const float t2 = tt * tt;
+    const float fc = t2 * t2 * tt;
+    *sum_a = AGB_FMA(1.0f - fc, g_vis, *sum_a);
+    *sum_b = AGB_FMA(fc, g_vis, *sum_b);
+  }
+}
+
 /* Correctly rounded reciprocals of 2*pi and pi as single-precision values
  * (1 / 6.2831855f and 1 / 3.1415927f). */
 #define AGB_RCP_TWO_PI_F 0x1.45f306p-3f

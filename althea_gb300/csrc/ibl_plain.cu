@@ -336,21 +336,8 @@ __global__ void __launch_bounds__(256) brdf_lut_kernel(float2* __restrict__ out,
     float cos_t = sqrtf((1.0f - xi_y) / (1.0f + (a2 - 1.0f) * xi_y));
     float sin_t = sqrtf(1.0f - cos_t * cos_t);
     float hx = sin_t * agb_cos(phi), hz = cos_t;
-    float vdh = vx * hx + vz * hz;
-    float lz = 2.0f * vdh * hz - vz;
-    float nol = lz > 0.0f ? (lz < 1.0f ? lz : 1.0f) : 0.0f;
     float noh = hz > 0.0f ? (hz < 1.0f ? hz : 1.0f) : 0.0f;
-    float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
-    const float rnoh = 1.0f / noh;
-    if (nol > 0.0f) {
-      float g1l = nol / (nol * (1.0f - k) + k);
-      float g_vis = ((g1l * gv) * voh) * rnoh;
-      float tt = 1.0f - voh;
-      float t2 = tt * tt;
-      float fc = t2 * t2 * tt;
-      sum_a += (1.0f - fc) * g_vis;
-      sum_b += fc * g_vis;
-    }
+    agb_lut_sample(vx, vz, hx, hz, 1.0f / noh, 1.0f - k, k, gv, &sum_a, &sum_b);
   }
   out[(long long)j * pitch + i] = make_float2(sum_a / (float)samples, sum_b / (float)samples);
 }
@@ -389,23 +376,11 @@ __global__ void __launch_bounds__(256) brdf_lut_row_kernel(float2* __restrict__ 
   // G1(V) / NoV once per texel; 1 / NoH comes with the sample
   const float gv = 1.0f / (nov * (1.0f - k) + k);
   float sum_a = 0.0f, sum_b = 0.0f;
+  const float omk = 1.0f - k;
 #pragma unroll 4
   for (int s = 0; s < samples; ++s) {
     const float4 hv = hsamp[s];
-    float hx = hv.x, hz = hv.y;
-    float vdh = vx * hx + vz * hz;
-    float lz = 2.0f * vdh * hz - vz;
-    float nol = lz > 0.0f ? (lz < 1.0f ? lz : 1.0f) : 0.0f;
-    float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
-    if (nol > 0.0f) {
-      float g1l = nol / (nol * (1.0f - k) + k);
-      float g_vis = ((g1l * gv) * voh) * hv.z;
-      float tt = 1.0f - voh;
-      float t2 = tt * tt;
-      float fc = t2 * t2 * tt;
-      sum_a += (1.0f - fc) * g_vis;
-      sum_b += fc * g_vis;
-    }
+    agb_lut_sample(vx, vz, hv.x, hv.y, hv.z, omk, k, gv, &sum_a, &sum_b);
   }
   out[(long long)j * pitch + i] = make_float2(sum_a / (float)samples, sum_b / (float)samples);
 }

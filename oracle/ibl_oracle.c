@@ -432,21 +432,9 @@ static void lut_texel_f32(int i, int j, int n, int samples, int orientation,
     float cos_t = sqrtf((1.0f - xi_y) / (1.0f + (a2 - 1.0f) * xi_y));
     float sin_t = sqrtf(1.0f - cos_t * cos_t);
     float hx = sin_t * agb_cos(phi), hz = cos_t;
-    float vdh = vx * hx + vz * hz; /* V.y = 0 */
-    float lz = 2.0f * vdh * hz - vz;
-    float nol = lz > 0.0f ? (lz < 1.0f ? lz : 1.0f) : 0.0f;
     float noh = hz > 0.0f ? (hz < 1.0f ? hz : 1.0f) : 0.0f;
-    float voh = vdh > 0.0f ? (vdh < 1.0f ? vdh : 1.0f) : 0.0f;
-    float rnoh = 1.0f / noh;
-    if (nol > 0.0f) {
-      float g1l = nol / (nol * (1.0f - k) + k);
-      float g_vis = ((g1l * gv) * voh) * rnoh;
-      float t = 1.0f - voh;
-      float t2 = t * t;
-      float fc = t2 * t2 * t;
-      sum_a += (1.0f - fc) * g_vis;
-      sum_b += fc * g_vis;
-    }
+    /* V.y = 0; the sample's terms as the LUT kernels compute them */
+    agb_lut_sample(vx, vz, hx, hz, 1.0f / noh, 1.0f - k, k, gv, &sum_a, &sum_b);
   }
   out[0] = sum_a / (float)samples;
   out[1] = sum_b / (float)samples;
